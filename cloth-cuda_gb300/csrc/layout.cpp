@@ -1,0 +1,259 @@
+// Host-side construction of the device layout: Morton reorder of every
+// cloth, cut into patches, local triangle/hinge records with 16-bit vertex
+// references, and per-vertex gather lists (CSR) over contribution slots.
+#include "pdg_solver.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace pdg {
+
+namespace {
+
+uint32_t spread10(uint32_t v)
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// Vertex order along the Z-order curve of the rest positions (one cube
+// spanning the bounding box, 10 bits per axis); ties keep input order.
+void morton_order(const MeshData& m, std::vector<int>& perm)
+{
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = 0; i < m.N; ++i)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], m.rest[3 * i + d]);
+            hi[d] = std::max(hi[d], m.rest[3 * i + d]);
+        }
+    float ext = 0.f;
+    for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
+    const float sc = ext > 0.f ? 1023.f / ext : 0.f;
+    std::vector<uint64_t> key(m.N);
+    for (int i = 0; i < m.N; ++i) {
+        uint32_t q[3];
+        for (int d = 0; d < 3; ++d) {
+            const float f = (m.rest[3 * i + d] - lo[d]) * sc;
+            q[d] = (uint32_t)std::min(1023.f, std::max(0.f, f));
+        }
+        const uint32_t code = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+        key[i] = ((uint64_t)code << 32) | (uint32_t)i;
+    }
+    std::sort(key.begin(), key.end());
+    perm.resize(m.N);
+    for (int i = 0; i < m.N; ++i) perm[i] = (int)(key[i] & 0xffffffffu);
+}
+
+}  // namespace
+
+bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout& L, std::string& err)
+{
+    L = HostLayout();
+    const int C = (int)cl.size();
+    L.ncloth = C;
+    int ntot = 0;
+    for (const auto& c : cl) ntot += c.mesh->N;
+    L.ntot = ntot;
+    L.perm_global.resize(ntot);
+    L.perm_local.resize(ntot);
+    L.vcloth.resize(ntot);
+    L.mass.resize(ntot);
+    L.aux.resize(ntot);
+    L.cinfo.resize(C);
+    L.cap = 0;
+    for (const auto& c : cl) L.cap = std::max(L.cap, c.cfg.max_iterations);
+    L.omega.assign((size_t)C * std::max(1, L.cap), 1.f);
+    L.omega_stride = std::max(1, L.cap);
+
+    int vbase = 0;
+    for (int ci = 0; ci < C; ++ci) {
+        const MeshData& m = *cl[ci].mesh;
+        const Topology& tp = *cl[ci].topo;
+        const ConstraintData& cd = cl[ci].cons;
+        const pdg_config& cfg = cl[ci].cfg;
+        const int N = m.N, T = m.T, E = (int)cd.bend_k.size();
+        std::vector<int> perm, iperm(N);
+        morton_order(m, perm);
+        for (int i = 0; i < N; ++i) iperm[perm[i]] = i;
+
+        std::vector<float> diag;
+        jacobi_diag(m, cd, cfg.dt, diag);
+        std::vector<int> pin_slot(N, -1);
+        for (size_t q = 0; q < cd.pins.size(); ++q) pin_slot[cd.pins[q]] = (int)q;
+        for (int i = 0; i < N; ++i) {
+            const int o = perm[i], g = vbase + i;
+            L.perm_global[g] = vbase + o;
+            L.perm_local[g] = o;
+            L.vcloth[g] = ci;
+            L.mass[g] = m.mass[o];
+            const float dg = diag[o];
+            if (pin_slot[o] >= 0) {
+                const int q = pin_slot[o];
+                L.aux[g] = make_float4(cd.targets[3 * q], cd.targets[3 * q + 1], cd.targets[3 * q + 2], -1.f);
+            } else {
+                L.aux[g] = make_float4(0.f, 0.f, 0.f, dg > 1e-10f ? 1.0f / dg : 0.f);
+            }
+        }
+
+        ClothInfo info{};
+        info.vbegin = vbase;
+        info.nverts = N;
+        info.patch_begin = (int)L.patches.size();
+        info.max_iter = cfg.max_iterations;
+        info.use_cheb = cfg.use_chebyshev;
+        info.cheb_delay = cfg.cheb_delay;
+        info.mode = cfg.mode;
+        info.init = cfg.mode == PDG_MODE_REFERENCE_LITERAL ? PDG_INIT_PREVIOUS : cfg.init;
+        info.h = cfg.dt;
+        info.damping = cfg.damping;
+        info.gamma = cfg.gamma;
+        info.tol = cfg.mode == PDG_MODE_REFERENCE_LITERAL ? 0.f : cfg.tolerance;
+        info.rho = cfg.rho;
+        info.ext[0] = cfg.wind[0];
+        info.ext[1] = cfg.gravity + cfg.wind[1];
+        info.ext[2] = cfg.wind[2];
+        // Chebyshev weights omega_k of sweep k (DESIGN of the reference,
+        // omega_1 = 1, omega_2 = 2/(2 - rho^2), omega_k+1 = 4/(4 - rho^2 omega_k))
+        {
+            float om = 1.f;
+            const float r2 = cfg.rho * cfg.rho;
+            for (int k = 0; k < cfg.max_iterations; ++k) {
+                if (!cfg.use_chebyshev || cfg.mode == PDG_MODE_REFERENCE_LITERAL || k < cfg.cheb_delay) om = 1.f;
+                else if (k == cfg.cheb_delay) om = 2.f / (2.f - r2);
+                else om = 4.f / (4.f - r2 * om);
+                L.omega[(size_t)ci * L.omega_stride + k] = om;
+            }
+        }
+
+        // vertex -> hinge lists
+        std::vector<int> vh_ptr(N + 1, 0), vh(4 * (size_t)E);
+        for (int e = 0; e < E; ++e)
+            for (int a = 0; a < 4; ++a) vh_ptr[cd.quads[4 * e + a] + 1]++;
+        for (int i = 0; i < N; ++i) vh_ptr[i + 1] += vh_ptr[i];
+        {
+            std::vector<int> f(vh_ptr.begin(), vh_ptr.end() - 1);
+            for (int e = 0; e < E; ++e)
+                for (int a = 0; a < 4; ++a) vh[f[cd.quads[4 * e + a]]++] = e;
+        }
+
+        std::vector<int> tmark(T, -1), hmark(E, -1), vmark(N, -1), vloc(N, 0);
+        std::vector<int> ltri, lhin, halo, cnt;
+        const float h2 = cfg.dt * cfg.dt;
+        for (int p0 = 0; p0 < N; p0 += patch_verts) {
+            const int p1 = std::min(N, p0 + patch_verts);
+            const int nown = p1 - p0;
+            const int stamp = (int)L.patches.size();
+            ltri.clear(); lhin.clear(); halo.clear();
+            for (int l = 0; l < nown; ++l) {
+                const int o = perm[p0 + l];
+                for (int q = tp.vt_ptr[o]; q < tp.vt_ptr[o + 1]; ++q) {
+                    const int t = tp.vt[q];
+                    if (tmark[t] != stamp) { tmark[t] = stamp; ltri.push_back(t); }
+                }
+                for (int q = vh_ptr[o]; q < vh_ptr[o + 1]; ++q) {
+                    const int e = vh[q];
+                    if (hmark[e] != stamp) { hmark[e] = stamp; lhin.push_back(e); }
+                }
+            }
+            std::sort(ltri.begin(), ltri.end());
+            std::sort(lhin.begin(), lhin.end());
+            auto touch = [&](int o) {
+                const int n = iperm[o];
+                if (n >= p0 && n < p1) return;
+                if (vmark[n] != stamp) { vmark[n] = stamp; halo.push_back(n); }
+            };
+            for (int t : ltri)
+                for (int a = 0; a < 3; ++a) touch(m.tris[3 * t + a]);
+            for (int e : lhin)
+                for (int a = 0; a < 4; ++a) touch(cd.quads[4 * e + a]);
+            std::sort(halo.begin(), halo.end());
+            for (int l = 0; l < nown; ++l) vloc[p0 + l] = l;
+            for (size_t q = 0; q < halo.size(); ++q) vloc[halo[q]] = nown + (int)q;
+            const int nlocal = nown + (int)halo.size();
+            const int ntri = (int)ltri.size(), nhin = (int)lhin.size();
+            const int nslot = 3 * ntri + 4 * nhin;
+            if (nlocal > 65535 || nslot > 65535) {
+                err = "patch too large for 16-bit local indices; lower patch_verts";
+                return false;
+            }
+            PatchHdr ph{};
+            ph.cloth = ci;
+            ph.vbegin = vbase + p0;
+            ph.nown = nown;
+            ph.nlocal = nlocal;
+            ph.halo_off = (int)L.halo.size();
+            ph.tri_off = (int)L.tris.size();
+            ph.ntri = ntri;
+            ph.hinge_off = (int)L.hinges.size();
+            ph.nhinge = nhin;
+            ph.csr_off = (int)L.csr_ptr.size();
+            ph.ent_off = (int)L.csr_ent.size();
+            ph.nslot = nslot;
+            for (int n : halo) L.halo.push_back(vbase + n);
+            auto loc = [&](int o) { return (uint32_t)vloc[iperm[o]]; };
+            for (int t : ltri) {
+                TriRec r{};
+                const float* G = &m.Dm_inv[4 * t];
+                r.G = make_float4(G[0], G[1], G[2], G[3]);
+                const float k = t < (int)cd.k_stretch.size() ? cd.k_stretch[t] : 0.f;
+                r.h2wA = h2 * (k * m.area[t]);
+                r.l01 = loc(m.tris[3 * t]) | (loc(m.tris[3 * t + 1]) << 16);
+                r.l2 = loc(m.tris[3 * t + 2]);
+                L.tris.push_back(r);
+            }
+            for (int e : lhin) {
+                HingeRec r{};
+                r.w = make_float4(cd.w[4 * e], cd.w[4 * e + 1], cd.w[4 * e + 2], cd.w[4 * e + 3]);
+                r.h2k = h2 * cd.bend_k[e];
+                r.nrest = cd.n_rest[e];
+                r.l01 = loc(cd.quads[4 * e]) | (loc(cd.quads[4 * e + 1]) << 16);
+                r.l23 = loc(cd.quads[4 * e + 2]) | (loc(cd.quads[4 * e + 3]) << 16);
+                L.hinges.push_back(r);
+            }
+            // gather lists: owned vertex l sums the slots of its corners in
+            // triangle order, then hinge order
+            cnt.assign(nown + 1, 0);
+            for (int lt = 0; lt < ntri; ++lt)
+                for (int a = 0; a < 3; ++a) {
+                    const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
+                    if (l < nown) cnt[l + 1]++;
+                }
+            for (int lh = 0; lh < nhin; ++lh)
+                for (int a = 0; a < 4; ++a) {
+                    const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
+                    if (l < nown) cnt[l + 1]++;
+                }
+            for (int l = 0; l < nown; ++l) cnt[l + 1] += cnt[l];
+            const size_t e0 = L.csr_ent.size();
+            L.csr_ent.resize(e0 + cnt[nown]);
+            for (int l = 0; l <= nown; ++l) L.csr_ptr.push_back(cnt[l]);
+            std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+            for (int lt = 0; lt < ntri; ++lt)
+                for (int a = 0; a < 3; ++a) {
+                    const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
+                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * lt + a);
+                }
+            for (int lh = 0; lh < nhin; ++lh)
+                for (int a = 0; a < 4; ++a) {
+                    const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
+                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + 4 * lh + a);
+                }
+            L.max_nlocal = std::max(L.max_nlocal, nlocal);
+            L.max_nslot = std::max(L.max_nslot, nslot);
+            L.patches.push_back(ph);
+        }
+        info.patch_end = (int)L.patches.size();
+        L.cinfo[ci] = info;
+        vbase += N;
+    }
+    L.npatch = (int)L.patches.size();
+    L.smem_bytes = 16 * (size_t)L.max_nlocal + 12 * (size_t)L.max_nslot;
+    return true;
+}
+
+}  // namespace pdg

@@ -1,0 +1,186 @@
+// Kernels of the PD cloth solve (sm_103a).
+//
+// One frame (src/pd_solver.cu:496-621, re-designed):
+//   k_predict     y = x + h v + h^2 a; x^0 and x^-1 set to the start iterate
+//   k_iter  x K   one fused local+global sweep per launch: each block stages
+//                 its patch's positions in shared memory, projects every
+//                 triangle (closed-form polar) and hinge, writes per-corner
+//                 contributions to shared slots, then every owned vertex
+//                 gathers its slots in a fixed order (no atomics, bitwise
+//                 deterministic), forms the Jacobi update with the Chebyshev
+//                 blend and adds its residual to a per-cloth sum.
+//   k_finalize    v = (x^K - x_n)(1 - damping)/h, x = x^K, pins re-applied
+//   k_frame_stats per-cloth bookkeeping of the frame
+#include "pd_kernels.cuh"
+#include "pdg_kernels.h"
+
+#include <cmath>
+
+namespace pdg {
+
+template <int MODE, int NT>
+__global__ void __launch_bounds__(NT) k_iter(IterArgs a, int k, int res_only)
+{
+    extern __shared__ float4 smem[];
+    __shared__ PatchHdr ph;
+    __shared__ float red[NT / 32];
+    __shared__ int skip;
+    __shared__ float omega;
+    if (threadIdx.x == 0) {
+        ph = a.patches[blockIdx.x];
+        const int c = ph.cloth;
+        const ClothInfo& ci = a.cinfo[c];
+        skip = cloth_done(a, c, k, (int)blockIdx.x == ci.patch_begin) ? 1 : 0;
+        omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
+    }
+    // the residual slot of sweep k+1 is zeroed here (it was last read at k-1)
+    if (blockIdx.x == 0)
+        for (int c = threadIdx.x; c < a.ncloth; c += NT) a.crt[c].acc[(k + 1) % 3] = 0.0;
+    __syncthreads();
+    if (skip) return;
+    float4* sx = smem;
+    float* cx = reinterpret_cast<float*>(sx + ph.nlocal);
+    float* cy = cx + ph.nslot;
+    float* cz = cy + ph.nslot;
+    process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, omega, sx, cx, cy, cz, red);
+}
+
+__global__ void k_predict(const float4* __restrict__ X, const float4* __restrict__ V,
+                          const float4* __restrict__ aux, const float* __restrict__ mass,
+                          const int* __restrict__ vcloth, const ClothInfo* __restrict__ cinfo,
+                          const float4* __restrict__ warm, float4* __restrict__ Y,
+                          float4* __restrict__ A, float4* __restrict__ B, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) predict_vertex(i, X, V, aux, mass, vcloth, cinfo, warm, Y, A, B);
+}
+
+__global__ void k_reset_rt(ClothRT* crt, int ncloth)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncloth) reset_rt(crt, c);
+}
+
+__global__ void k_frame_stats(const ClothInfo* __restrict__ cinfo, ClothRT* crt, int ncloth, int have_final)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncloth) frame_stats_cloth(cinfo, crt, c, have_final);
+}
+
+__global__ void k_finalize(float4* __restrict__ X, float4* __restrict__ V, const float4* __restrict__ A,
+                           const float4* __restrict__ B, const float4* __restrict__ aux,
+                           const int* __restrict__ vcloth, const ClothInfo* __restrict__ cinfo,
+                           const ClothRT* __restrict__ crt, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) finalize_vertex(i, X, V, A, B, aux, vcloth, cinfo, crt);
+}
+
+// AoS xyz (caller order, cloth by cloth) <-> float4 reordered.
+__global__ void k_scatter_state(const float* __restrict__ src, float4* __restrict__ dst,
+                                const int* __restrict__ perm_global, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int o = perm_global[i];
+    dst[i] = make_float4(src[3 * o], src[3 * o + 1], src[3 * o + 2], 0.f);
+}
+
+__global__ void k_gather_state(const float4* __restrict__ src, float* __restrict__ dst,
+                               const int* __restrict__ perm_global, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int o = perm_global[i];
+    const float4 v = src[i];
+    dst[3 * o] = v.x; dst[3 * o + 1] = v.y; dst[3 * o + 2] = v.z;
+}
+
+// apply_constraints_kernel (src/pd_solver.cu:414-428) on AoS device arrays.
+__global__ void k_apply_pins(float* __restrict__ pos, float* __restrict__ vel, const int* __restrict__ idx,
+                             const float* __restrict__ target, int P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const int v = idx[i];
+    pos[3 * v] = target[3 * i]; pos[3 * v + 1] = target[3 * i + 1]; pos[3 * v + 2] = target[3 * i + 2];
+    if (vel) { vel[3 * v] = 0.f; vel[3 * v + 1] = 0.f; vel[3 * v + 2] = 0.f; }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+template <int MODE, int NT>
+static cudaError_t launch_iter_t(const IterArgs& a, int npatch, size_t smem, int k, int res_only, cudaStream_t s)
+{
+    static bool attr_set = false;   // per template instance
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_iter<MODE, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    k_iter<MODE, NT><<<npatch, NT, smem, s>>>(a, k, res_only);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_iter(const IterArgs& a, int mode, int nt, int npatch, size_t smem, int k, int res_only,
+                        cudaStream_t s)
+{
+    if (mode == kModeConsistent) {
+        switch (nt) {
+            case 128: return launch_iter_t<kModeConsistent, 128>(a, npatch, smem, k, res_only, s);
+            case 256: return launch_iter_t<kModeConsistent, 256>(a, npatch, smem, k, res_only, s);
+            case 512: return launch_iter_t<kModeConsistent, 512>(a, npatch, smem, k, res_only, s);
+        }
+    } else {
+        switch (nt) {
+            case 128: return launch_iter_t<kModeLiteral, 128>(a, npatch, smem, k, res_only, s);
+            case 256: return launch_iter_t<kModeLiteral, 256>(a, npatch, smem, k, res_only, s);
+            case 512: return launch_iter_t<kModeLiteral, 512>(a, npatch, smem, k, res_only, s);
+        }
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_predict(const float4* X, const float4* V, const float4* aux, const float* mass,
+                           const int* vcloth, const ClothInfo* cinfo, const float4* warm, float4* Y,
+                           float4* A, float4* B, ClothRT* crt, int n, int ncloth, cudaStream_t s)
+{
+    k_reset_rt<<<nblk(ncloth, 128), 128, 0, s>>>(crt, ncloth);
+    k_predict<<<nblk(n, 256), 256, 0, s>>>(X, V, aux, mass, vcloth, cinfo, warm, Y, A, B, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(float4* X, float4* V, const float4* A, const float4* B, const float4* aux,
+                            const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n, int ncloth,
+                            int have_final, cudaStream_t s)
+{
+    k_frame_stats<<<nblk(ncloth, 128), 128, 0, s>>>(cinfo, crt, ncloth, have_final);
+    k_finalize<<<nblk(n, 256), 256, 0, s>>>(X, V, A, B, aux, vcloth, cinfo, crt, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_scatter_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, perm, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_gather_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, perm, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P, cudaStream_t s)
+{
+    if (P == 0) return cudaSuccess;
+    k_apply_pins<<<nblk(P, 256), 256, 0, s>>>(pos, vel, idx, target, P);
+    return cudaGetLastError();
+}
+
+}  // namespace pdg

@@ -1,0 +1,46 @@
+// Host-callable launchers of the PD kernels (implemented in *.cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pdg_layout.h"
+
+namespace pdg {
+
+cudaError_t launch_iter(const IterArgs& a, int mode, int nt, int npatch, size_t smem, int k, int res_only,
+                        cudaStream_t s);
+cudaError_t launch_predict(const float4* X, const float4* V, const float4* aux, const float* mass,
+                           const int* vcloth, const ClothInfo* cinfo, const float4* warm, float4* Y,
+                           float4* A, float4* B, ClothRT* crt, int n, int ncloth, cudaStream_t s);
+cudaError_t launch_finalize(float4* X, float4* V, const float4* A, const float4* B, const float4* aux,
+                            const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n, int ncloth,
+                            int have_final, cudaStream_t s);
+cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s);
+cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s);
+cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P,
+                              cudaStream_t s);
+
+// Persistent whole-frame kernel (pd_persistent.cu).
+struct PersistArgs {
+    IterArgs it;
+    const float4* X;
+    float4* Xw;          // state x (written at the end of the frame)
+    float4* V;
+    const float4* aux;
+    const float* mass;
+    const int* vcloth;
+    const float4* warm;
+    float4* Y;
+    int n;               // vertices
+    int npatch;
+    int max_iter;        // largest cap over cloths
+    int have_final;      // evaluate r(x) of the returned iterate
+    int mode;
+    unsigned* bar;       // [0] arrive counter, [1] generation
+    int* err;            // set when a grid barrier times out
+    long long spin_budget;  // clock64 cycles a barrier may wait
+};
+cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s);
+int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
+
+}  // namespace pdg

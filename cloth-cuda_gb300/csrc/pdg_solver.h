@@ -1,0 +1,100 @@
+// Internal solver object of the PD cloth library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/pdg.h"
+#include "pdg_host.h"
+#include "pdg_kernels.h"
+#include "pdg_layout.h"
+
+namespace pdg {
+
+struct ClothSetup {
+    std::shared_ptr<const MeshData> mesh;
+    std::shared_ptr<const Topology> topo;
+    ConstraintData cons;
+    pdg_config cfg;
+};
+
+struct HostLayout {
+    int ntot = 0, ncloth = 0, npatch = 0, cap = 0, omega_stride = 1;
+    int max_nlocal = 0, max_nslot = 0;
+    size_t smem_bytes = 0;
+    std::vector<int> perm_global;   // reordered vertex -> index in the batch's caller order
+    std::vector<int> perm_local;    // reordered vertex -> index within its cloth
+    std::vector<int> vcloth;
+    std::vector<float> mass;
+    std::vector<float4> aux;
+    std::vector<ClothInfo> cinfo;
+    std::vector<float> omega;
+    std::vector<PatchHdr> patches;
+    std::vector<int> halo;
+    std::vector<TriRec> tris;
+    std::vector<HingeRec> hinges;
+    std::vector<int> csr_ptr;
+    std::vector<uint16_t> csr_ent;
+};
+
+bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout& L, std::string& err);
+
+// Owning device allocation.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t count)
+    {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = count;
+        return cudaMalloc(&p, sizeof(T) * (count ? count : 1));
+    }
+    cudaError_t upload(const std::vector<T>& h, cudaStream_t s)
+    {
+        cudaError_t e = alloc(h.size());
+        if (e != cudaSuccess || h.empty()) return e;
+        return cudaMemcpyAsync(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s);
+    }
+};
+
+}  // namespace pdg
+
+struct pdg_solver {
+    std::vector<pdg::ClothSetup> cloths;
+    pdg::HostLayout L;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int kernel = PDG_KERNEL_GRAPH;
+    int patch_verts = 256;
+    int nt = 256;
+    int mode = PDG_MODE_CONSISTENT;
+    int have_final = 1;
+    int persist_grid = 0;
+    long long launches = 0;
+    int kernels_per_frame = 0;
+
+    pdg::DevBuf<float4> X, V, Y, A, B, aux, warm;
+    pdg::DevBuf<float> mass, omega, stage_x, stage_v;
+    pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, err;
+    pdg::DevBuf<uint16_t> csr_ent;
+    pdg::DevBuf<pdg::PatchHdr> patches;
+    pdg::DevBuf<pdg::TriRec> tris;
+    pdg::DevBuf<pdg::HingeRec> hinges;
+    pdg::DevBuf<pdg::ClothInfo> cinfo;
+    pdg::DevBuf<pdg::ClothRT> crt;
+    pdg::DevBuf<unsigned> bar;
+
+    cudaGraphExec_t graph = nullptr;
+    std::vector<pdg::ClothRT> h_rt;
+    bool warm_valid = false;
+
+    ~pdg_solver();
+};

@@ -1,0 +1,480 @@
+// Solver lifecycle and per-frame orchestration (PDSolver, src/pd_solver.cu:445-621,
+// re-designed): layout upload, CUDA-graph or persistent frame, state I/O.
+#include "pdg_solver.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+using namespace pdg;
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return set_error(e_ == cudaErrorMemoryAllocation ? PDG_ERR_ALLOC : PDG_ERR_CUDA,  \
+                             "%s failed: %s", #call, cudaGetErrorString(e_));                 \
+    } while (0)
+
+pdg_solver::~pdg_solver()
+{
+    if (graph) cudaGraphExecDestroy(graph);
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+namespace {
+
+int check_cfg(const pdg_config& c, int i)
+{
+    if (c.max_iterations < 0 || c.max_iterations > 100000)
+        return set_error(PDG_ERR_ARG, "cloth %d: max_iterations out of range", i);
+    if (!(c.dt > 0.f) || !std::isfinite(c.dt)) return set_error(PDG_ERR_ARG, "cloth %d: dt must be > 0", i);
+    if (!(c.damping >= 0.f && c.damping <= 1.f)) return set_error(PDG_ERR_ARG, "cloth %d: damping must be in [0, 1]", i);
+    if (c.use_chebyshev && !(c.rho >= 0.f && c.rho < 1.f))
+        return set_error(PDG_ERR_ARG, "cloth %d: rho must be in [0, 1)", i);
+    if (!(c.gamma > 0.f && c.gamma <= 2.f)) return set_error(PDG_ERR_ARG, "cloth %d: gamma must be in (0, 2]", i);
+    if (c.cheb_delay < 0) return set_error(PDG_ERR_ARG, "cloth %d: cheb_delay must be >= 0", i);
+    if (c.mode != PDG_MODE_CONSISTENT && c.mode != PDG_MODE_REFERENCE_LITERAL)
+        return set_error(PDG_ERR_ARG, "cloth %d: unknown mode", i);
+    if (c.init < 0 || c.init > 2) return set_error(PDG_ERR_ARG, "cloth %d: unknown init", i);
+    if (!std::isfinite(c.gravity) || !std::isfinite(c.wind[0]) || !std::isfinite(c.wind[1]) || !std::isfinite(c.wind[2]))
+        return set_error(PDG_ERR_ARG, "cloth %d: non-finite acceleration", i);
+    return PDG_OK;
+}
+
+int upload_all(pdg_solver* s)
+{
+    const HostLayout& L = s->L;
+    cudaStream_t st = s->stream;
+    CK(s->aux.upload(L.aux, st));
+    CK(s->mass.upload(L.mass, st));
+    CK(s->omega.upload(L.omega, st));
+    CK(s->vcloth.upload(L.vcloth, st));
+    CK(s->perm_global.upload(L.perm_global, st));
+    CK(s->perm_local.upload(L.perm_local, st));
+    CK(s->halo.upload(L.halo, st));
+    CK(s->csr_ptr.upload(L.csr_ptr, st));
+    CK(s->csr_ent.upload(L.csr_ent, st));
+    CK(s->patches.upload(L.patches, st));
+    CK(s->tris.upload(L.tris, st));
+    CK(s->hinges.upload(L.hinges, st));
+    CK(s->cinfo.upload(L.cinfo, st));
+    CK(s->crt.alloc(L.ncloth));
+    CK(s->X.alloc(L.ntot)); CK(s->V.alloc(L.ntot)); CK(s->Y.alloc(L.ntot));
+    CK(s->A.alloc(L.ntot)); CK(s->B.alloc(L.ntot));
+    CK(s->stage_x.alloc(3 * (size_t)L.ntot)); CK(s->stage_v.alloc(3 * (size_t)L.ntot));
+    CK(s->bar.alloc(2)); CK(s->err.alloc(1));
+    CK(cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(s->err.p, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(s->crt.p, 0, sizeof(ClothRT) * L.ncloth, st));
+    CK(cudaMemsetAsync(s->Y.p, 0, sizeof(float4) * L.ntot, st));
+    CK(cudaMemsetAsync(s->V.p, 0, sizeof(float4) * L.ntot, st));
+    // x = rest positions (ClothMesh::upload_to_gpu, src/cloth_mesh.cpp:44-55)
+    std::vector<float> rest(3 * (size_t)L.ntot);
+    size_t off = 0;
+    for (const auto& c : s->cloths) {
+        std::memcpy(rest.data() + off, c.mesh->rest.data(), sizeof(float) * c.mesh->rest.size());
+        off += c.mesh->rest.size();
+    }
+    CK(cudaMemcpyAsync(s->stage_x.p, rest.data(), sizeof(float) * rest.size(), cudaMemcpyHostToDevice, st));
+    CK(launch_scatter_state(s->stage_x.p, s->X.p, s->perm_global.p, L.ntot, st));
+    CK(cudaStreamSynchronize(st));
+    return PDG_OK;
+}
+
+IterArgs iter_args(pdg_solver* s)
+{
+    IterArgs a;
+    a.patches = s->patches.p; a.halo = s->halo.p; a.tris = s->tris.p; a.hinges = s->hinges.p;
+    a.csr_ptr = s->csr_ptr.p; a.csr_ent = s->csr_ent.p; a.cinfo = s->cinfo.p; a.crt = s->crt.p;
+    a.omega = s->omega.p; a.omega_stride = s->L.omega_stride;
+    a.Y = s->Y.p; a.buf[0] = s->A.p; a.buf[1] = s->B.p; a.ncloth = s->L.ncloth;
+    a.have_final = s->have_final;
+    return a;
+}
+
+PersistArgs persist_args(pdg_solver* s)
+{
+    PersistArgs p;
+    p.it = iter_args(s);
+    p.X = s->X.p; p.Xw = s->X.p; p.V = s->V.p; p.aux = s->aux.p; p.mass = s->mass.p; p.vcloth = s->vcloth.p;
+    p.warm = s->warm_valid ? s->warm.p : nullptr; p.Y = s->Y.p;
+    p.n = s->L.ntot; p.npatch = s->L.npatch; p.max_iter = s->L.cap; p.have_final = s->have_final;
+    p.mode = s->mode; p.bar = s->bar.p; p.err = s->err.p;
+    p.spin_budget = 2000000000LL;   // ~1 s at 2 GHz per barrier
+    return p;
+}
+
+// One frame as a sequence of stream-ordered launches.
+int enqueue_frame(pdg_solver* s)
+{
+    const HostLayout& L = s->L;
+    cudaStream_t st = s->stream;
+    CK(launch_predict(s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, s->cinfo.p,
+                      s->warm_valid ? s->warm.p : nullptr, s->Y.p, s->A.p, s->B.p, s->crt.p, L.ntot, L.ncloth, st));
+    const IterArgs a = iter_args(s);
+    for (int k = 0; k < L.cap; ++k) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st));
+    if (s->have_final) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st));
+    CK(launch_finalize(s->X.p, s->V.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p, L.ntot,
+                       L.ncloth, s->have_final, st));
+    return PDG_OK;
+}
+
+int build_graph(pdg_solver* s)
+{
+    if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_frame(s);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (rc != PDG_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return set_error(PDG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    const cudaError_t e2 = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return set_error(PDG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e2));
+    return PDG_OK;
+}
+
+int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                void* stream, pdg_solver** out)
+{
+    if (!out || n <= 0 || !cfgs || !meshes || !cons) return set_error(PDG_ERR_ARG, "solver create: bad arguments");
+    std::unique_ptr<pdg_solver> s(new pdg_solver);
+    for (int i = 0; i < n; ++i) {
+        if (!meshes[i] || !cons[i]) return set_error(PDG_ERR_ARG, "cloth %d: null mesh or constraints", i);
+        if (cons[i]->mesh != meshes[i]->data)
+            return set_error(PDG_ERR_ARG, "cloth %d: constraints were built for another mesh", i);
+        const int rc = check_cfg(cfgs[i], i);
+        if (rc) return rc;
+        if (cfgs[i].mode != cfgs[0].mode) return set_error(PDG_ERR_ARG, "all cloths of a solver share one mode");
+        ClothSetup c;
+        c.mesh = meshes[i]->data;
+        c.topo = cons[i]->topo;
+        c.cons = cons[i]->c;
+        if (c.cons.k_stretch.empty()) c.cons.k_stretch.assign(c.mesh->T, 0.f);  // no stretch data: no stretch term
+        c.cfg = cfgs[i];
+        s->cloths.push_back(std::move(c));
+    }
+    const pdg_config& c0 = cfgs[0];
+    s->mode = c0.mode;
+    s->have_final = (c0.mode == PDG_MODE_CONSISTENT) && (c0.compute_final_residual || c0.tolerance > 0.f);
+    s->nt = c0.block_threads ? c0.block_threads : 256;
+    if (s->nt != 128 && s->nt != 256 && s->nt != 512)
+        return set_error(PDG_ERR_ARG, "block_threads must be 128, 256 or 512");
+    s->patch_verts = c0.patch_verts ? c0.patch_verts : 256;
+    if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
+    s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_GRAPH : c0.kernel;
+
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    int smem_optin = 0;
+    CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    std::string err;
+    for (;;) {
+        if (!build_layout(s->cloths, s->patch_verts, s->L, err)) return set_error(PDG_ERR_ARG, "%s", err.c_str());
+        if (s->L.smem_bytes + 1024 <= (size_t)std::min(smem_optin, 200 * 1024)) break;
+        if (s->patch_verts <= 16) return set_error(PDG_ERR_ARG, "mesh too dense for the shared-memory patch layout");
+        s->patch_verts /= 2;
+    }
+    if (stream) {
+        s->stream = (cudaStream_t)stream;
+    } else {
+        CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        s->own_stream = true;
+    }
+    int rc = upload_all(s.get());
+    if (rc) return rc;
+    s->h_rt.resize(s->L.ncloth);
+    s->kernels_per_frame = 4 + s->L.cap + (s->have_final ? 1 : 0);
+    if (s->kernel == PDG_KERNEL_PERSISTENT) {
+        int per_sm = 0;
+        const int maxb = persistent_max_blocks(s->mode, s->nt, s->L.smem_bytes, &per_sm);
+        if (maxb <= 0)
+            return set_error(PDG_ERR_CUDA, "persistent kernel cannot be resident with %zu B of shared memory",
+                             s->L.smem_bytes);
+        s->persist_grid = std::min(maxb, s->L.npatch);
+    }
+    *out = s.release();
+    return PDG_OK;
+}
+
+int cloth_range(const pdg_solver* s, int cloth, int* vb, int* n)
+{
+    if (!s || cloth < 0 || cloth >= s->L.ncloth) return set_error(PDG_ERR_ARG, "cloth index out of range");
+    *vb = s->L.cinfo[cloth].vbegin;
+    *n = s->L.cinfo[cloth].nverts;
+    return PDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pdg_solver_create(const pdg_config* cfg, const pdg_mesh* m, const pdg_constraints* c, void* stream,
+                      pdg_solver** out)
+{
+    try {
+        if (!cfg) return set_error(PDG_ERR_ARG, "null config");
+        return create_impl(1, cfg, &m, &c, stream, out);
+    } catch (const std::bad_alloc&) {
+        return set_error(PDG_ERR_ALLOC, "host allocation failed");
+    }
+}
+
+int pdg_solver_create_batch(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes,
+                            const pdg_constraints* const* cons, void* stream, pdg_solver** out)
+{
+    try {
+        return create_impl(n, cfgs, meshes, cons, stream, out);
+    } catch (const std::bad_alloc&) {
+        return set_error(PDG_ERR_ALLOC, "host allocation failed");
+    }
+}
+
+int pdg_solver_num_cloths(const pdg_solver* s, int* n)
+{
+    if (!s || !n) return set_error(PDG_ERR_ARG, "bad arguments");
+    *n = s->L.ncloth;
+    return PDG_OK;
+}
+
+int pdg_solver_cloth_counts(const pdg_solver* s, int cloth, int* N, int* T)
+{
+    int vb = 0, n = 0;
+    const int rc = cloth_range(s, cloth, &vb, &n);
+    if (rc) return rc;
+    if (N) *N = n;
+    if (T) *T = s->cloths[cloth].mesh->T;
+    return PDG_OK;
+}
+
+int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
+{
+    if (!s || nframes < 0) return set_error(PDG_ERR_ARG, "pdg_solver_step: bad arguments");
+    for (int f = 0; f < nframes; ++f) {
+        if (s->kernel == PDG_KERNEL_PERSISTENT) {
+            const PersistArgs p = persist_args(s);
+            CK(launch_persistent(p, s->nt, s->persist_grid, s->L.smem_bytes, s->stream));
+            s->launches += 1;
+        } else {
+            if (!s->graph) {
+                const int rc = build_graph(s);
+                if (rc) return rc;
+            }
+            CK(cudaGraphLaunch(s->graph, s->stream));
+            s->launches += s->kernels_per_frame;
+        }
+    }
+    if (stats) {
+        CK(cudaMemcpyAsync(s->h_rt.data(), s->crt.p, sizeof(ClothRT) * s->L.ncloth, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->kernel == PDG_KERNEL_PERSISTENT) {
+            int e = 0;
+            CK(cudaMemcpy(&e, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (e) return set_error(PDG_ERR_TIMEOUT, "grid barrier timed out (code %d)", e);
+        }
+        for (int c = 0; c < s->L.ncloth; ++c) {
+            const ClothRT& r = s->h_rt[c];
+            const ClothInfo& ci = s->L.cinfo[c];
+            pdg_frame_stats& o = stats[c];
+            o.iterations = r.used;
+            o.warm_start_used = r.warm;
+            o.status = r.status;
+            o.res_inertial = std::sqrt(std::max(0.0, r.res_y2));
+            o.res_initial = std::sqrt(std::max(0.0, r.res0_2));
+            o.res_final = r.resf_2 >= 0.0 ? std::sqrt(r.resf_2) : (std::isnan(r.resf_2) ? NAN : -1.0);
+            o.rel_residual = (o.res_final >= 0.0 && o.res_inertial > 0.0) ? o.res_final / o.res_inertial
+                             : (o.res_final == 0.0 ? 0.0 : -1.0);
+            o.converged = (r.status == 0 && ci.tol > 0.f && o.res_final >= 0.0 &&
+                           o.res_final <= (double)ci.tol * o.res_inertial) ? 1 : 0;
+        }
+    }
+    return PDG_OK;
+}
+
+int pdg_solver_reset(pdg_solver* s)
+{
+    // The Chebyshev weights restart every frame; nothing persists between frames.
+    if (!s) return set_error(PDG_ERR_ARG, "null solver");
+    return PDG_OK;
+}
+
+static int set_state_range(pdg_solver* s, int vb, int n, const float* x, const float* v, int on_device, bool whole)
+{
+    const int* perm = whole ? s->perm_global.p : s->perm_local.p + vb;
+    for (int which = 0; which < 2; ++which) {
+        const float* src = which == 0 ? x : v;
+        if (!src) continue;
+        float4* dst = (which == 0 ? s->X.p : s->V.p) + vb;
+        if (!on_device) {
+            float* stage = (which == 0 ? s->stage_x.p : s->stage_v.p);
+            CK(cudaMemcpyAsync(stage, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+            src = stage;
+        }
+        CK(launch_scatter_state(src, dst, perm, n, s->stream));
+    }
+    if (!on_device) CK(cudaStreamSynchronize(s->stream));
+    return PDG_OK;
+}
+
+static int get_state_range(pdg_solver* s, int vb, int n, float* x, float* v, int on_device, bool whole)
+{
+    const int* perm = whole ? s->perm_global.p : s->perm_local.p + vb;
+    for (int which = 0; which < 2; ++which) {
+        float* dstp = which == 0 ? x : v;
+        if (!dstp) continue;
+        const float4* src = (which == 0 ? s->X.p : s->V.p) + vb;
+        float* dst = on_device ? dstp : (which == 0 ? s->stage_x.p : s->stage_v.p);
+        CK(launch_gather_state(src, dst, perm, n, s->stream));
+        if (!on_device)
+            CK(cudaMemcpyAsync(dstp, dst, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (!on_device) CK(cudaStreamSynchronize(s->stream));
+    return PDG_OK;
+}
+
+int pdg_solver_set_state(pdg_solver* s, int cloth, const float* x, const float* v, int on_device)
+{
+    int vb = 0, n = 0;
+    const int rc = cloth_range(s, cloth, &vb, &n);
+    return rc ? rc : set_state_range(s, vb, n, x, v, on_device, false);
+}
+
+int pdg_solver_get_state(pdg_solver* s, int cloth, float* x, float* v, int on_device)
+{
+    int vb = 0, n = 0;
+    const int rc = cloth_range(s, cloth, &vb, &n);
+    return rc ? rc : get_state_range(s, vb, n, x, v, on_device, false);
+}
+
+int pdg_solver_set_state_all(pdg_solver* s, const float* x, const float* v, int on_device)
+{
+    if (!s) return set_error(PDG_ERR_ARG, "null solver");
+    return set_state_range(s, 0, s->L.ntot, x, v, on_device, true);
+}
+
+int pdg_solver_get_state_all(pdg_solver* s, float* x, float* v, int on_device)
+{
+    if (!s) return set_error(PDG_ERR_ARG, "null solver");
+    return get_state_range(s, 0, s->L.ntot, x, v, on_device, true);
+}
+
+int pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets)
+{
+    int vb = 0, n = 0;
+    int rc = cloth_range(s, cloth, &vb, &n);
+    if (rc) return rc;
+    if (!targets) return set_error(PDG_ERR_ARG, "null targets");
+    ClothSetup& c = s->cloths[cloth];
+    const int P = (int)c.cons.pins.size();
+    for (int i = 0; i < 3 * P; ++i)
+        if (!std::isfinite(targets[i])) return set_error(PDG_ERR_ARG, "non-finite pin target");
+    std::memcpy(c.cons.targets.data(), targets, sizeof(float) * 3 * (size_t)P);
+    for (int g = vb; g < vb + n; ++g) {
+        float4& a = s->L.aux[g];
+        if (a.w >= 0.f) continue;
+        const int o = s->L.perm_local[g];
+        for (int q = 0; q < P; ++q)
+            if (c.cons.pins[q] == o) { a.x = targets[3 * q]; a.y = targets[3 * q + 1]; a.z = targets[3 * q + 2]; }
+    }
+    CK(cudaMemcpyAsync(s->aux.p + vb, s->L.aux.data() + vb, sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return PDG_OK;
+}
+
+int pdg_solver_get_prediction(pdg_solver* s, int cloth, float* y)
+{
+    int vb = 0, n = 0;
+    const int rc = cloth_range(s, cloth, &vb, &n);
+    if (rc) return rc;
+    if (!y) return set_error(PDG_ERR_ARG, "null output");
+    CK(launch_gather_state(s->Y.p + vb, s->stage_x.p, s->perm_local.p + vb, n, s->stream));
+    CK(cudaMemcpyAsync(y, s->stage_x.p, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return PDG_OK;
+}
+
+int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* sweep_ms)
+{
+    if (!s || nframes <= 0) return set_error(PDG_ERR_ARG, "pdg_solver_time_frames: bad arguments");
+    cudaEvent_t e[4];
+    for (auto& ev : e) CK(cudaEventCreate(&ev));
+    const HostLayout& L = s->L;
+    cudaStream_t st = s->stream;
+    double tf = 0.0, ts = 0.0;
+    int rc = PDG_OK;
+    for (int f = 0; f < nframes && rc == PDG_OK; ++f) {
+        cudaEventRecord(e[0], st);
+        if (s->kernel == PDG_KERNEL_PERSISTENT) {
+            const PersistArgs p = persist_args(s);
+            cudaError_t err = launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
+            if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "persistent launch: %s", cudaGetErrorString(err));
+            s->launches += 1;
+            cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
+        } else {
+            cudaError_t err = launch_predict(s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, s->cinfo.p,
+                                             s->warm_valid ? s->warm.p : nullptr, s->Y.p, s->A.p, s->B.p, s->crt.p,
+                                             L.ntot, L.ncloth, st);
+            cudaEventRecord(e[1], st);
+            const IterArgs a = iter_args(s);
+            for (int k = 0; k < L.cap && err == cudaSuccess; ++k)
+                err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st);
+            cudaEventRecord(e[2], st);
+            if (err == cudaSuccess && s->have_final) err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st);
+            if (err == cudaSuccess)
+                err = launch_finalize(s->X.p, s->V.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p,
+                                      L.ntot, L.ncloth, s->have_final, st);
+            if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "frame launch: %s", cudaGetErrorString(err));
+            s->launches += s->kernels_per_frame;
+        }
+        cudaEventRecord(e[3], st);
+        cudaError_t se = cudaEventSynchronize(e[3]);
+        if (se != cudaSuccess) { rc = set_error(PDG_ERR_CUDA, "frame: %s", cudaGetErrorString(se)); break; }
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, e[0], e[3]);
+        cudaEventElapsedTime(&b, e[1], e[2]);
+        tf += a;
+        ts += s->kernel == PDG_KERNEL_PERSISTENT ? a : b;
+    }
+    for (auto& ev : e) cudaEventDestroy(ev);
+    if (rc) return rc;
+    if (frame_ms) *frame_ms = (float)(tf / nframes);
+    const int sweeps = std::max(1, L.cap + (s->kernel == PDG_KERNEL_PERSISTENT && s->have_final ? 1 : 0));
+    if (sweep_ms) *sweep_ms = (float)(ts / nframes / sweeps);
+    return PDG_OK;
+}
+
+int pdg_solver_launch_count(const pdg_solver* s, long long* n)
+{
+    if (!s || !n) return set_error(PDG_ERR_ARG, "bad arguments");
+    *n = s->launches;
+    return PDG_OK;
+}
+
+int pdg_solver_stream(const pdg_solver* s, void** stream)
+{
+    if (!s || !stream) return set_error(PDG_ERR_ARG, "bad arguments");
+    *stream = (void*)s->stream;
+    return PDG_OK;
+}
+
+int pdg_solver_launch_info(const pdg_solver* s, int* kernel, int* patch_verts, int* block_threads, int* npatches)
+{
+    if (!s) return set_error(PDG_ERR_ARG, "null solver");
+    if (kernel) *kernel = s->kernel;
+    if (patch_verts) *patch_verts = s->patch_verts;
+    if (block_threads) *block_threads = s->nt;
+    if (npatches) *npatches = s->L.npatch;
+    return PDG_OK;
+}
+
+void pdg_solver_destroy(pdg_solver* s) { delete s; }
+
+int pdg_apply_pins(float* d_pos, float* d_vel, const int* d_idx, const float* d_target, int P, void* stream)
+{
+    if (P < 0 || (P > 0 && (!d_pos || !d_idx || !d_target))) return set_error(PDG_ERR_ARG, "pdg_apply_pins: bad arguments");
+    CK(launch_apply_pins(d_pos, d_vel, d_idx, d_target, P, (cudaStream_t)stream));
+    return PDG_OK;
+}
+
+}  // extern "C"

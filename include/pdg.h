@@ -1,0 +1,213 @@
+/*
+ * pdg.h -- C ABI of the GB300-native projective-dynamics (PD) cloth solver.
+ *
+ * Drop-in boundary for the per-frame solve of Chongyao/cloth-cuda.  Every
+ * entry point takes plain pointers and sizes, returns an int status
+ * (PDG_OK = 0, negative on error; pdg_last_error_string() explains the last
+ * failure on the calling thread) and never exits the process.  The reference
+ * interface each group replaces is cited beside it.
+ *
+ * Vertex arrays crossing this boundary are AoS xyz float32 in the caller's
+ * vertex order.  Internally the solver keeps a Morton-reordered float4 layout;
+ * the permutation never leaves the library.
+ *
+ * Threading: one host thread per handle.  Work is stream-ordered on the
+ * stream given at creation (NULL = the legacy default stream, as in the
+ * reference); host-pointer getters synchronise that stream.
+ */
+#ifndef PDG_H
+#define PDG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PDG_OK              0
+#define PDG_ERR_ARG        -1   /* invalid argument or size                 */
+#define PDG_ERR_CUDA       -2   /* a CUDA call failed                       */
+#define PDG_ERR_ALLOC      -3   /* host or device allocation failed          */
+#define PDG_ERR_STATE      -4   /* call out of order (e.g. no constraints)  */
+#define PDG_ERR_TIMEOUT    -5   /* a bounded device wait gave up             */
+#define PDG_ERR_NUMERIC    -6   /* NaN/Inf detected in the solve             */
+#define PDG_ERR_IO         -7   /* file could not be read                    */
+
+/* Global step of the solve. */
+#define PDG_MODE_CONSISTENT        0  /* x += gamma D^-1 (b - K x), Chebyshev blend */
+#define PDG_MODE_REFERENCE_LITERAL 1  /* x = rhs / diag as src/pd_solver.cu:385-398 */
+
+/* Initial iterate of a frame. */
+#define PDG_INIT_INERTIAL 0   /* y = x + h v + h^2 a, pins at their targets */
+#define PDG_INIT_PREVIOUS 1   /* x_n (what src/pd_solver.cu:528 does)      */
+#define PDG_INIT_WARMSTART 2  /* the learned prediction, kept only if its
+                                 residual is below the inertial start's     */
+
+/* Launch structure of the iteration loop. */
+#define PDG_KERNEL_AUTO       0  /* autotuner picks                         */
+#define PDG_KERNEL_GRAPH      1  /* one fused launch per iteration, frame in a CUDA graph */
+#define PDG_KERNEL_PERSISTENT 2  /* one cooperative launch per frame, bounded grid barrier */
+
+/* Solver configuration.  Mirrors PDSolverConfig (include/pd_solver.h:4-15);
+ * fields after `damping` extend it. */
+typedef struct pdg_config {
+    int   max_iterations;     /* iteration cap per frame (50)                 */
+    float tolerance;          /* relative residual target; <= 0: run the cap  */
+    int   use_chebyshev;      /* Chebyshev blend (1)                          */
+    float rho;                /* spectral-radius estimate (0.9)               */
+    float gravity;            /* acceleration along y (-9.8)                  */
+    float dt;                 /* time step (0.01)                             */
+    float stretch_stiffness;  /* informational, as in the reference (1.0)     */
+    float bend_stiffness;     /* informational, as in the reference (0.0)     */
+    float damping;            /* velocity damping 0..1 (0)                    */
+    /* ---- extensions ---- */
+    float wind[3];            /* constant extra acceleration (0,0,0)          */
+    int   cheb_delay;         /* omega = 1 while k < cheb_delay (1)           */
+    float gamma;              /* under-relaxation of the Jacobi update (1)    */
+    int   mode;               /* PDG_MODE_* (CONSISTENT)                      */
+    int   init;               /* PDG_INIT_* (INERTIAL)                        */
+    int   kernel;             /* PDG_KERNEL_* (AUTO)                          */
+    int   patch_verts;        /* owned vertices per patch, 0 = autotune       */
+    int   block_threads;      /* threads per patch block, 0 = autotune        */
+    int   compute_final_residual; /* evaluate r(x) of the returned iterate (1) */
+} pdg_config;
+
+/* Per-frame statistics (one per cloth). */
+typedef struct pdg_frame_stats {
+    int    iterations;        /* Jacobi sweeps whose result was kept          */
+    int    converged;         /* final relative residual <= tolerance         */
+    int    warm_start_used;   /* learned start kept (1) or discarded (0)      */
+    int    status;            /* PDG_OK or an error code for this cloth       */
+    double res_inertial;      /* ||r(y_pinned)|| over free DOFs               */
+    double res_initial;       /* ||r(x^0)||                                    */
+    double res_final;         /* ||r(x returned)|| (if computed, else -1)     */
+    double rel_residual;      /* res_final / res_inertial                      */
+} pdg_frame_stats;
+
+typedef struct pdg_mesh        pdg_mesh;         /* ClothMesh (include/cloth_mesh.h:18-67)          */
+typedef struct pdg_constraints pdg_constraints;  /* SimConstraints + Constraints                    */
+typedef struct pdg_solver      pdg_solver;       /* PDSolver (include/pd_solver.h:30-71), 1..n cloths */
+typedef struct pdg_warmstart   pdg_warmstart;    /* learned warm start (no reference counterpart)   */
+
+const char* pdg_last_error_string(void);
+const char* pdg_version(void);
+int  pdg_config_default(pdg_config* cfg);
+
+/* ---------------- mesh: include/cloth_mesh.h:18-67 ----------------------- */
+/* ClothMesh::precompute_rest_state (src/cloth_mesh.cpp:138-211) on a caller
+ * mesh: rest_xyz N*3, tris T*3 (0-based). */
+int  pdg_mesh_create(const float* rest_xyz, int N, const int* tris, int T,
+                     float density, pdg_mesh** out);
+/* generate_square_cloth (src/mesh_generator.cpp:6-91): x-z plane, `size` =
+ * cell edge, type 0..3; then precompute_rest_state(density). */
+int  pdg_mesh_generate(int nrows, int ncols, float size, int type,
+                       float density, pdg_mesh** out);
+/* Square cloth hanging in the x-y plane: row 0 on top at y = 0, rows going
+ * down, cell = side/(n-1), z jitter N(0, jitter) from `seed`. */
+int  pdg_mesh_generate_hanging(int nrows, int ncols, float side, int type,
+                               float jitter, unsigned long long seed,
+                               float density, pdg_mesh** out);
+/* ClothMesh::load_obj (src/cloth_mesh.cpp:89-132): v / f records, 1-based,
+ * polygons fan-triangulated. */
+int  pdg_mesh_load_obj(const char* path, float density, pdg_mesh** out);
+int  pdg_mesh_counts(const pdg_mesh* m, int* N, int* T);
+/* Copy out rest positions, triangles, Dm_inv (T*4 col-major), rest area,
+ * lumped mass and dF/dx (T*54, row-major 6x9).  Any pointer may be NULL. */
+int  pdg_mesh_get(const pdg_mesh* m, float* rest_xyz, int* tris, float* Dm_inv,
+                  float* area, float* mass, float* dFdx);
+void pdg_mesh_destroy(pdg_mesh* m);
+
+/* ---------------- topology: MeshTopology::build (src/mesh_topology.cpp:11-97) */
+int  pdg_topology_counts(const pdg_mesh* m, int* num_edges, int* num_inner);
+/* edges: rows (v0, v1, tri_a, tri_b) sorted by (v0, v1), v0 < v1, tri_b = -1
+ * on the boundary; rest_len per edge; vert_tri_ptr N+1 / vert_tri (3T)
+ * vertex->triangle adjacency; tri_tri T*3 neighbour opposite each corner
+ * (-1 if none).  Any pointer may be NULL. */
+int  pdg_topology_get(const pdg_mesh* m, int* edges, float* rest_len,
+                      int* vert_tri_ptr, int* vert_tri, int* tri_tri);
+
+/* ---------------- constraints: SimConstraints (include/sim_constraints.h:30-78)
+ *                  and Constraints (include/constraints.h:5-36) ----------- */
+int  pdg_constraints_create(const pdg_mesh* m, pdg_constraints** out);
+/* SimConstraints::build_stretch (src/sim_constraints.cpp:16-22) */
+int  pdg_constraints_build_stretch(pdg_constraints* c, float stiffness);
+int  pdg_constraints_set_stretch_k(pdg_constraints* c, const float* k_per_tri);
+/* SimConstraints::build_bend (src/sim_constraints.cpp:48-127) */
+int  pdg_constraints_build_bend(pdg_constraints* c, float stiffness);
+/* Constraints::set_from_list / pin_top_row / pin_corners
+ * (src/constraints.cpp:14-41); targets NULL = rest positions. */
+int  pdg_constraints_set_pins(pdg_constraints* c, const int* idx, int P,
+                              const float* targets);
+int  pdg_constraints_pin_top_row(pdg_constraints* c, int ncols);
+int  pdg_constraints_pin_corners(pdg_constraints* c, int ncols);
+int  pdg_constraints_counts(const pdg_constraints* c, int* num_bend, int* num_pins);
+/* Bend hinges (v0,v1,v2,v3), weights w0..w3, rest norm, stiffness; pins and
+ * targets.  Any pointer may be NULL. */
+int  pdg_constraints_get(const pdg_constraints* c, float* stretch_k, int* quads,
+                         float* w, float* n_rest, float* bend_k, int* pins,
+                         float* targets);
+/* SimConstraints::precompute_jacobi_diag (src/sim_constraints.cpp:133-192) */
+int  pdg_constraints_jacobi_diag(const pdg_constraints* c, float dt, float* diag);
+void pdg_constraints_destroy(pdg_constraints* c);
+
+/* ---------------- solver: PDSolver (include/pd_solver.h:30-71) ------------ */
+/* PDSolver::PDSolver (src/pd_solver.cu:445-460).  The mesh and constraints
+ * are copied; they may be destroyed afterwards.  stream = cudaStream_t or
+ * NULL.  Initial state: x = rest positions, v = 0 (ClothMesh::upload_to_gpu,
+ * src/cloth_mesh.cpp:31-83). */
+int  pdg_solver_create(const pdg_config* cfg, const pdg_mesh* m,
+                       const pdg_constraints* c, void* stream, pdg_solver** out);
+/* Many cloths of uneven size in one solver (one persistent launch / graph per
+ * frame).  cfgs: one per cloth (dt, gravity, wind, damping, rho, tolerance,
+ * cap may differ; the launch fields of cfgs[0] apply to all). */
+int  pdg_solver_create_batch(int ncloths, const pdg_config* cfgs,
+                             const pdg_mesh* const* meshes,
+                             const pdg_constraints* const* cons, void* stream,
+                             pdg_solver** out);
+int  pdg_solver_num_cloths(const pdg_solver* s, int* n);
+int  pdg_solver_cloth_counts(const pdg_solver* s, int cloth, int* N, int* T);
+/* PDSolver::step (src/pd_solver.cu:496-621): `nframes` frames.  stats: NULL
+ * or ncloths entries describing the last frame (reading them synchronises). */
+int  pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats);
+/* PDSolver::reset (src/pd_solver.cu:491-494): restart the Chebyshev state. */
+int  pdg_solver_reset(pdg_solver* s);
+/* State of one cloth, AoS xyz float32 in its own vertex order.  x or v may be
+ * NULL.  on_device != 0: pointers are device pointers (stream-ordered copy),
+ * else host pointers (the copy synchronises). */
+int  pdg_solver_set_state(pdg_solver* s, int cloth, const float* x,
+                          const float* v, int on_device);
+int  pdg_solver_get_state(pdg_solver* s, int cloth, float* x, float* v,
+                          int on_device);
+/* Whole batch at once: x, v hold sum(N) vertices, cloths back to back. */
+int  pdg_solver_set_state_all(pdg_solver* s, const float* x, const float* v, int on_device);
+int  pdg_solver_get_state_all(pdg_solver* s, float* x, float* v, int on_device);
+/* Move the pins of one cloth (Constraints::target_positions). */
+int  pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets);
+/* Inertial prediction y of the last frame and the residual r(x) of a given
+ * state against it (host arrays, caller order), for diagnostics/tests. */
+int  pdg_solver_get_prediction(pdg_solver* s, int cloth, float* y);
+/* Kernel launches issued so far (fused iteration, predict, finalize, ...). */
+int  pdg_solver_launch_count(const pdg_solver* s, long long* n);
+/* Measurement helper: runs `nframes` frames as individual launches (no
+ * graph) and times them with CUDA events on the solver's stream.  frame_ms:
+ * average frame; sweep_ms: average duration of one fused sweep (the events
+ * bracket the sweep launches; persistent kernel: frame time / sweeps). */
+int  pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* sweep_ms);
+/* Stream the solver works on (a cudaStream_t). */
+int  pdg_solver_stream(const pdg_solver* s, void** stream);
+/* Launch shape the solver picked: kernel (PDG_KERNEL_*), patch_verts,
+ * block_threads, number of patches. */
+int  pdg_solver_launch_info(const pdg_solver* s, int* kernel, int* patch_verts,
+                            int* block_threads, int* npatches);
+void pdg_solver_destroy(pdg_solver* s);
+
+/* launch_apply_constraints_kernel (include/pd_solver.h:74-77): set
+ * d_pos[idx] = target and d_vel[idx] = 0 for P pinned vertices, AoS xyz
+ * device arrays, on `stream`. */
+int  pdg_apply_pins(float* d_pos, float* d_vel, const int* d_indices,
+                    const float* d_target, int num_pinned, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDG_H */

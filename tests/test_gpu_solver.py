@@ -1,0 +1,214 @@
+"""CUDA solver against the oracle, through the C ABI (GPU).
+
+Tolerances: float32 arithmetic on both sides with different summation
+order; one frame of 10 sweeps agrees to 1e-5 relative in positions (the
+spec bar), and every multi-frame comparison against the float64 oracle
+to 1e-4 relative.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_ONE_FRAME = 1e-5
+REL_F64 = 1e-4
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64).reshape(-1); b = np.asarray(b, np.float64).reshape(-1)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def scene(pdg, oracle, n=33, side=1.0, mtype=1, ks=1e3, kb=1e-2, pins="corners", seed=0, **cfgkw):
+    m = pdg.Mesh.hanging(n, side, mtype=mtype, jitter=1e-4, seed=seed)
+    c = pdg.Constraints(m).build_stretch(ks)
+    if kb > 0:
+        c.build_bend(kb)
+    if pins == "corners":
+        c.pin_corners(n)
+    elif pins == "top":
+        c.pin_top_row(n)
+    kw = dict(max_iterations=10, rho=0.99, dt=1 / 60, gravity=-9.81)
+    kw.update(cfgkw)
+    cfg = pdg.Config.default(**kw)
+    a = m.arrays(); ca = c.arrays()
+    sc = oracle.Scene(a["rest"], a["tris"], k_stretch=ca["k_stretch"], k_bend=kb if kb > 0 else 0.0,
+                      pins=ca["pins"], h=cfg.dt, gravity=cfg.gravity, wind=tuple(cfg.wind), damping=cfg.damping)
+    return m, c, cfg, sc, a
+
+
+def test_one_frame_matches_oracle(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle)
+    s = pdg.Solver(cfg, m, c)
+    st = s.step(1)[0]
+    x, v = s.get_state()
+    x0 = a["rest"]; v0 = np.zeros_like(x0)
+    xo, vo, info = sc.step_jacobi(x0.reshape(-1), v0.reshape(-1), 10, rho=0.99, dtype=np.float32)
+    xd, vd, info64 = sc.step_jacobi(x0.reshape(-1), v0.reshape(-1), 10, rho=0.99, dtype=np.float64)
+    assert rel(x, xo) < REL_ONE_FRAME
+    assert rel(x, xd) < REL_ONE_FRAME
+    assert rel(v, vd) < 1e-3
+    assert st["iterations"] == 10 and st["status"] == 0
+    assert abs(st["res_inertial"] - info64["res_y"]) / info64["res_y"] < 1e-3
+    assert abs(st["res_final"] - info64["res"][-1]) / info64["res"][-1] < 1e-2
+
+
+def test_many_frames_match_f64(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=17, max_iterations=32)
+    s = pdg.Solver(cfg, m, c)
+    x = a["rest"].astype(np.float64).reshape(-1); v = np.zeros_like(x)
+    for f in range(20):
+        s.step(1, stats=False)
+        x, v, _ = sc.step_jacobi(x, v, 32, rho=0.99)
+    xg, vg = s.get_state()
+    assert rel(xg, x) < REL_F64
+    assert rel(vg, v) < 1e-2
+
+
+def test_reference_literal_matches_oracle(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=17, mode=pdg.MODE_REFERENCE_LITERAL)
+    s = pdg.Solver(cfg, m, c)
+    s.step(1, stats=False)
+    x, v = s.get_state()
+    xo, vo = sc.step_literal(a["rest"].reshape(-1), np.zeros(3 * m.N, np.float32), 10)
+    assert rel(x, xo) < REL_ONE_FRAME
+    assert rel(v, vo) < 1e-4
+
+
+@pytest.mark.parametrize("kernel", ["persistent"])
+def test_persistent_equals_graph(pdg, oracle, kernel):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=16)
+    s1 = pdg.Solver(cfg, m, c)
+    cfg2 = pdg.Config.default(**{f: getattr(cfg, f) for f, _ in cfg._fields_ if f != "wind"})
+    cfg2.kernel = pdg.KERNEL_PERSISTENT
+    s2 = pdg.Solver(cfg2, m, c)
+    for _ in range(3):
+        st1 = s1.step(1)[0]
+        st2 = s2.step(1)[0]
+    x1, v1 = s1.get_state(); x2, v2 = s2.get_state()
+    assert np.array_equal(x1, x2) and np.array_equal(v1, v2)
+    assert st1["iterations"] == st2["iterations"]
+    assert s2.launch_info()["kernel"] == pdg.KERNEL_PERSISTENT
+
+
+def test_patch_size_does_not_change_bits(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=33)
+    out = []
+    for pv, nt in [(64, 128), (256, 256), (1024, 512)]:
+        cfg.patch_verts, cfg.block_threads = pv, nt
+        s = pdg.Solver(cfg, m, c)
+        s.step(2, stats=False)
+        out.append(s.get_state())
+    for x, v in out[1:]:
+        assert np.array_equal(x, out[0][0]) and np.array_equal(v, out[0][1])
+
+
+def test_batch_equals_single(pdg, oracle):
+    scenes = [scene(pdg, oracle, n=n, seed=n, ks=k, kb=kb) for n, k, kb in [(9, 1e2, 1e-3), (17, 1e3, 1e-2), (12, 5e3, 0.0)]]
+    singles = []
+    for m, c, cfg, sc, a in scenes:
+        s = pdg.Solver(cfg, m, c)
+        s.step(2, stats=False)
+        singles.append(s.get_state())
+    b = pdg.Solver([sc_[2] for sc_ in scenes], [sc_[0] for sc_ in scenes], [sc_[1] for sc_ in scenes])
+    b.step(2, stats=False)
+    for i, (x, v) in enumerate(singles):
+        xb, vb = b.get_state(i)
+        assert np.array_equal(x, xb) and np.array_equal(v, vb)
+    xa, va = b.get_state_all()
+    assert np.array_equal(xa[b.offsets[1]:b.offsets[2]], singles[1][0])
+
+
+def test_tolerance_mode_stops_like_oracle(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=9, side=0.5, ks=20.0, kb=1e-3, max_iterations=400, tolerance=1e-4,
+                             rho=0.9)
+    s = pdg.Solver(cfg, m, c)
+    st = s.step(1)[0]
+    x0 = a["rest"].astype(np.float64).reshape(-1)
+    xo, vo, info = sc.step_jacobi(x0, np.zeros_like(x0), 400, tol=1e-4, rho=0.9)
+    assert st["converged"] == 1 and st["rel_residual"] <= 1e-4
+    assert abs(st["iterations"] - info["used"]) <= 2
+    x, v = s.get_state()
+    assert rel(x, xo) < 1e-5
+
+
+def test_deterministic(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=33)
+    r = []
+    for _ in range(2):
+        s = pdg.Solver(cfg, m, c)
+        s.step(3, stats=False)
+        r.append(s.get_state())
+    assert np.array_equal(r[0][0], r[1][0]) and np.array_equal(r[0][1], r[1][1])
+
+
+def test_state_roundtrip_and_free_fall(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=9, ks=0.0, kb=0.0, pins="none", max_iterations=5)
+    s = pdg.Solver(cfg, m, c)
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=(m.N, 3)).astype(np.float32); v = rng.normal(size=(m.N, 3)).astype(np.float32)
+    s.set_state(x, v)
+    x2, v2 = s.get_state()
+    assert np.array_equal(x, x2) and np.array_equal(v, v2)
+    s.step(1, stats=False)
+    x3, v3 = s.get_state()
+    h = np.float32(cfg.dt)
+    expect = x + h * v + h * h * np.array([0, cfg.gravity, 0], np.float32)
+    assert np.allclose(x3, expect, rtol=0, atol=1e-6)
+
+
+def test_apply_pins_device(pdg):
+    torch = pytest.importorskip("torch")
+    pos = torch.arange(30, dtype=torch.float32, device="cuda")
+    vel = torch.ones(30, dtype=torch.float32, device="cuda")
+    idx = torch.tensor([1, 7], dtype=torch.int32, device="cuda")
+    tgt = torch.tensor([-1, -2, -3, -4, -5, -6], dtype=torch.float32, device="cuda")
+    import ctypes
+    rc = pdg.lib().pdg_apply_pins(ctypes.c_void_p(pos.data_ptr()), ctypes.c_void_p(vel.data_ptr()),
+                                  ctypes.c_void_p(idx.data_ptr()), ctypes.c_void_p(tgt.data_ptr()), 2, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    p = pos.view(10, 3).cpu().numpy(); v = vel.view(10, 3).cpu().numpy()
+    assert np.array_equal(p[1], [-1, -2, -3]) and np.array_equal(p[7], [-4, -5, -6])
+    assert np.all(v[[1, 7]] == 0) and np.all(v[[0, 2, 3]] == 1)
+
+
+def test_nan_input_is_reported(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=9)
+    s = pdg.Solver(cfg, m, c)
+    x = a["rest"].copy(); x[4, 1] = np.nan
+    s.set_state(x, np.zeros_like(x))
+    st = s.step(1)[0]
+    assert st["status"] == pdg.ERR_NUMERIC
+    x2, v2 = s.get_state()
+    assert np.all(v2[np.isfinite(x2).all(1)] == 0)
+
+
+def test_pin_targets_move(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=9)
+    s = pdg.Solver(cfg, m, c)
+    t = c.arrays()["targets"] + np.array([0.0, 0.1, 0.0], np.float32)
+    s.set_pin_targets(t)
+    s.step(1, stats=False)
+    x, v = s.get_state()
+    assert np.allclose(x[[0, 8]], t) and np.all(v[[0, 8]] == 0)
+
+
+@pytest.mark.parametrize("nr,mtype", [(2, 0), (3, 3), (5, 2)])
+def test_small_and_other_meshes(pdg, oracle, nr, mtype):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=nr, mtype=mtype, max_iterations=6)
+    s = pdg.Solver(cfg, m, c)
+    s.step(1, stats=False)
+    x, v = s.get_state()
+    xo, vo, _ = sc.step_jacobi(a["rest"].reshape(-1), np.zeros(3 * m.N), 6, rho=0.99)
+    assert rel(x, xo) < REL_ONE_FRAME
+
+
+def test_zero_iterations(pdg, oracle):
+    m, c, cfg, sc, a = scene(pdg, oracle, n=9, max_iterations=0)
+    s = pdg.Solver(cfg, m, c)
+    st = s.step(1)[0]
+    x, v = s.get_state()
+    y = sc.predict(a["rest"], np.zeros_like(a["rest"])).reshape(-1, 3)
+    y[[0, 8]] = a["rest"][[0, 8]]
+    assert np.allclose(x, y, atol=1e-7) and st["iterations"] == 0
