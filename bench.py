@@ -222,6 +222,12 @@ def run_ours(args, rank, world, local_rank):
     if os.path.exists(tp):
         traffic = json.load(open(tp)).get(args.workload)
 
+    if args.quick:   # profiling runs: device-timed region only
+        if rank == 0:
+            print(json.dumps({"workload": args.workload, "value": N * world * args.steps / total_s,
+                              "sweep_us": sweep_ms * 1e3, "frame_ms": frame_ms, "gpu_launches": launches,
+                              "rel_residual_last_frame": st["rel_residual"]}), flush=True)
+        return
     # ---- end to end through the C ABI, host buffers, copies inside the region
     hx = torch.empty((N, 3), dtype=torch.float32).pin_memory()
     hv = torch.zeros((N, 3), dtype=torch.float32).pin_memory()
@@ -292,6 +298,7 @@ def main():
     ap.add_argument("--patch-verts", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="device-timed region only (for profiling)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

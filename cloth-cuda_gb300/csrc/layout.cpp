@@ -252,7 +252,7 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
         vbase += N;
     }
     L.npatch = (int)L.patches.size();
-    L.smem_bytes = 16 * (size_t)L.max_nlocal + 12 * (size_t)L.max_nslot;
+    L.smem_bytes = 32 * (size_t)L.max_nlocal + 12 * (size_t)L.max_nslot;   // y, d per local vertex + slots
     return true;
 }
 

@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(NT) k_iter(IterArgs a, int k, int res_only)
     __syncthreads();
     if (skip) return;
     float4* sx = smem;
-    float* cx = reinterpret_cast<float*>(sx + ph.nlocal);
+    float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
     float* cy = cx + ph.nslot;
     float* cz = cy + ph.nslot;
     process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, omega, sx, cx, cy, cz, red);
@@ -67,13 +67,13 @@ __global__ void k_frame_stats(const ClothInfo* __restrict__ cinfo, ClothRT* crt,
     if (c < ncloth) frame_stats_cloth(cinfo, crt, c, have_final);
 }
 
-__global__ void k_finalize(float4* __restrict__ X, float4* __restrict__ V, const float4* __restrict__ A,
-                           const float4* __restrict__ B, const float4* __restrict__ aux,
-                           const int* __restrict__ vcloth, const ClothInfo* __restrict__ cinfo,
-                           const ClothRT* __restrict__ crt, int n)
+__global__ void k_finalize(float4* __restrict__ X, float4* __restrict__ V, const float4* __restrict__ Y,
+                           const float4* __restrict__ A, const float4* __restrict__ B,
+                           const float4* __restrict__ aux, const int* __restrict__ vcloth,
+                           const ClothInfo* __restrict__ cinfo, const ClothRT* __restrict__ crt, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) finalize_vertex(i, X, V, A, B, aux, vcloth, cinfo, crt);
+    if (i < n) finalize_vertex(i, X, V, Y, A, B, aux, vcloth, cinfo, crt);
 }
 
 // AoS xyz (caller order, cloth by cloth) <-> float4 reordered.
@@ -153,12 +153,12 @@ cudaError_t launch_predict(const float4* X, const float4* V, const float4* aux, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(float4* X, float4* V, const float4* A, const float4* B, const float4* aux,
-                            const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n, int ncloth,
-                            int have_final, cudaStream_t s)
+cudaError_t launch_finalize(float4* X, float4* V, const float4* Y, const float4* A, const float4* B,
+                            const float4* aux, const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n,
+                            int ncloth, int have_final, cudaStream_t s)
 {
     k_frame_stats<<<nblk(ncloth, 128), 128, 0, s>>>(cinfo, crt, ncloth, have_final);
-    k_finalize<<<nblk(n, 256), 256, 0, s>>>(X, V, A, B, aux, vcloth, cinfo, crt, n);
+    k_finalize<<<nblk(n, 256), 256, 0, s>>>(X, V, Y, A, B, aux, vcloth, cinfo, crt, n);
     return cudaGetLastError();
 }
 

@@ -109,18 +109,26 @@ __device__ __forceinline__ void polar_literal(float3 F0, float3 F1, float3& R0, 
 
 __device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
 
+// Positions are carried as x = y + d: y the inertial prediction, d the
+// offset the solve iterates on.  Edge vectors are formed as
+// (y_j - y_i) + (d_j - d_i), so their rounding error is that of the small
+// offsets, not of coordinates of size ~1 m.
+__device__ __forceinline__ float3 edge(const float4* sy, const float4* sd, int i, int j)
+{
+    const float4 yi = sy[i], yj = sy[j], di = sd[i], dj = sd[j];
+    return make_float3((yj.x - yi.x) + (dj.x - di.x), (yj.y - yi.y) + (dj.y - di.y), (yj.z - yi.z) + (dj.z - di.z));
+}
+
 // Triangle phase for one local triangle: writes the contributions of its
 // three corners to the slots 3*lt + corner.
 template <int MODE>
-__device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sx, int lt,
+__device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
                                                  float* cx, float* cy, float* cz)
 {
-    const float3 p0 = f3(sx[r.l01 & 0xffffu]);
-    const float3 p1 = f3(sx[r.l01 >> 16]);
-    const float3 p2 = f3(sx[r.l2]);
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2;
     const float g00 = r.G.x, g10 = r.G.y, g01 = r.G.z, g11 = r.G.w;
-    const float3 d1 = make_float3(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z);
-    const float3 d2 = make_float3(p2.x - p0.x, p2.y - p0.y, p2.z - p0.z);
+    const float3 d1 = edge(sy, sd, i0, i1);
+    const float3 d2 = edge(sy, sd, i0, i2);
     const float3 F0 = make_float3(d1.x * g00 + d2.x * g10, d1.y * g00 + d2.y * g10, d1.z * g00 + d2.z * g10);
     const float3 F1 = make_float3(d1.x * g01 + d2.x * g11, d1.y * g01 + d2.y * g11, d1.z * g01 + d2.z * g11);
     float3 R0, R1, q0, q1;
@@ -144,15 +152,19 @@ __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* 
 // n_rest <= 1e-10, src/pd_solver.cu:304-335); slot s gets h^2 k w_s (p - e)
 // (consistent) or h^2 k w_s p (literal).
 template <int MODE>
-__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sx, int base,
+__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int base,
                                               float* cx, float* cy, float* cz)
 {
-    const float3 x0 = f3(sx[r.l01 & 0xffffu]), x1 = f3(sx[r.l01 >> 16]);
-    const float3 x2 = f3(sx[r.l23 & 0xffffu]), x3 = f3(sx[r.l23 >> 16]);
+    // e = sum w_i x_i = sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
+    const float3 e1 = edge(sy, sd, i0, i1), e2 = edge(sy, sd, i0, i2), e3 = edge(sy, sd, i0, i3);
     const float4 w = r.w;
-    const float3 e = make_float3(w.x * x0.x + w.y * x1.x + w.z * x2.x + w.w * x3.x,
-                                 w.x * x0.y + w.y * x1.y + w.z * x2.y + w.w * x3.y,
-                                 w.x * x0.z + w.y * x1.z + w.z * x2.z + w.w * x3.z);
+    const float ws = (w.x + w.y) + (w.z + w.w);
+    const float4 y0 = sy[i0], d0 = sd[i0];
+    const float3 x0 = make_float3(y0.x + d0.x, y0.y + d0.y, y0.z + d0.z);
+    const float3 e = make_float3(w.y * e1.x + w.z * e2.x + w.w * e3.x + ws * x0.x,
+                                 w.y * e1.y + w.z * e2.y + w.w * e3.y + ws * x0.y,
+                                 w.y * e1.z + w.z * e2.z + w.w * e3.z + ws * x0.z);
     const float len = sqrtf(e.x * e.x + e.y * e.y + e.z * e.z);
     float3 p = make_float3(0.f, 0.f, 0.f);
     if (len > 1e-10f && r.nrest > 1e-10f) {
@@ -177,25 +189,29 @@ __device__ __forceinline__ float warp_sum(float v)
 
 // ---------------------------------------------------------------------------
 // Fused iteration over one patch.  `k` is the sweep index: the block reads
-// x^k from buf[k & 1], reads x^(k-1) and writes x^(k+1) in buf[(k+1) & 1]
-// (the same slot, owned by this thread), and accumulates ||r(x^k)||^2 into
-// crt[c].acc[k % 3].  With res_only it only evaluates the residual.  Data
-// produced by other blocks is loaded with __ldcg (L2, not L1), so the same
-// code is correct inside the persistent kernel between grid barriers.
+// the offsets d^k = x^k - y from buf[k & 1], reads d^(k-1) and writes d^(k+1)
+// in buf[(k+1) & 1] (the same slot, owned by this thread), and accumulates
+// ||r(x^k)||^2 into crt[c].acc[k % 3].  With res_only it only evaluates the
+// residual.  Data produced by other blocks is loaded with __ldcg (L2, not
+// L1), so the same code is correct inside the persistent kernel between
+// grid barriers.  Shared memory: sy, sd (float4 per local vertex), then the
+// three slot arrays.
 // ---------------------------------------------------------------------------
 template <int MODE, int NT>
 __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr& ph, int k, bool res_only,
-                                              float omega, float4* sx, float* cx, float* cy, float* cz,
+                                              float omega, float4* sy, float* cx, float* cy, float* cz,
                                               float* red)
 {
-    const float4* __restrict__ Xk = a.buf[k & 1];
-    float4* __restrict__ Xn = a.buf[(k + 1) & 1];
+    const float4* __restrict__ Dk = a.buf[k & 1];
+    float4* __restrict__ Dn = a.buf[(k + 1) & 1];
+    float4* sd = sy + ph.nlocal;
     const int tid = threadIdx.x;
 
-    // 1. stage x^k of owned + halo vertices
+    // 1. stage y and d^k of owned + halo vertices
     for (int l = tid; l < ph.nlocal; l += NT) {
         const int g = l < ph.nown ? ph.vbegin + l : __ldg(&a.halo[ph.halo_off + l - ph.nown]);
-        sx[l] = __ldcg(&Xk[g]);
+        sy[l] = __ldcg(&a.Y[g]);
+        sd[l] = __ldcg(&Dk[g]);
     }
     __syncthreads();
 
@@ -203,13 +219,13 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     const TriRec* __restrict__ tr = a.tris + ph.tri_off;
     for (int t = tid; t < ph.ntri; t += NT) {
         const TriRec r = tr[t];
-        triangle_contrib<MODE>(r, sx, t, cx, cy, cz);
+        triangle_contrib<MODE>(r, sy, sd, t, cx, cy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;
     const int hbase = 3 * ph.ntri;
     for (int e = tid; e < ph.nhinge; e += NT) {
         const HingeRec r = hr[e];
-        hinge_contrib<MODE>(r, sx, hbase + 4 * e, cx, cy, cz);
+        hinge_contrib<MODE>(r, sy, sd, hbase + 4 * e, cx, cy, cz);
     }
     __syncthreads();
 
@@ -226,36 +242,36 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
             fx += cx[s]; fy += cy[s]; fz += cz[s];
         }
         const int g = ph.vbegin + l;
-        const float4 x = sx[l];
-        const float4 y = __ldcg(&a.Y[g]);
-        const bool pinned = x.w < 0.f;
+        const float4 d = sd[l];
+        const float4 y = sy[l];
+        const bool pinned = d.w < 0.f;
         if (MODE == kModeConsistent) {
-            // -r = m (y - x) + f
-            const float rx = y.w * (y.x - x.x) + fx;
-            const float ry = y.w * (y.y - x.y) + fy;
-            const float rz = y.w * (y.z - x.z) + fz;
+            // -r = m (y - x) + f = -m d + f
+            const float rx = fx - y.w * d.x;
+            const float ry = fy - y.w * d.y;
+            const float rz = fz - y.w * d.z;
             if (!pinned) r2 += rx * rx + ry * ry + rz * rz;
             if (!res_only) {
-                const float4 xp = __ldcg(&Xn[g]);
-                float4 o = x;
+                const float4 dp = __ldcg(&Dn[g]);
+                float4 o = d;
                 if (!pinned) {
-                    const float gi = gamma * x.w;
-                    const float hx = x.x + gi * rx, hy = x.y + gi * ry, hz = x.z + gi * rz;
-                    o.x = omega * (hx - xp.x) + xp.x;
-                    o.y = omega * (hy - xp.y) + xp.y;
-                    o.z = omega * (hz - xp.z) + xp.z;
+                    const float gi = gamma * d.w;
+                    const float hx = d.x + gi * rx, hy = d.y + gi * ry, hz = d.z + gi * rz;
+                    o.x = omega * (hx - dp.x) + dp.x;
+                    o.y = omega * (hy - dp.y) + dp.y;
+                    o.z = omega * (hz - dp.z) + dp.z;
                 }
-                Xn[g] = o;
+                Dn[g] = o;
             }
         } else {
             if (!res_only) {
-                float4 o = x;   // pinned vertices keep their target
-                if (!pinned) {
-                    o.x = (y.w * y.x + fx) * x.w;
-                    o.y = (y.w * y.y + fy) * x.w;
-                    o.z = (y.w * y.z + fz) * x.w;
+                float4 o = d;   // pinned vertices keep their target
+                if (!pinned) {  // x = rhs / diag (src/pd_solver.cu:385-398), stored as x - y
+                    o.x = (y.w * y.x + fx) * d.w - y.x;
+                    o.y = (y.w * y.y + fy) * d.w - y.y;
+                    o.z = (y.w * y.z + fz) * d.w - y.z;
                 }
-                Xn[g] = o;
+                Dn[g] = o;
             }
         }
     }
@@ -331,11 +347,12 @@ __device__ __forceinline__ void predict_vertex(int i, const float4* X, const flo
     y.z = x.z + h * v.z + h2 * ci.ext[2];
     y.w = mass[i];
     Y[i] = y;
+    // start offset d^0 = x^0 - y
     float4 s;
-    if (au.w < 0.f)                    s = make_float4(au.x, au.y, au.z, au.w);   // pinned: target
-    else if (ci.init == 1)             s = make_float4(x.x, x.y, x.z, au.w);
+    if (au.w < 0.f)                    s = make_float4(au.x - y.x, au.y - y.y, au.z - y.z, au.w);  // pin target
+    else if (ci.init == 1)             s = make_float4(x.x - y.x, x.y - y.y, x.z - y.z, au.w);     // x_n
     else if (ci.init == 2 && warm) {   const float4 w = __ldcg(&warm[i]); s = make_float4(w.x, w.y, w.z, au.w); }
-    else                               s = make_float4(y.x, y.y, y.z, au.w);
+    else                               s = make_float4(0.f, 0.f, 0.f, au.w);                        // y
     A[i] = s;
     B[i] = s;
 }
@@ -358,18 +375,19 @@ __device__ __forceinline__ void frame_stats_cloth(const ClothInfo* cinfo, ClothR
     }
 }
 
-// v = (x^used - x_n)(1 - damping)/h, x = x^used; pins at target with v = 0.
-// A cloth whose solve produced NaN/Inf keeps x_n and gets v = 0.
-__device__ __forceinline__ void finalize_vertex(int i, float4* X, float4* V, const float4* A, const float4* B,
-                                                const float4* aux, const int* vcloth, const ClothInfo* cinfo,
-                                                const ClothRT* crt)
+// x = y + d^used; v = (x - x_n)(1 - damping)/h, formed without cancellation
+// as (1 - damping)(v_n + h a + d/h) since x - x_n = h v_n + h^2 a + d.
+// Pins go to their target with v = 0.  A cloth whose solve produced
+// NaN/Inf keeps x_n and gets v = 0.
+__device__ __forceinline__ void finalize_vertex(int i, float4* X, float4* V, const float4* Y, const float4* A,
+                                                const float4* B, const float4* aux, const int* vcloth,
+                                                const ClothInfo* cinfo, const ClothRT* crt)
 {
     const int c = vcloth[i];
     const ClothInfo& ci = cinfo[c];
     const int status = __ldcg(&crt[c].status);
     const int used = __ldcg(&crt[c].used);
     const float4 au = __ldcg(&aux[i]);
-    const float4 xo = __ldcg(&X[i]);
     if (au.w < 0.f) {
         X[i] = make_float4(au.x, au.y, au.z, 0.f);
         V[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -379,10 +397,13 @@ __device__ __forceinline__ void finalize_vertex(int i, float4* X, float4* V, con
         V[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    const float4 xr = (used & 1) ? __ldcg(&B[i]) : __ldcg(&A[i]);
-    const float sc = (1.f - ci.damping) / ci.h;
-    V[i] = make_float4((xr.x - xo.x) * sc, (xr.y - xo.y) * sc, (xr.z - xo.z) * sc, 0.f);
-    X[i] = make_float4(xr.x, xr.y, xr.z, 0.f);
+    const float4 d = (used & 1) ? __ldcg(&B[i]) : __ldcg(&A[i]);
+    const float4 y = __ldcg(&Y[i]);
+    const float4 v = __ldcg(&V[i]);
+    const float h = ci.h, sc = 1.f - ci.damping, ih = 1.f / h;
+    V[i] = make_float4(sc * (v.x + h * ci.ext[0] + d.x * ih), sc * (v.y + h * ci.ext[1] + d.y * ih),
+                       sc * (v.z + h * ci.ext[2] + d.z * ih), 0.f);
+    X[i] = make_float4(y.x + d.x, y.y + d.y, y.z + d.z, 0.f);
 }
 
 }  // namespace pdg

@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(NT) k_persistent(PersistArgs p)
             __syncthreads();
             if (!skip) {
                 float4* sx = smem;
-                float* cx = reinterpret_cast<float*>(sx + ph.nlocal);
+                float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
                 float* cy = cx + ph.nslot;
                 float* cz = cy + ph.nslot;
                 process_patch<MODE, NT>(a, ph, k, res_only || k >= a.cinfo[ph.cloth].max_iter, omega,
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(NT) k_persistent(PersistArgs p)
     for (int c = gtid; c < a.ncloth; c += gstride) frame_stats_cloth(a.cinfo, a.crt, c, p.have_final);
     if (!grid_barrier(p.bar, p.err, p.spin_budget)) return;
     for (int i = gtid; i < p.n; i += gstride)
-        finalize_vertex(i, p.Xw, p.V, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
+        finalize_vertex(i, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
 }
 
 template <int MODE, int NT>

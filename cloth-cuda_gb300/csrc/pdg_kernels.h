@@ -12,9 +12,9 @@ cudaError_t launch_iter(const IterArgs& a, int mode, int nt, int npatch, size_t 
 cudaError_t launch_predict(const float4* X, const float4* V, const float4* aux, const float* mass,
                            const int* vcloth, const ClothInfo* cinfo, const float4* warm, float4* Y,
                            float4* A, float4* B, ClothRT* crt, int n, int ncloth, cudaStream_t s);
-cudaError_t launch_finalize(float4* X, float4* V, const float4* A, const float4* B, const float4* aux,
-                            const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n, int ncloth,
-                            int have_final, cudaStream_t s);
+cudaError_t launch_finalize(float4* X, float4* V, const float4* Y, const float4* A, const float4* B,
+                            const float4* aux, const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n,
+                            int ncloth, int have_final, cudaStream_t s);
 cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s);
 cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s);
 cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P,

@@ -115,7 +115,7 @@ int enqueue_frame(pdg_solver* s)
     const IterArgs a = iter_args(s);
     for (int k = 0; k < L.cap; ++k) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st));
     if (s->have_final) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st));
-    CK(launch_finalize(s->X.p, s->V.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p, L.ntot,
+    CK(launch_finalize(s->X.p, s->V.p, s->Y.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p, L.ntot,
                        L.ncloth, s->have_final, st));
     return PDG_OK;
 }
@@ -422,7 +422,7 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
             cudaEventRecord(e[2], st);
             if (err == cudaSuccess && s->have_final) err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st);
             if (err == cudaSuccess)
-                err = launch_finalize(s->X.p, s->V.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p,
+                err = launch_finalize(s->X.p, s->V.p, s->Y.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p,
                                       L.ntot, L.ncloth, s->have_final, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "frame launch: %s", cudaGetErrorString(err));
             s->launches += s->kernels_per_frame;
