@@ -245,6 +245,11 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                 }
             L.max_nlocal = std::max(L.max_nlocal, nlocal);
             L.max_nslot = std::max(L.max_nslot, nslot);
+            L.max_nown = std::max(L.max_nown, nown);
+            L.max_ntri = std::max(L.max_ntri, ntri);
+            L.max_nhinge = std::max(L.max_nhinge, nhin);
+            const size_t res = 32 * (size_t)nlocal + 12 * (size_t)nslot + 4 * (size_t)(nown + 1) + 2 * (size_t)cnt[nown];
+            L.smem_resident = std::max(L.smem_resident, (res + 15) / 16 * 16);
             L.patches.push_back(ph);
         }
         info.patch_end = (int)L.patches.size();

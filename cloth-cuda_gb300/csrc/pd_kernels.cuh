@@ -202,8 +202,10 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
                                               float omega, float4* sy, float* cx, float* cy, float* cz,
                                               float* red)
 {
-    const float4* __restrict__ Dk = a.buf[k & 1];
-    float4* __restrict__ Dn = a.buf[(k + 1) & 1];
+    // select, not index: a dynamic index into the parameter struct would
+    // copy it to local memory
+    const float4* __restrict__ Dk = (k & 1) ? a.buf[1] : a.buf[0];
+    float4* __restrict__ Dn = (k & 1) ? a.buf[0] : a.buf[1];
     float4* sd = sy + ph.nlocal;
     const int tid = threadIdx.x;
 

@@ -1,0 +1,213 @@
+// Resident persistent PD kernel: one cooperative launch per frame, one patch
+// per block for the whole frame.  Each thread keeps its triangle and hinge
+// records in registers and its owned vertex's previous offset d^(k-1) in a
+// register; the patch's gather lists, y and d^k live in shared memory.  Per
+// sweep only the owned offsets go out to L2 and the halo offsets come back
+// in, then a bounded grid barrier separates sweeps.  Used when every patch
+// fits one block (nown <= NT, ntri <= MT*NT, nhinge <= MH*NT) and all patches
+// are co-resident.
+#include "pd_kernels.cuh"
+#include "pdg_kernels.h"
+
+namespace pdg {
+
+__device__ __forceinline__ bool grid_barrier_r(unsigned* bar, int* err, long long budget)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == gen) {
+                if (clock64() - t0 > budget) { atomicCAS(err, 0, 2); break; }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        ok = (*(volatile int*)err == 0);
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int MODE, int NT, int MT, int MH>
+__global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
+{
+    extern __shared__ float4 smem[];
+    __shared__ PatchHdr ph;
+    __shared__ float red[NT / 32];
+    __shared__ int skip;
+    __shared__ float omega;
+    const IterArgs& a = p.it;
+    const int tid = threadIdx.x;
+    if (tid == 0) ph = a.patches[blockIdx.x];
+    __syncthreads();
+    const int nown = ph.nown, nlocal = ph.nlocal, ntri = ph.ntri, nhin = ph.nhinge;
+    float4* sy = smem;
+    float4* sd = sy + nlocal;
+    float* cx = reinterpret_cast<float*>(sd + nlocal);
+    float* cy = cx + ph.nslot;
+    float* cz = cy + ph.nslot;
+    int* sptr = reinterpret_cast<int*>(cz + ph.nslot);
+    uint16_t* sent = reinterpret_cast<uint16_t*>(sptr + nown + 1);
+
+    // records in registers for the whole frame
+    TriRec rt[MT];
+    HingeRec rh[MH];
+    #pragma unroll
+    for (int j = 0; j < MT; ++j) {
+        const int t = tid + j * NT;
+        if (t < ntri) rt[j] = a.tris[ph.tri_off + t];
+    }
+    #pragma unroll
+    for (int j = 0; j < MH; ++j) {
+        const int e = tid + j * NT;
+        if (e < nhin) rh[j] = a.hinges[ph.hinge_off + e];
+    }
+    // gather lists in shared memory
+    for (int l = tid; l <= nown; l += NT) sptr[l] = a.csr_ptr[ph.csr_off + l];
+    __syncthreads();
+    const int nent = sptr[nown];
+    for (int q = tid; q < nent; q += NT) sent[q] = a.csr_ent[ph.ent_off + q];
+
+    // predict the owned vertices; the cloth's first block resets its record
+    const int c = ph.cloth;
+    const ClothInfo& ci = a.cinfo[c];
+    const bool own = tid < nown;
+    const int g = ph.vbegin + tid;
+    float4 dprev = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((int)blockIdx.x == ci.patch_begin && tid == 0) reset_rt(a.crt, c);
+    if (own) {
+        predict_vertex(g, p.X, p.V, p.aux, p.mass, p.vcloth, a.cinfo, p.warm, p.Y, a.buf[0], a.buf[1]);
+        dprev = __ldcg(&a.buf[0][g]);
+    }
+    if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+    for (int l = tid; l < nlocal; l += NT) {
+        const int gg = l < nown ? ph.vbegin + l : __ldg(&a.halo[ph.halo_off + l - nown]);
+        sy[l] = __ldcg(&a.Y[gg]);
+        sd[l] = __ldcg(&a.buf[0][gg]);
+    }
+
+    const float gamma = ci.gamma;
+    const int nsweep = p.max_iter + (p.have_final ? 1 : 0);
+    for (int k = 0; k < nsweep; ++k) {
+        if (tid == 0) {
+            skip = cloth_done(a, c, k, (int)blockIdx.x == ci.patch_begin) ? 1 : 0;
+            omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
+        }
+        if (k > 0) {   // halo offsets d^k written by the neighbouring blocks
+            const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
+            for (int l = nown + tid; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
+        }
+        __syncthreads();
+        const bool res_only = k >= ci.max_iter;
+        if (!skip) {
+            #pragma unroll
+            for (int j = 0; j < MT; ++j) {
+                const int t = tid + j * NT;
+                if (t < ntri) triangle_contrib<MODE>(rt[j], sy, sd, t, cx, cy, cz);
+            }
+            const int hbase = 3 * ntri;
+            #pragma unroll
+            for (int j = 0; j < MH; ++j) {
+                const int e = tid + j * NT;
+                if (e < nhin) hinge_contrib<MODE>(rh[j], sy, sd, hbase + 4 * e, cx, cy, cz);
+            }
+            __syncthreads();
+            float r2 = 0.f;
+            if (own) {
+                float fx = 0.f, fy = 0.f, fz = 0.f;
+                const int b = sptr[tid], e = sptr[tid + 1];
+                for (int q = b; q < e; ++q) {
+                    const int s = sent[q];
+                    fx += cx[s]; fy += cy[s]; fz += cz[s];
+                }
+                const float4 d = sd[tid];
+                const float4 y = sy[tid];
+                const bool pinned = d.w < 0.f;
+                float4 o = d;
+                if (MODE == kModeConsistent) {
+                    const float rx = fx - y.w * d.x, ry = fy - y.w * d.y, rz = fz - y.w * d.z;
+                    if (!pinned) {
+                        r2 = rx * rx + ry * ry + rz * rz;
+                        const float gi = gamma * d.w;
+                        o.x = omega * (d.x + gi * rx - dprev.x) + dprev.x;
+                        o.y = omega * (d.y + gi * ry - dprev.y) + dprev.y;
+                        o.z = omega * (d.z + gi * rz - dprev.z) + dprev.z;
+                    }
+                } else if (!pinned) {
+                    o.x = (y.w * y.x + fx) * d.w - y.x;
+                    o.y = (y.w * y.y + fy) * d.w - y.y;
+                    o.z = (y.w * y.z + fz) * d.w - y.z;
+                }
+                if (!res_only) {
+                    ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
+                    sd[tid] = o;
+                    dprev = d;
+                }
+            }
+            if (MODE == kModeConsistent) {
+                r2 = warp_sum(r2);
+                if ((tid & 31) == 0) red[tid >> 5] = r2;
+                __syncthreads();
+                if (tid < 32) {
+                    float v = tid < NT / 32 ? red[tid] : 0.f;
+                    v = warp_sum(v);
+                    if (tid == 0) atomicAdd(&a.crt[c].acc[k % 3], (double)v);
+                }
+            }
+        }
+        if (blockIdx.x == 0)
+            for (int cc = tid; cc < a.ncloth; cc += NT) a.crt[cc].acc[(k + 1) % 3] = 0.0;
+        if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+    }
+    if ((int)blockIdx.x == ci.patch_begin && tid == 0) frame_stats_cloth(a.cinfo, a.crt, c, p.have_final);
+    if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+    if (own) finalize_vertex(g, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
+}
+
+// MT x NT triangles and MH x NT hinges per block
+#define PDG_RES_NT 512
+#define PDG_RES_MT 3
+#define PDG_RES_MH 4
+
+int resident_limits(int* nt, int* mt, int* mh)
+{
+    *nt = PDG_RES_NT; *mt = PDG_RES_MT; *mh = PDG_RES_MH;
+    return 0;
+}
+
+static void* pick_resident(int mode)
+{
+    return mode == kModeConsistent ? (void*)k_resident<kModeConsistent, PDG_RES_NT, PDG_RES_MT, PDG_RES_MH>
+                                   : (void*)k_resident<kModeLiteral, PDG_RES_NT, PDG_RES_MT, PDG_RES_MH>;
+}
+
+int resident_max_blocks(int mode, size_t smem)
+{
+    void* f = pick_resident(mode);
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess) return 0;
+    int dev = 0, nsm = 0, nb = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, PDG_RES_NT, smem) != cudaSuccess) return 0;
+    return nb * nsm;
+}
+
+cudaError_t launch_resident(const PersistArgs& p, int grid, size_t smem, cudaStream_t s)
+{
+    void* f = pick_resident(p.mode);
+    PersistArgs copy = p;
+    void* args[] = {&copy};
+    return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(PDG_RES_NT), args, smem, s);
+}
+
+}  // namespace pdg

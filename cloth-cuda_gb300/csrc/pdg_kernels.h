@@ -43,4 +43,10 @@ struct PersistArgs {
 cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s);
 int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
 
+// Resident persistent kernel (pd_resident.cu): one patch per block, records
+// in registers.  Limits: nown <= nt, ntri <= mt*nt, nhinge <= mh*nt.
+int resident_limits(int* nt, int* mt, int* mh);
+int resident_max_blocks(int mode, size_t smem);
+cudaError_t launch_resident(const PersistArgs& p, int grid, size_t smem, cudaStream_t s);
+
 }  // namespace pdg

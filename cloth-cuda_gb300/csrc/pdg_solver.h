@@ -23,8 +23,9 @@ struct ClothSetup {
 
 struct HostLayout {
     int ntot = 0, ncloth = 0, npatch = 0, cap = 0, omega_stride = 1;
-    int max_nlocal = 0, max_nslot = 0;
-    size_t smem_bytes = 0;
+    int max_nlocal = 0, max_nslot = 0, max_nown = 0, max_ntri = 0, max_nhinge = 0;
+    size_t smem_bytes = 0;          // per-sweep kernels
+    size_t smem_resident = 0;       // resident kernel: + gather lists
     std::vector<int> perm_global;   // reordered vertex -> index in the batch's caller order
     std::vector<int> perm_local;    // reordered vertex -> index within its cloth
     std::vector<int> vcloth;

@@ -163,14 +163,40 @@ int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, co
         return set_error(PDG_ERR_ARG, "block_threads must be 128, 256 or 512");
     s->patch_verts = c0.patch_verts ? c0.patch_verts : 256;
     if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
+    if (c0.kernel < PDG_KERNEL_AUTO || c0.kernel > PDG_KERNEL_RESIDENT) return set_error(PDG_ERR_ARG, "unknown kernel");
     s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_GRAPH : c0.kernel;
 
     int dev = 0;
     CK(cudaGetDevice(&dev));
-    int smem_optin = 0;
+    int smem_optin = 0, nsm = 0;
     CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     std::string err;
-    for (;;) {
+    if (c0.kernel == PDG_KERNEL_AUTO || c0.kernel == PDG_KERNEL_RESIDENT) {
+        // Resident kernel: one patch per SM-sized block, every patch co-resident.
+        int rnt = 0, rmt = 0, rmh = 0;
+        resident_limits(&rnt, &rmt, &rmh);
+        int ntot = 0;
+        for (const auto& c : s->cloths) ntot += c.mesh->N;
+        int P = c0.patch_verts;
+        if (!P) P = std::min(rnt, std::max(32, ((ntot + nsm - 1) / nsm + 31) / 32 * 32));
+        bool ok = P <= rnt && build_layout(s->cloths, P, s->L, err);
+        if (ok) {
+            ok = s->L.max_nown <= rnt && s->L.max_ntri <= rmt * rnt && s->L.max_nhinge <= rmh * rnt &&
+                 s->L.smem_resident <= (size_t)std::min(smem_optin - 2048, 220 * 1024);
+            if (ok) ok = s->L.npatch <= resident_max_blocks(s->mode, s->L.smem_resident);
+        }
+        if (ok) {
+            s->kernel = PDG_KERNEL_RESIDENT;
+            s->patch_verts = P;
+            s->nt = rnt;
+            s->persist_grid = s->L.npatch;
+        } else if (c0.kernel == PDG_KERNEL_RESIDENT) {
+            return set_error(PDG_ERR_ARG, "resident kernel does not fit this problem (%d patches of %d vertices)",
+                             s->L.npatch, P);
+        }
+    }
+    for (; s->kernel != PDG_KERNEL_RESIDENT;) {
         if (!build_layout(s->cloths, s->patch_verts, s->L, err)) return set_error(PDG_ERR_ARG, "%s", err.c_str());
         if (s->L.smem_bytes + 1024 <= (size_t)std::min(smem_optin, 200 * 1024)) break;
         if (s->patch_verts <= 16) return set_error(PDG_ERR_ARG, "mesh too dense for the shared-memory patch layout");
@@ -256,6 +282,10 @@ int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
             const PersistArgs p = persist_args(s);
             CK(launch_persistent(p, s->nt, s->persist_grid, s->L.smem_bytes, s->stream));
             s->launches += 1;
+        } else if (s->kernel == PDG_KERNEL_RESIDENT) {
+            const PersistArgs p = persist_args(s);
+            CK(launch_resident(p, s->persist_grid, s->L.smem_resident, s->stream));
+            s->launches += 1;
         } else {
             if (!s->graph) {
                 const int rc = build_graph(s);
@@ -268,7 +298,7 @@ int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
     if (stats) {
         CK(cudaMemcpyAsync(s->h_rt.data(), s->crt.p, sizeof(ClothRT) * s->L.ncloth, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
-        if (s->kernel == PDG_KERNEL_PERSISTENT) {
+        if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
             int e = 0;
             CK(cudaMemcpy(&e, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
             if (e) return set_error(PDG_ERR_TIMEOUT, "grid barrier timed out (code %d)", e);
@@ -405,9 +435,11 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
     int rc = PDG_OK;
     for (int f = 0; f < nframes && rc == PDG_OK; ++f) {
         cudaEventRecord(e[0], st);
-        if (s->kernel == PDG_KERNEL_PERSISTENT) {
+        if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
             const PersistArgs p = persist_args(s);
-            cudaError_t err = launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
+            cudaError_t err = s->kernel == PDG_KERNEL_RESIDENT
+                                  ? launch_resident(p, s->persist_grid, L.smem_resident, st)
+                                  : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "persistent launch: %s", cudaGetErrorString(err));
             s->launches += 1;
             cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
@@ -434,12 +466,13 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
         cudaEventElapsedTime(&a, e[0], e[3]);
         cudaEventElapsedTime(&b, e[1], e[2]);
         tf += a;
-        ts += s->kernel == PDG_KERNEL_PERSISTENT ? a : b;
+        ts += (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) ? a : b;
     }
     for (auto& ev : e) cudaEventDestroy(ev);
     if (rc) return rc;
     if (frame_ms) *frame_ms = (float)(tf / nframes);
-    const int sweeps = std::max(1, L.cap + (s->kernel == PDG_KERNEL_PERSISTENT && s->have_final ? 1 : 0));
+    const bool one_launch = s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT;
+    const int sweeps = std::max(1, L.cap + (one_launch && s->have_final ? 1 : 0));
     if (sweep_ms) *sweep_ms = (float)(ts / nframes / sweeps);
     return PDG_OK;
 }

@@ -47,6 +47,7 @@ extern "C" {
 #define PDG_KERNEL_AUTO       0  /* autotuner picks                         */
 #define PDG_KERNEL_GRAPH      1  /* one fused launch per iteration, frame in a CUDA graph */
 #define PDG_KERNEL_PERSISTENT 2  /* one cooperative launch per frame, bounded grid barrier */
+#define PDG_KERNEL_RESIDENT   3  /* persistent, one patch per block, records kept on chip */
 
 /* Solver configuration.  Mirrors PDSolverConfig (include/pd_solver.h:4-15);
  * fields after `damping` extend it. */
