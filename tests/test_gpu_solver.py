@@ -78,6 +78,10 @@ def test_reference_literal_matches_oracle(pdg, oracle):
     for f in range(6):
         x = a["rest"] + (0 if f == 0 else 0.01 * cell) * rng.standard_normal(a["rest"].shape).astype(np.float32)
         v = (0.05 * rng.standard_normal(x.shape)).astype(np.float32) if f else np.zeros_like(x)
+        # the reference re-applies the pins after every step, so its state
+        # always holds them at their targets
+        x[sc.pins] = sc.pin_targets
+        v[sc.pins] = 0.0
         s.set_state(x, v)
         s.step(1, stats=False)
         xg, vg = s.get_state()
