@@ -233,15 +233,17 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.csr_ent.resize(e0 + cnt[nown]);
             for (int l = 0; l <= nown; ++l) L.csr_ptr.push_back(cnt[l]);
             std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+            // slots are corner-major: triangle corner a at a*ntri + lt, hinge
+            // slot a at 3*ntri + a*nhin + lh
             for (int lt = 0; lt < ntri; ++lt)
                 for (int a = 0; a < 3; ++a) {
                     const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
-                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * lt + a);
+                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(a * ntri + lt);
                 }
             for (int lh = 0; lh < nhin; ++lh)
                 for (int a = 0; a < 4; ++a) {
                     const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
-                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + 4 * lh + a);
+                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
                 }
             L.max_nlocal = std::max(L.max_nlocal, nlocal);
             L.max_nslot = std::max(L.max_nslot, nslot);

@@ -121,9 +121,11 @@ __device__ __forceinline__ float3 edge(const float4* sy, const float4* sd, int i
 
 // Triangle phase for one local triangle: writes the contributions of its
 // three corners to the slots 3*lt + corner.
+// Slots are corner-major (corner c of local triangle lt at c*ntri + lt), so
+// a warp's stores are unit-stride and free of bank conflicts.
 template <int MODE>
 __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
-                                                 float* cx, float* cy, float* cz)
+                                                 int ntri, float* cx, float* cy, float* cz)
 {
     const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2;
     const float g00 = r.G.x, g10 = r.G.y, g01 = r.G.z, g11 = r.G.w;
@@ -142,18 +144,19 @@ __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* 
         q1 = make_float3(r.h2wA * R1.x, r.h2wA * R1.y, r.h2wA * R1.z);
     }
     const float s0 = -(g00 + g10), s1 = -(g01 + g11);
-    const int b = 3 * lt;
-    cx[b] = s0 * q0.x + s1 * q1.x;   cy[b] = s0 * q0.y + s1 * q1.y;   cz[b] = s0 * q0.z + s1 * q1.z;
-    cx[b + 1] = g00 * q0.x + g01 * q1.x; cy[b + 1] = g00 * q0.y + g01 * q1.y; cz[b + 1] = g00 * q0.z + g01 * q1.z;
-    cx[b + 2] = g10 * q0.x + g11 * q1.x; cy[b + 2] = g10 * q0.y + g11 * q1.y; cz[b + 2] = g10 * q0.z + g11 * q1.z;
+    const int b1 = ntri + lt, b2 = 2 * ntri + lt;
+    cx[lt] = s0 * q0.x + s1 * q1.x;   cy[lt] = s0 * q0.y + s1 * q1.y;   cz[lt] = s0 * q0.z + s1 * q1.z;
+    cx[b1] = g00 * q0.x + g01 * q1.x; cy[b1] = g00 * q0.y + g01 * q1.y; cz[b1] = g00 * q0.z + g01 * q1.z;
+    cx[b2] = g10 * q0.x + g11 * q1.x; cy[b2] = g10 * q0.y + g11 * q1.y; cz[b2] = g10 * q0.z + g11 * q1.z;
 }
 
 // Hinge phase: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
 // n_rest <= 1e-10, src/pd_solver.cu:304-335); slot s gets h^2 k w_s (p - e)
 // (consistent) or h^2 k w_s p (literal).
+// Slot s of local hinge e sits at hbase + s*nhin + e.
 template <int MODE>
-__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int base,
-                                              float* cx, float* cy, float* cz)
+__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int e_,
+                                              int hbase, int nhin, float* cx, float* cy, float* cz)
 {
     // e = sum w_i x_i = sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0
     const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
@@ -174,10 +177,45 @@ __device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* s
     float3 q;
     if (MODE == kModeConsistent) q = make_float3(r.h2k * (p.x - e.x), r.h2k * (p.y - e.y), r.h2k * (p.z - e.z));
     else                         q = make_float3(r.h2k * p.x, r.h2k * p.y, r.h2k * p.z);
-    cx[base] = w.x * q.x;     cy[base] = w.x * q.y;     cz[base] = w.x * q.z;
-    cx[base + 1] = w.y * q.x; cy[base + 1] = w.y * q.y; cz[base + 1] = w.y * q.z;
-    cx[base + 2] = w.z * q.x; cy[base + 2] = w.z * q.y; cz[base + 2] = w.z * q.z;
-    cx[base + 3] = w.w * q.x; cy[base + 3] = w.w * q.y; cz[base + 3] = w.w * q.z;
+    const int s0 = hbase + e_, s1 = s0 + nhin, s2 = s1 + nhin, s3 = s2 + nhin;
+    cx[s0] = w.x * q.x; cy[s0] = w.x * q.y; cz[s0] = w.x * q.z;
+    cx[s1] = w.y * q.x; cy[s1] = w.y * q.y; cz[s1] = w.y * q.z;
+    cx[s2] = w.z * q.x; cy[s2] = w.z * q.y; cz[s2] = w.z * q.z;
+    cx[s3] = w.w * q.x; cy[s3] = w.w * q.y; cz[s3] = w.w * q.z;
+}
+
+// Jacobi update of one owned vertex in the consistent form:
+// -r = f - m d;  d_hat = d + gamma D^-1 (-r);  d' = omega (d_hat - d_prev) + d_prev.
+// Explicit roundings keep every launch structure bitwise identical.
+__device__ __forceinline__ float4 update_consistent(float4 d, float4 y, float fx, float fy, float fz, float4 dp,
+                                                   float gamma, float omega, float& r2)
+{
+    const float rx = __fsub_rn(fx, __fmul_rn(y.w, d.x));
+    const float ry = __fsub_rn(fy, __fmul_rn(y.w, d.y));
+    const float rz = __fsub_rn(fz, __fmul_rn(y.w, d.z));
+    float4 o = d;
+    if (d.w >= 0.f) {   // free vertex (pinned ones carry -1)
+        r2 = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz)));
+        const float gi = __fmul_rn(gamma, d.w);
+        o.x = __fmaf_rn(omega, __fsub_rn(__fmaf_rn(gi, rx, d.x), dp.x), dp.x);
+        o.y = __fmaf_rn(omega, __fsub_rn(__fmaf_rn(gi, ry, d.y), dp.y), dp.y);
+        o.z = __fmaf_rn(omega, __fsub_rn(__fmaf_rn(gi, rz, d.z), dp.z), dp.z);
+    } else {
+        r2 = 0.f;
+    }
+    return o;
+}
+
+// x = rhs / diag with rhs = m y + f (src/pd_solver.cu:371-398), stored as x - y.
+__device__ __forceinline__ float4 update_literal(float4 d, float4 y, float fx, float fy, float fz)
+{
+    float4 o = d;
+    if (d.w >= 0.f) {
+        o.x = __fsub_rn(__fmul_rn(__fmaf_rn(y.w, y.x, fx), d.w), y.x);
+        o.y = __fsub_rn(__fmul_rn(__fmaf_rn(y.w, y.y, fy), d.w), y.y);
+        o.z = __fsub_rn(__fmul_rn(__fmaf_rn(y.w, y.z, fz), d.w), y.z);
+    }
+    return o;
 }
 
 __device__ __forceinline__ float warp_sum(float v)
@@ -219,15 +257,15 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
 
     // 2. local step: triangles then hinges, contributions to shared slots
     const TriRec* __restrict__ tr = a.tris + ph.tri_off;
-    for (int t = tid; t < ph.ntri; t += NT) {
+    const int ntri = ph.ntri, nhin = ph.nhinge;
+    for (int t = tid; t < ntri; t += NT) {
         const TriRec r = tr[t];
-        triangle_contrib<MODE>(r, sy, sd, t, cx, cy, cz);
+        triangle_contrib<MODE>(r, sy, sd, t, ntri, cx, cy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;
-    const int hbase = 3 * ph.ntri;
-    for (int e = tid; e < ph.nhinge; e += NT) {
+    for (int e = tid; e < nhin; e += NT) {
         const HingeRec r = hr[e];
-        hinge_contrib<MODE>(r, sy, sd, hbase + 4 * e, cx, cy, cz);
+        hinge_contrib<MODE>(r, sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
     }
     __syncthreads();
 
@@ -246,35 +284,14 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
         const int g = ph.vbegin + l;
         const float4 d = sd[l];
         const float4 y = sy[l];
-        const bool pinned = d.w < 0.f;
         if (MODE == kModeConsistent) {
-            // -r = m (y - x) + f = -m d + f
-            const float rx = fx - y.w * d.x;
-            const float ry = fy - y.w * d.y;
-            const float rz = fz - y.w * d.z;
-            if (!pinned) r2 += rx * rx + ry * ry + rz * rz;
-            if (!res_only) {
-                const float4 dp = __ldcg(&Dn[g]);
-                float4 o = d;
-                if (!pinned) {
-                    const float gi = gamma * d.w;
-                    const float hx = d.x + gi * rx, hy = d.y + gi * ry, hz = d.z + gi * rz;
-                    o.x = omega * (hx - dp.x) + dp.x;
-                    o.y = omega * (hy - dp.y) + dp.y;
-                    o.z = omega * (hz - dp.z) + dp.z;
-                }
-                Dn[g] = o;
-            }
-        } else {
-            if (!res_only) {
-                float4 o = d;   // pinned vertices keep their target
-                if (!pinned) {  // x = rhs / diag (src/pd_solver.cu:385-398), stored as x - y
-                    o.x = (y.w * y.x + fx) * d.w - y.x;
-                    o.y = (y.w * y.y + fy) * d.w - y.y;
-                    o.z = (y.w * y.z + fz) * d.w - y.z;
-                }
-                Dn[g] = o;
-            }
+            float rv;
+            const float4 dp = res_only ? d : __ldcg(&Dn[g]);
+            const float4 o = update_consistent(d, y, fx, fy, fz, dp, gamma, omega, rv);
+            r2 += rv;
+            if (!res_only) Dn[g] = o;
+        } else if (!res_only) {
+            Dn[g] = update_literal(d, y, fx, fy, fz);
         }
     }
     if (MODE == kModeConsistent) {

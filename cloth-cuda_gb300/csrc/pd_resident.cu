@@ -38,6 +38,12 @@ __device__ __forceinline__ bool grid_barrier_r(unsigned* bar, int* err, long lon
     return ok != 0;
 }
 
+template <int NT, int MT>
+__device__ __forceinline__ int tri_index(int tid, int j)
+{
+    return j < MT - 1 ? tid + j * NT : (MT - 1) * NT + (NT - 1 - tid);
+}
+
 template <int MODE, int NT, int MT, int MH>
 __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
 {
@@ -59,12 +65,14 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
     int* sptr = reinterpret_cast<int*>(cz + ph.nslot);
     uint16_t* sent = reinterpret_cast<uint16_t*>(sptr + nown + 1);
 
-    // records in registers for the whole frame
+    // records in registers for the whole frame.  The partial last round of
+    // triangles goes to the highest threads and that of hinges to the
+    // lowest, so warps finish the local step together.
     TriRec rt[MT];
     HingeRec rh[MH];
     #pragma unroll
     for (int j = 0; j < MT; ++j) {
-        const int t = tid + j * NT;
+        const int t = tri_index<NT, MT>(tid, j);
         if (t < ntri) rt[j] = a.tris[ph.tri_off + t];
     }
     #pragma unroll
@@ -112,14 +120,13 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
         if (!skip) {
             #pragma unroll
             for (int j = 0; j < MT; ++j) {
-                const int t = tid + j * NT;
-                if (t < ntri) triangle_contrib<MODE>(rt[j], sy, sd, t, cx, cy, cz);
+                const int t = tri_index<NT, MT>(tid, j);
+                if (t < ntri) triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
             }
-            const int hbase = 3 * ntri;
             #pragma unroll
             for (int j = 0; j < MH; ++j) {
                 const int e = tid + j * NT;
-                if (e < nhin) hinge_contrib<MODE>(rh[j], sy, sd, hbase + 4 * e, cx, cy, cz);
+                if (e < nhin) hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
             }
             __syncthreads();
             float r2 = 0.f;
@@ -132,22 +139,9 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
                 }
                 const float4 d = sd[tid];
                 const float4 y = sy[tid];
-                const bool pinned = d.w < 0.f;
-                float4 o = d;
-                if (MODE == kModeConsistent) {
-                    const float rx = fx - y.w * d.x, ry = fy - y.w * d.y, rz = fz - y.w * d.z;
-                    if (!pinned) {
-                        r2 = rx * rx + ry * ry + rz * rz;
-                        const float gi = gamma * d.w;
-                        o.x = omega * (d.x + gi * rx - dprev.x) + dprev.x;
-                        o.y = omega * (d.y + gi * ry - dprev.y) + dprev.y;
-                        o.z = omega * (d.z + gi * rz - dprev.z) + dprev.z;
-                    }
-                } else if (!pinned) {
-                    o.x = (y.w * y.x + fx) * d.w - y.x;
-                    o.y = (y.w * y.y + fy) * d.w - y.y;
-                    o.z = (y.w * y.z + fz) * d.w - y.z;
-                }
+                float4 o;
+                if (MODE == kModeConsistent) o = update_consistent(d, y, fx, fy, fz, dprev, gamma, omega, r2);
+                else                         o = update_literal(d, y, fx, fy, fz);
                 if (!res_only) {
                     ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
                     sd[tid] = o;

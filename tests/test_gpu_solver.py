@@ -128,8 +128,8 @@ def test_launch_structures_agree_bitwise(pdg, oracle, kernel, mode):
 
 def test_resident_tolerance_and_batch(pdg, oracle):
     # per-cloth convergence inside one resident launch equals the graph path
-    scenes = [scene(pdg, oracle, n=n, seed=n, side=0.5, ks=20.0, kb=1e-3, rho=0.9, max_iterations=300,
-                    tolerance=1e-4) for n in (9, 13, 17)]
+    scenes = [scene(pdg, oracle, n=n, seed=n, side=0.5, ks=20.0, kb=1e-3, rho=0.9, max_iterations=400,
+                    tolerance=1e-4) for n in (9, 10, 11)]
     outs = []
     for kern in (pdg.KERNEL_GRAPH, pdg.KERNEL_RESIDENT):
         cfgs = []
