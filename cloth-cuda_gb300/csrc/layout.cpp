@@ -259,6 +259,24 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
         vbase += N;
     }
     L.npatch = (int)L.patches.size();
+    // neighbour patches: the owners of each patch's halo vertices
+    {
+        std::vector<int> vpatch(ntot, -1);
+        for (int p = 0; p < L.npatch; ++p)
+            for (int l = 0; l < L.patches[p].nown; ++l) vpatch[L.patches[p].vbegin + l] = p;
+        L.nbr_ptr.assign(1, 0);
+        L.nbr.clear();
+        std::vector<int> tmp;
+        for (int p = 0; p < L.npatch; ++p) {
+            const PatchHdr& h = L.patches[p];
+            tmp.clear();
+            for (int q = 0; q < h.nlocal - h.nown; ++q) tmp.push_back(vpatch[L.halo[h.halo_off + q]]);
+            std::sort(tmp.begin(), tmp.end());
+            tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+            L.nbr.insert(L.nbr.end(), tmp.begin(), tmp.end());
+            L.nbr_ptr.push_back((int)L.nbr.size());
+        }
+    }
     L.smem_bytes = 32 * (size_t)L.max_nlocal + 12 * (size_t)L.max_nslot;   // y, d per local vertex + slots
     return true;
 }

@@ -33,9 +33,6 @@ __global__ void __launch_bounds__(NT) k_iter(IterArgs a, int k, int res_only)
         skip = cloth_done(a, c, k, (int)blockIdx.x == ci.patch_begin) ? 1 : 0;
         omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
     }
-    // the residual slot of sweep k+1 is zeroed here (it was last read at k-1)
-    if (blockIdx.x == 0)
-        for (int c = threadIdx.x; c < a.ncloth; c += NT) a.crt[c].acc[(k + 1) % 3] = 0.0;
     __syncthreads();
     if (skip) return;
     float4* sx = smem;
@@ -55,16 +52,16 @@ __global__ void k_predict(const float4* __restrict__ X, const float4* __restrict
     if (i < n) predict_vertex(i, X, V, aux, mass, vcloth, cinfo, warm, Y, A, B);
 }
 
-__global__ void k_reset_rt(ClothRT* crt, int ncloth)
+// one block per cloth
+__global__ void k_reset_rt(ClothRT* crt, double* acc, int acc_stride)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < ncloth) reset_rt(crt, c);
+    reset_rt(crt, acc, acc_stride, blockIdx.x, threadIdx.x, blockDim.x);
 }
 
-__global__ void k_frame_stats(const ClothInfo* __restrict__ cinfo, ClothRT* crt, int ncloth, int have_final)
+__global__ void k_frame_stats(IterArgs a)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < ncloth) frame_stats_cloth(cinfo, crt, c, have_final);
+    if (c < a.ncloth) frame_stats_cloth(a, c);
 }
 
 __global__ void k_finalize(float4* __restrict__ X, float4* __restrict__ V, const float4* __restrict__ Y,
@@ -144,21 +141,20 @@ cudaError_t launch_iter(const IterArgs& a, int mode, int nt, int npatch, size_t 
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_predict(const float4* X, const float4* V, const float4* aux, const float* mass,
-                           const int* vcloth, const ClothInfo* cinfo, const float4* warm, float4* Y,
-                           float4* A, float4* B, ClothRT* crt, int n, int ncloth, cudaStream_t s)
+cudaError_t launch_predict(const IterArgs& a, const float4* X, const float4* V, const float4* aux,
+                           const float* mass, const int* vcloth, const float4* warm, int n, cudaStream_t s)
 {
-    k_reset_rt<<<nblk(ncloth, 128), 128, 0, s>>>(crt, ncloth);
-    k_predict<<<nblk(n, 256), 256, 0, s>>>(X, V, aux, mass, vcloth, cinfo, warm, Y, A, B, n);
+    k_reset_rt<<<a.ncloth, 64, 0, s>>>(a.crt, a.acc, a.acc_stride);
+    k_predict<<<nblk(n, 256), 256, 0, s>>>(X, V, aux, mass, vcloth, a.cinfo, warm, const_cast<float4*>(a.Y),
+                                           a.buf[0], a.buf[1], n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(float4* X, float4* V, const float4* Y, const float4* A, const float4* B,
-                            const float4* aux, const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n,
-                            int ncloth, int have_final, cudaStream_t s)
+cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float4* aux, const int* vcloth, int n,
+                            cudaStream_t s)
 {
-    k_frame_stats<<<nblk(ncloth, 128), 128, 0, s>>>(cinfo, crt, ncloth, have_final);
-    k_finalize<<<nblk(n, 256), 256, 0, s>>>(X, V, Y, A, B, aux, vcloth, cinfo, crt, n);
+    k_frame_stats<<<nblk(a.ncloth, 128), 128, 0, s>>>(a);
+    k_finalize<<<nblk(n, 256), 256, 0, s>>>(X, V, a.Y, a.buf[0], a.buf[1], aux, vcloth, a.cinfo, a.crt, n);
     return cudaGetLastError();
 }
 

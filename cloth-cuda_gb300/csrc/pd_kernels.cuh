@@ -1,5 +1,7 @@
-// Device-side pieces of the PD solve shared by the per-iteration kernel and
-// the persistent kernel.
+// Device-side pieces of the PD solve shared by the per-sweep kernel, the
+// persistent kernel and the resident kernel.  All arithmetic on the solve
+// path uses explicitly rounded intrinsics, so the three launch structures
+// give bitwise identical results whatever the surrounding code.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -11,6 +13,15 @@ namespace pdg {
 
 enum { kModeConsistent = 0, kModeLiteral = 1 };
 
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return ffma(a.x, b.x, ffma(a.y, b.y, fmul(a.z, b.z))); }
+__device__ __forceinline__ float3 scale3(float3 a, float s) { return make_float3(fmul(a.x, s), fmul(a.y, s), fmul(a.z, s)); }
+__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+
 // ---------------------------------------------------------------------------
 // Stretch projection, consistent form: Gram-Schmidt basis (b0, b1) of F's
 // columns, F2d = [b0 b1]^T F, closest rotation in SO(2) in closed form
@@ -20,37 +31,27 @@ enum { kModeConsistent = 0, kModeLiteral = 1 };
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void polar_consistent(float3 F0, float3 F1, float3& R0, float3& R1)
 {
-    const float n0sq = F0.x * F0.x + F0.y * F0.y + F0.z * F0.z;
-    float3 b0;
-    if (n0sq > 1e-20f) {
-        const float r = rsqrtf(n0sq);
-        b0 = make_float3(F0.x * r, F0.y * r, F0.z * r);
-    } else {
-        b0 = make_float3(1.f, 0.f, 0.f);
-    }
-    const float a01 = F1.x * b0.x + F1.y * b0.y + F1.z * b0.z;
-    const float3 c1 = make_float3(F1.x - a01 * b0.x, F1.y - a01 * b0.y, F1.z - a01 * b0.z);
-    const float n1sq = c1.x * c1.x + c1.y * c1.y + c1.z * c1.z;
+    const float n0sq = dot3(F0, F0);
+    const float3 b0 = n0sq > 1e-20f ? scale3(F0, rsqrtf(n0sq)) : make_float3(1.f, 0.f, 0.f);
+    const float a01 = dot3(F1, b0);
+    const float3 c1 = make_float3(ffma(-a01, b0.x, F1.x), ffma(-a01, b0.y, F1.y), ffma(-a01, b0.z, F1.z));
+    const float n1sq = dot3(c1, c1);
     float3 b1;
     if (n1sq > 1e-20f) {
-        const float r = rsqrtf(n1sq);
-        b1 = make_float3(c1.x * r, c1.y * r, c1.z * r);
-    } else {
+        b1 = scale3(c1, rsqrtf(n1sq));
+    } else {   // F1 parallel to F0: any unit vector orthogonal to b0
         float3 q = make_float3(-b0.y, b0.x, 0.f);
-        float nq = q.x * q.x + q.y * q.y;
-        if (nq < 1e-20f) { q = make_float3(0.f, -b0.z, b0.y); nq = q.y * q.y + q.z * q.z; }
-        const float r = rsqrtf(nq);
-        b1 = make_float3(q.x * r, q.y * r, q.z * r);
+        float nq = ffma(q.x, q.x, fmul(q.y, q.y));
+        if (nq < 1e-20f) { q = make_float3(0.f, -b0.z, b0.y); nq = ffma(q.y, q.y, fmul(q.z, q.z)); }
+        b1 = scale3(q, rsqrtf(nq));
     }
-    const float a00 = b0.x * F0.x + b0.y * F0.y + b0.z * F0.z;
-    const float a10 = b1.x * F0.x + b1.y * F0.y + b1.z * F0.z;
-    const float a11 = b1.x * F1.x + b1.y * F1.y + b1.z * F1.z;
-    const float s = a00 + a11, t = a10 - a01;
-    const float rr = s * s + t * t;
+    const float a00 = dot3(b0, F0), a10 = dot3(b1, F0), a11 = dot3(b1, F1);
+    const float s = fadd(a00, a11), t = fsub(a10, a01);
+    const float rr = ffma(s, s, fmul(t, t));
     float c = 1.f, sn = 0.f;
-    if (rr > 1e-30f) { const float r = rsqrtf(rr); c = s * r; sn = t * r; }
-    R0 = make_float3(b0.x * c + b1.x * sn, b0.y * c + b1.y * sn, b0.z * c + b1.z * sn);
-    R1 = make_float3(b1.x * c - b0.x * sn, b1.y * c - b0.y * sn, b1.z * c - b0.z * sn);
+    if (rr > 1e-30f) { const float r = rsqrtf(rr); c = fmul(s, r); sn = fmul(t, r); }
+    R0 = make_float3(ffma(b0.x, c, fmul(b1.x, sn)), ffma(b0.y, c, fmul(b1.y, sn)), ffma(b0.z, c, fmul(b1.z, sn)));
+    R1 = make_float3(ffma(b1.x, c, fmul(-b0.x, sn)), ffma(b1.y, c, fmul(-b0.y, sn)), ffma(b1.z, c, fmul(-b0.z, sn)));
 }
 
 // ---------------------------------------------------------------------------
@@ -61,53 +62,57 @@ __device__ __forceinline__ void polar_consistent(float3 F0, float3 F1, float3& R
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void polar_literal(float3 F0, float3 F1, float3& R0, float3& R1)
 {
-    const float lf0 = sqrtf(F0.x * F0.x + F0.y * F0.y + F0.z * F0.z);
-    float3 u1 = lf0 > 1e-10f ? make_float3(F0.x / lf0, F0.y / lf0, F0.z / lf0) : make_float3(1.f, 0.f, 0.f);
-    const float f1u1 = F1.x * u1.x + F1.y * u1.y + F1.z * u1.z;
-    const float3 up = make_float3(F1.x - f1u1 * u1.x, F1.y - f1u1 * u1.y, F1.z - f1u1 * u1.z);
-    const float lup = sqrtf(up.x * up.x + up.y * up.y + up.z * up.z);
+    const float lf0 = __fsqrt_rn(dot3(F0, F0));
+    const float3 u1 = lf0 > 1e-10f ? make_float3(fdiv(F0.x, lf0), fdiv(F0.y, lf0), fdiv(F0.z, lf0))
+                                   : make_float3(1.f, 0.f, 0.f);
+    const float f1u1 = dot3(F1, u1);
+    const float3 up = make_float3(fsub(F1.x, fmul(f1u1, u1.x)), fsub(F1.y, fmul(f1u1, u1.y)),
+                                  fsub(F1.z, fmul(f1u1, u1.z)));
+    const float lup = __fsqrt_rn(dot3(up, up));
     float3 u2;
     if (lup > 1e-10f) {
-        u2 = make_float3(up.x / lup, up.y / lup, up.z / lup);
+        u2 = make_float3(fdiv(up.x, lup), fdiv(up.y, lup), fdiv(up.z, lup));
     } else {
         u2 = fabsf(u1.x) > 0.9f ? make_float3(-u1.y, u1.x, 0.f) : make_float3(0.f, -u1.z, u1.y);
-        const float l = sqrtf(u2.x * u2.x + u2.y * u2.y + u2.z * u2.z);
-        u2 = make_float3(u2.x / l, u2.y / l, u2.z / l);
+        const float l = __fsqrt_rn(dot3(u2, u2));
+        u2 = make_float3(fdiv(u2.x, l), fdiv(u2.y, l), fdiv(u2.z, l));
     }
-    const float F00 = u1.x * F0.x + u1.y * F0.y + u1.z * F0.z;
-    const float F01 = u1.x * F1.x + u1.y * F1.y + u1.z * F1.z;
-    const float F10 = u2.x * F0.x + u2.y * F0.y + u2.z * F0.z;
-    const float F11 = u2.x * F1.x + u2.y * F1.y + u2.z * F1.z;
-    const float A00 = F00 * F00 + F10 * F10, A01 = F00 * F01 + F10 * F11, A11 = F01 * F01 + F11 * F11;
-    const float tr = (A00 + A11) * 0.5f;
-    const float disc = sqrtf(fmaxf(0.f, (A00 - A11) * (A00 - A11) * 0.25f + A01 * A01));
-    const float l1 = tr + disc, l2 = tr - disc;
+    const float F00 = dot3(u1, F0), F01 = dot3(u1, F1), F10 = dot3(u2, F0), F11 = dot3(u2, F1);
+    const float A00 = ffma(F00, F00, fmul(F10, F10));
+    const float A01 = ffma(F00, F01, fmul(F10, F11));
+    const float A11 = ffma(F01, F01, fmul(F11, F11));
+    const float tr = fmul(fadd(A00, A11), 0.5f);
+    const float dd = fsub(A00, A11);
+    const float disc = __fsqrt_rn(fmaxf(0.f, ffma(fmul(dd, dd), 0.25f, fmul(A01, A01))));
+    const float l1 = fadd(tr, disc), l2 = fsub(tr, disc);
     float v1x = 1.f, v1y = 0.f, v2x = 0.f, v2y = 1.f;
     if (!(disc < 1e-10f || fabsf(A01) < 1e-10f)) {
-        const float tmp = l1 - A00;
-        const float l = sqrtf(A01 * A01 + tmp * tmp);
-        if (l > 1e-10f) { v1x = A01 / l; v1y = tmp / l; }
+        const float tmp = fsub(l1, A00);
+        const float l = __fsqrt_rn(ffma(A01, A01, fmul(tmp, tmp)));
+        if (l > 1e-10f) { v1x = fdiv(A01, l); v1y = fdiv(tmp, l); }
         v2x = -v1y; v2y = v1x;
     }
-    const float s1 = sqrtf(fmaxf(0.f, l1)), s2 = sqrtf(fmaxf(0.f, l2));
+    const float s1 = __fsqrt_rn(fmaxf(0.f, l1)), s2 = __fsqrt_rn(fmaxf(0.f, l2));
     float w1x = 1.f, w1y = 0.f, w2x, w2y;
-    if (s1 > 1e-10f) { w1x = (F00 * v1x + F01 * v1y) / s1; w1y = (F10 * v1x + F11 * v1y) / s1; }
-    if (s2 > 1e-10f) {
-        w2x = (F00 * v2x + F01 * v2y) / s2; w2y = (F10 * v2x + F11 * v2y) / s2;
-    } else {
-        const float fx = F00 * v2x + F01 * v2y, fy = F10 * v2x + F11 * v2y;
-        const float d = w1x * fx + w1y * fy;
-        const float wx = fx - d * w1x, wy = fy - d * w1y;
-        const float l = sqrtf(wx * wx + wy * wy);
-        if (l > 1e-10f) { w2x = wx / l; w2y = wy / l; } else { w2x = -w1y; w2y = w1x; }
+    if (s1 > 1e-10f) {
+        w1x = fdiv(ffma(F00, v1x, fmul(F01, v1y)), s1);
+        w1y = fdiv(ffma(F10, v1x, fmul(F11, v1y)), s1);
     }
-    const float r00 = v1x * w1x + v2x * w2x, r01 = v1x * w1y + v2x * w2y;
-    const float r10 = v1y * w1x + v2y * w2x, r11 = v1y * w1y + v2y * w2y;
-    R0 = make_float3(u1.x * r00 + u2.x * r10, u1.y * r00 + u2.y * r10, u1.z * r00 + u2.z * r10);
-    R1 = make_float3(u1.x * r01 + u2.x * r11, u1.y * r01 + u2.y * r11, u1.z * r01 + u2.z * r11);
+    if (s2 > 1e-10f) {
+        w2x = fdiv(ffma(F00, v2x, fmul(F01, v2y)), s2);
+        w2y = fdiv(ffma(F10, v2x, fmul(F11, v2y)), s2);
+    } else {
+        const float fx = ffma(F00, v2x, fmul(F01, v2y)), fy = ffma(F10, v2x, fmul(F11, v2y));
+        const float d = ffma(w1x, fx, fmul(w1y, fy));
+        const float wx = fsub(fx, fmul(d, w1x)), wy = fsub(fy, fmul(d, w1y));
+        const float l = __fsqrt_rn(ffma(wx, wx, fmul(wy, wy)));
+        if (l > 1e-10f) { w2x = fdiv(wx, l); w2y = fdiv(wy, l); } else { w2x = -w1y; w2y = w1x; }
+    }
+    const float r00 = ffma(v1x, w1x, fmul(v2x, w2x)), r01 = ffma(v1x, w1y, fmul(v2x, w2y));
+    const float r10 = ffma(v1y, w1x, fmul(v2y, w2x)), r11 = ffma(v1y, w1y, fmul(v2y, w2y));
+    R0 = make_float3(ffma(u1.x, r00, fmul(u2.x, r10)), ffma(u1.y, r00, fmul(u2.y, r10)), ffma(u1.z, r00, fmul(u2.z, r10)));
+    R1 = make_float3(ffma(u1.x, r01, fmul(u2.x, r11)), ffma(u1.y, r01, fmul(u2.y, r11)), ffma(u1.z, r01, fmul(u2.z, r11)));
 }
-
-__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
 
 // Positions are carried as x = y + d: y the inertial prediction, d the
 // offset the solve iterates on.  Edge vectors are formed as
@@ -116,13 +121,13 @@ __device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.
 __device__ __forceinline__ float3 edge(const float4* sy, const float4* sd, int i, int j)
 {
     const float4 yi = sy[i], yj = sy[j], di = sd[i], dj = sd[j];
-    return make_float3((yj.x - yi.x) + (dj.x - di.x), (yj.y - yi.y) + (dj.y - di.y), (yj.z - yi.z) + (dj.z - di.z));
+    return make_float3(fadd(fsub(yj.x, yi.x), fsub(dj.x, di.x)), fadd(fsub(yj.y, yi.y), fsub(dj.y, di.y)),
+                       fadd(fsub(yj.z, yi.z), fsub(dj.z, di.z)));
 }
 
 // Triangle phase for one local triangle: writes the contributions of its
-// three corners to the slots 3*lt + corner.
-// Slots are corner-major (corner c of local triangle lt at c*ntri + lt), so
-// a warp's stores are unit-stride and free of bank conflicts.
+// three corners.  Slots are corner-major (corner c of local triangle lt at
+// c*ntri + lt), so a warp's stores are unit-stride and free of bank conflicts.
 template <int MODE>
 __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
                                                  int ntri, float* cx, float* cy, float* cz)
@@ -131,89 +136,103 @@ __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* 
     const float g00 = r.G.x, g10 = r.G.y, g01 = r.G.z, g11 = r.G.w;
     const float3 d1 = edge(sy, sd, i0, i1);
     const float3 d2 = edge(sy, sd, i0, i2);
-    const float3 F0 = make_float3(d1.x * g00 + d2.x * g10, d1.y * g00 + d2.y * g10, d1.z * g00 + d2.z * g10);
-    const float3 F1 = make_float3(d1.x * g01 + d2.x * g11, d1.y * g01 + d2.y * g11, d1.z * g01 + d2.z * g11);
+    const float3 F0 = make_float3(ffma(d1.x, g00, fmul(d2.x, g10)), ffma(d1.y, g00, fmul(d2.y, g10)),
+                                  ffma(d1.z, g00, fmul(d2.z, g10)));
+    const float3 F1 = make_float3(ffma(d1.x, g01, fmul(d2.x, g11)), ffma(d1.y, g01, fmul(d2.y, g11)),
+                                  ffma(d1.z, g01, fmul(d2.z, g11)));
     float3 R0, R1, q0, q1;
     if (MODE == kModeConsistent) {
         polar_consistent(F0, F1, R0, R1);
-        q0 = make_float3(r.h2wA * (R0.x - F0.x), r.h2wA * (R0.y - F0.y), r.h2wA * (R0.z - F0.z));
-        q1 = make_float3(r.h2wA * (R1.x - F1.x), r.h2wA * (R1.y - F1.y), r.h2wA * (R1.z - F1.z));
+        q0 = make_float3(fmul(r.h2wA, fsub(R0.x, F0.x)), fmul(r.h2wA, fsub(R0.y, F0.y)), fmul(r.h2wA, fsub(R0.z, F0.z)));
+        q1 = make_float3(fmul(r.h2wA, fsub(R1.x, F1.x)), fmul(r.h2wA, fsub(R1.y, F1.y)), fmul(r.h2wA, fsub(R1.z, F1.z)));
     } else {
         polar_literal(F0, F1, R0, R1);
-        q0 = make_float3(r.h2wA * R0.x, r.h2wA * R0.y, r.h2wA * R0.z);
-        q1 = make_float3(r.h2wA * R1.x, r.h2wA * R1.y, r.h2wA * R1.z);
+        q0 = scale3(R0, r.h2wA);
+        q1 = scale3(R1, r.h2wA);
     }
-    const float s0 = -(g00 + g10), s1 = -(g01 + g11);
+    const float s0 = -fadd(g00, g10), s1 = -fadd(g01, g11);
     const int b1 = ntri + lt, b2 = 2 * ntri + lt;
-    cx[lt] = s0 * q0.x + s1 * q1.x;   cy[lt] = s0 * q0.y + s1 * q1.y;   cz[lt] = s0 * q0.z + s1 * q1.z;
-    cx[b1] = g00 * q0.x + g01 * q1.x; cy[b1] = g00 * q0.y + g01 * q1.y; cz[b1] = g00 * q0.z + g01 * q1.z;
-    cx[b2] = g10 * q0.x + g11 * q1.x; cy[b2] = g10 * q0.y + g11 * q1.y; cz[b2] = g10 * q0.z + g11 * q1.z;
+    cx[lt] = ffma(s0, q0.x, fmul(s1, q1.x));  cy[lt] = ffma(s0, q0.y, fmul(s1, q1.y));  cz[lt] = ffma(s0, q0.z, fmul(s1, q1.z));
+    cx[b1] = ffma(g00, q0.x, fmul(g01, q1.x)); cy[b1] = ffma(g00, q0.y, fmul(g01, q1.y)); cz[b1] = ffma(g00, q0.z, fmul(g01, q1.z));
+    cx[b2] = ffma(g10, q0.x, fmul(g11, q1.x)); cy[b2] = ffma(g10, q0.y, fmul(g11, q1.y)); cz[b2] = ffma(g10, q0.z, fmul(g11, q1.z));
 }
 
 // Hinge phase: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
 // n_rest <= 1e-10, src/pd_solver.cu:304-335); slot s gets h^2 k w_s (p - e)
-// (consistent) or h^2 k w_s p (literal).
-// Slot s of local hinge e sits at hbase + s*nhin + e.
+// (consistent) or h^2 k w_s p (literal).  Slot s of local hinge e sits at
+// hbase + s*nhin + e.
 template <int MODE>
 __device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int e_,
                                               int hbase, int nhin, float* cx, float* cy, float* cz)
 {
-    // e = sum w_i x_i = sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0
+    // e = sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0
     const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
     const float3 e1 = edge(sy, sd, i0, i1), e2 = edge(sy, sd, i0, i2), e3 = edge(sy, sd, i0, i3);
     const float4 w = r.w;
-    const float ws = (w.x + w.y) + (w.z + w.w);
+    const float ws = fadd(fadd(w.x, w.y), fadd(w.z, w.w));
     const float4 y0 = sy[i0], d0 = sd[i0];
-    const float3 x0 = make_float3(y0.x + d0.x, y0.y + d0.y, y0.z + d0.z);
-    const float3 e = make_float3(w.y * e1.x + w.z * e2.x + w.w * e3.x + ws * x0.x,
-                                 w.y * e1.y + w.z * e2.y + w.w * e3.y + ws * x0.y,
-                                 w.y * e1.z + w.z * e2.z + w.w * e3.z + ws * x0.z);
-    const float len = sqrtf(e.x * e.x + e.y * e.y + e.z * e.z);
+    const float3 x0 = make_float3(fadd(y0.x, d0.x), fadd(y0.y, d0.y), fadd(y0.z, d0.z));
+    const float3 e = make_float3(ffma(w.y, e1.x, ffma(w.z, e2.x, ffma(w.w, e3.x, fmul(ws, x0.x)))),
+                                 ffma(w.y, e1.y, ffma(w.z, e2.y, ffma(w.w, e3.y, fmul(ws, x0.y)))),
+                                 ffma(w.y, e1.z, ffma(w.z, e2.z, ffma(w.w, e3.z, fmul(ws, x0.z)))));
     float3 p = make_float3(0.f, 0.f, 0.f);
-    if (len > 1e-10f && r.nrest > 1e-10f) {
-        const float sc = r.nrest / len;
-        p = make_float3(e.x * sc, e.y * sc, e.z * sc);
+    if (r.nrest > 1e-10f) {
+        const float len = __fsqrt_rn(dot3(e, e));
+        if (len > 1e-10f) p = scale3(e, fdiv(r.nrest, len));
     }
     float3 q;
-    if (MODE == kModeConsistent) q = make_float3(r.h2k * (p.x - e.x), r.h2k * (p.y - e.y), r.h2k * (p.z - e.z));
-    else                         q = make_float3(r.h2k * p.x, r.h2k * p.y, r.h2k * p.z);
+    if (MODE == kModeConsistent)
+        q = make_float3(fmul(r.h2k, fsub(p.x, e.x)), fmul(r.h2k, fsub(p.y, e.y)), fmul(r.h2k, fsub(p.z, e.z)));
+    else
+        q = scale3(p, r.h2k);
     const int s0 = hbase + e_, s1 = s0 + nhin, s2 = s1 + nhin, s3 = s2 + nhin;
-    cx[s0] = w.x * q.x; cy[s0] = w.x * q.y; cz[s0] = w.x * q.z;
-    cx[s1] = w.y * q.x; cy[s1] = w.y * q.y; cz[s1] = w.y * q.z;
-    cx[s2] = w.z * q.x; cy[s2] = w.z * q.y; cz[s2] = w.z * q.z;
-    cx[s3] = w.w * q.x; cy[s3] = w.w * q.y; cz[s3] = w.w * q.z;
+    cx[s0] = fmul(w.x, q.x); cy[s0] = fmul(w.x, q.y); cz[s0] = fmul(w.x, q.z);
+    cx[s1] = fmul(w.y, q.x); cy[s1] = fmul(w.y, q.y); cz[s1] = fmul(w.y, q.z);
+    cx[s2] = fmul(w.z, q.x); cy[s2] = fmul(w.z, q.y); cz[s2] = fmul(w.z, q.z);
+    cx[s3] = fmul(w.w, q.x); cy[s3] = fmul(w.w, q.y); cz[s3] = fmul(w.w, q.z);
+}
+
+// Sum of the contribution slots of one owned vertex, in gather-list order.
+template <class IDX>
+__device__ __forceinline__ float3 gather_slots(const IDX* ent, int b, int e, const float* cx, const float* cy,
+                                               const float* cz)
+{
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int q = b; q < e; ++q) {
+        const int s = ent[q];
+        fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
+    }
+    return make_float3(fx, fy, fz);
 }
 
 // Jacobi update of one owned vertex in the consistent form:
 // -r = f - m d;  d_hat = d + gamma D^-1 (-r);  d' = omega (d_hat - d_prev) + d_prev.
-// Explicit roundings keep every launch structure bitwise identical.
-__device__ __forceinline__ float4 update_consistent(float4 d, float4 y, float fx, float fy, float fz, float4 dp,
-                                                   float gamma, float omega, float& r2)
+__device__ __forceinline__ float4 update_consistent(float4 d, float4 y, float3 f, float4 dp, float gamma,
+                                                   float omega, float& r2)
 {
-    const float rx = __fsub_rn(fx, __fmul_rn(y.w, d.x));
-    const float ry = __fsub_rn(fy, __fmul_rn(y.w, d.y));
-    const float rz = __fsub_rn(fz, __fmul_rn(y.w, d.z));
+    const float rx = fsub(f.x, fmul(y.w, d.x));
+    const float ry = fsub(f.y, fmul(y.w, d.y));
+    const float rz = fsub(f.z, fmul(y.w, d.z));
     float4 o = d;
+    r2 = 0.f;
     if (d.w >= 0.f) {   // free vertex (pinned ones carry -1)
-        r2 = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz)));
-        const float gi = __fmul_rn(gamma, d.w);
-        o.x = __fmaf_rn(omega, __fsub_rn(__fmaf_rn(gi, rx, d.x), dp.x), dp.x);
-        o.y = __fmaf_rn(omega, __fsub_rn(__fmaf_rn(gi, ry, d.y), dp.y), dp.y);
-        o.z = __fmaf_rn(omega, __fsub_rn(__fmaf_rn(gi, rz, d.z), dp.z), dp.z);
-    } else {
-        r2 = 0.f;
+        r2 = ffma(rx, rx, ffma(ry, ry, fmul(rz, rz)));
+        const float gi = fmul(gamma, d.w);
+        o.x = ffma(omega, fsub(ffma(gi, rx, d.x), dp.x), dp.x);
+        o.y = ffma(omega, fsub(ffma(gi, ry, d.y), dp.y), dp.y);
+        o.z = ffma(omega, fsub(ffma(gi, rz, d.z), dp.z), dp.z);
     }
     return o;
 }
 
 // x = rhs / diag with rhs = m y + f (src/pd_solver.cu:371-398), stored as x - y.
-__device__ __forceinline__ float4 update_literal(float4 d, float4 y, float fx, float fy, float fz)
+__device__ __forceinline__ float4 update_literal(float4 d, float4 y, float3 f)
 {
     float4 o = d;
     if (d.w >= 0.f) {
-        o.x = __fsub_rn(__fmul_rn(__fmaf_rn(y.w, y.x, fx), d.w), y.x);
-        o.y = __fsub_rn(__fmul_rn(__fmaf_rn(y.w, y.y, fy), d.w), y.y);
-        o.z = __fsub_rn(__fmul_rn(__fmaf_rn(y.w, y.z, fz), d.w), y.z);
+        o.x = fsub(fmul(fadd(f.x, fmul(y.w, y.x)), d.w), y.x);
+        o.y = fsub(fmul(fadd(f.y, fmul(y.w, y.y)), d.w), y.y);
+        o.z = fsub(fmul(fadd(f.z, fmul(y.w, y.z)), d.w), y.z);
     }
     return o;
 }
@@ -225,15 +244,31 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
+// Block-wide sum of r2 added to the per-sweep accumulator (one double atomic
+// per block).  Contains a __syncthreads.
+template <int NT>
+__device__ __forceinline__ void block_residual(float r2, float* red, double* acc)
+{
+    const int tid = threadIdx.x;
+    r2 = warp_sum(r2);
+    if ((tid & 31) == 0) red[tid >> 5] = r2;
+    __syncthreads();
+    if (tid < 32) {
+        float v = tid < NT / 32 ? red[tid] : 0.f;
+        v = warp_sum(v);
+        if (tid == 0) atomicAdd(acc, (double)v);
+    }
+}
+
 // ---------------------------------------------------------------------------
-// Fused iteration over one patch.  `k` is the sweep index: the block reads
-// the offsets d^k = x^k - y from buf[k & 1], reads d^(k-1) and writes d^(k+1)
-// in buf[(k+1) & 1] (the same slot, owned by this thread), and accumulates
-// ||r(x^k)||^2 into crt[c].acc[k % 3].  With res_only it only evaluates the
-// residual.  Data produced by other blocks is loaded with __ldcg (L2, not
-// L1), so the same code is correct inside the persistent kernel between
-// grid barriers.  Shared memory: sy, sd (float4 per local vertex), then the
-// three slot arrays.
+// Fused sweep over one patch.  `k` is the sweep index: the block reads the
+// offsets d^k = x^k - y from buf[k & 1], reads d^(k-1) and writes d^(k+1) in
+// buf[(k+1) & 1] (the same slot, owned by this thread), and adds
+// ||r(x^k)||^2 to acc[cloth][k].  With res_only it only evaluates the
+// residual.  Data produced by other blocks is loaded with __ldcg (L2, not L1),
+// so the same code is correct inside the persistent kernel between grid
+// barriers.  Shared memory: sy, sd (float4 per local vertex), then the three
+// slot arrays.
 // ---------------------------------------------------------------------------
 template <int MODE, int NT>
 __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr& ph, int k, bool res_only,
@@ -275,48 +310,37 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     const uint16_t* __restrict__ ce = a.csr_ent + ph.ent_off;
     float r2 = 0.f;
     for (int l = tid; l < ph.nown; l += NT) {
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        const int b = __ldg(&cp[l]), e = __ldg(&cp[l + 1]);
-        for (int q = b; q < e; ++q) {
-            const int s = __ldg(&ce[q]);
-            fx += cx[s]; fy += cy[s]; fz += cz[s];
-        }
+        const float3 f = gather_slots(ce, __ldg(&cp[l]), __ldg(&cp[l + 1]), cx, cy, cz);
         const int g = ph.vbegin + l;
         const float4 d = sd[l];
         const float4 y = sy[l];
         if (MODE == kModeConsistent) {
             float rv;
             const float4 dp = res_only ? d : __ldcg(&Dn[g]);
-            const float4 o = update_consistent(d, y, fx, fy, fz, dp, gamma, omega, rv);
+            const float4 o = update_consistent(d, y, f, dp, gamma, omega, rv);
             r2 += rv;
             if (!res_only) Dn[g] = o;
         } else if (!res_only) {
-            Dn[g] = update_literal(d, y, fx, fy, fz);
+            Dn[g] = update_literal(d, y, f);
         }
     }
-    if (MODE == kModeConsistent) {
-        r2 = warp_sum(r2);
-        if ((tid & 31) == 0) red[tid >> 5] = r2;
-        __syncthreads();
-        if (tid < 32) {
-            float v = tid < NT / 32 ? red[tid] : 0.f;
-            v = warp_sum(v);
-            if (tid == 0) atomicAdd(&a.crt[ph.cloth].acc[k % 3], (double)v);
-        }
-    }
+    if (MODE == kModeConsistent) block_residual<NT>(r2, red, a.acc + (size_t)ph.cloth * a.acc_stride + k);
 }
 
 // Per-cloth decision at the start of sweep k, taken by one thread per block;
 // every block of a cloth reaches the same answer from the same data.
 // Returns true if the cloth is done.  The cloth's first patch records it.
-__device__ __forceinline__ bool cloth_done(const IterArgs& a, int c, int k, bool designated)
+// With check == false only the static cap is applied (the per-sweep sums may
+// still be incomplete: sweeps synchronised with neighbours only).
+__device__ __forceinline__ bool cloth_done(const IterArgs& a, int c, int k, bool designated, bool check = true)
 {
     ClothRT* rt = a.crt + c;
     if (!__ldcg(&rt->active)) return true;
     const ClothInfo& ci = a.cinfo[c];
-    if (k >= 1 && ci.mode == kModeConsistent) {
-        const double acc0 = __ldcg(&rt->acc[0]);
-        const double rk2 = __ldcg(&rt->acc[(k - 1) % 3]);          // ||r(x^(k-1))||^2
+    const double* acc = a.acc + (size_t)c * a.acc_stride;
+    if (check && k >= 1 && ci.mode == kModeConsistent) {
+        const double acc0 = __ldcg(&acc[0]);
+        const double rk2 = __ldcg(&acc[k - 1]);          // ||r(x^(k-1))||^2
         const double ry2 = (k == 1 && ci.init == 0) ? acc0 : __ldcg(&rt->res_y2);
         if (k == 1 && designated) {
             rt->res0_2 = acc0;
@@ -336,60 +360,73 @@ __device__ __forceinline__ bool cloth_done(const IterArgs& a, int c, int k, bool
         }
     }
     if (k >= ci.max_iter && (k > ci.max_iter || !a.have_final)) {
-        if (designated) { rt->used = ci.max_iter; rt->resf_2 = -1.0; rt->active = 0; }
+        if (designated && (check || ci.mode != kModeConsistent)) {
+            rt->used = ci.max_iter; rt->resf_2 = -1.0; rt->active = 0;
+        }
         return true;
     }
     return false;
 }
 
-__device__ __forceinline__ void reset_rt(ClothRT* crt, int c)
+// Start of a frame: the cloth's record and per-sweep sums are cleared.
+__device__ __forceinline__ void reset_rt(ClothRT* crt, double* acc, int acc_stride, int c, int t0, int nt)
 {
-    ClothRT r;
-    r.active = 1; r.used = 0; r.status = 0; r.warm = 0;
-    r.res_y2 = 0.0; r.res0_2 = 0.0; r.resf_2 = -1.0;
-    r.acc[0] = r.acc[1] = r.acc[2] = 0.0;
-    crt[c] = r;
+    if (t0 == 0) {
+        ClothRT r;
+        r.active = 1; r.used = 0; r.status = 0; r.warm = 0;
+        r.res_y2 = 0.0; r.res0_2 = 0.0; r.resf_2 = -1.0;
+        crt[c] = r;
+    }
+    for (int k = t0; k < acc_stride; k += nt) acc[(size_t)c * acc_stride + k] = 0.0;
 }
 
-// y = x + h v + h^2 a (w = mass); start iterate into both buffers
-// (w = inverse diagonal, -1 for pinned vertices).
+// y = x + h v + h^2 a (w = mass); start offset d^0 = x^0 - y into both
+// buffers (w = inverse diagonal, -1 for pinned vertices).
 __device__ __forceinline__ void predict_vertex(int i, const float4* X, const float4* V, const float4* aux,
                                                const float* mass, const int* vcloth, const ClothInfo* cinfo,
                                                const float4* warm, float4* Y, float4* A, float4* B)
 {
     const ClothInfo& ci = cinfo[vcloth[i]];
-    const float h = ci.h, h2 = h * h;
+    const float h = ci.h, h2 = fmul(h, h);
     const float4 x = __ldcg(&X[i]), v = __ldcg(&V[i]), au = __ldcg(&aux[i]);
     float4 y;
-    y.x = x.x + h * v.x + h2 * ci.ext[0];
-    y.y = x.y + h * v.y + h2 * ci.ext[1];
-    y.z = x.z + h * v.z + h2 * ci.ext[2];
+    y.x = ffma(h2, ci.ext[0], ffma(h, v.x, x.x));
+    y.y = ffma(h2, ci.ext[1], ffma(h, v.y, x.y));
+    y.z = ffma(h2, ci.ext[2], ffma(h, v.z, x.z));
     y.w = mass[i];
     Y[i] = y;
-    // start offset d^0 = x^0 - y
     float4 s;
-    if (au.w < 0.f)                    s = make_float4(au.x - y.x, au.y - y.y, au.z - y.z, au.w);  // pin target
-    else if (ci.init == 1)             s = make_float4(x.x - y.x, x.y - y.y, x.z - y.z, au.w);     // x_n
+    if (au.w < 0.f)                    s = make_float4(fsub(au.x, y.x), fsub(au.y, y.y), fsub(au.z, y.z), au.w);
+    else if (ci.init == 1)             s = make_float4(fsub(x.x, y.x), fsub(x.y, y.y), fsub(x.z, y.z), au.w);
     else if (ci.init == 2 && warm) {   const float4 w = __ldcg(&warm[i]); s = make_float4(w.x, w.y, w.z, au.w); }
-    else                               s = make_float4(0.f, 0.f, 0.f, au.w);                        // y
+    else                               s = make_float4(0.f, 0.f, 0.f, au.w);
     A[i] = s;
     B[i] = s;
 }
 
-// Cloths still active after the last sweep keep x^cap.
-__device__ __forceinline__ void frame_stats_cloth(const ClothInfo* cinfo, ClothRT* crt, int c, int have_final)
+// Cloths still active after the last sweep keep x^max_iter.  A non-finite
+// per-sweep sum marks the cloth as failed (sweeps that ran with neighbour
+// synchronisation skip the per-sweep check).
+__device__ __forceinline__ void frame_stats_cloth(const IterArgs& a, int c)
 {
-    ClothRT* rt = crt + c;
-    const ClothInfo& ci = cinfo[c];
-    if (ci.max_iter <= 1 && ci.mode == kModeConsistent) {   // the k == 1 bookkeeping never ran
-        rt->res0_2 = __ldcg(&rt->acc[0]);
+    ClothRT* rt = a.crt + c;
+    const ClothInfo& ci = a.cinfo[c];
+    const double* acc = a.acc + (size_t)c * a.acc_stride;
+    if (ci.mode == kModeConsistent) {
+        rt->res0_2 = __ldcg(&acc[0]);
         if (ci.init == 0) rt->res_y2 = rt->res0_2;
     }
     if (__ldcg(&rt->active)) {
         rt->used = ci.max_iter;
-        const double rf = __ldcg(&rt->acc[ci.max_iter % 3]);
-        rt->resf_2 = (have_final && ci.mode == kModeConsistent) ? rf : -1.0;
-        if (have_final && ci.mode == kModeConsistent && !isfinite(rf)) rt->status = -6;
+        if (ci.mode == kModeConsistent) {
+            bool finite = true;
+            for (int k = 0; k <= ci.max_iter && k < a.acc_stride; ++k) finite = finite && isfinite(__ldcg(&acc[k]));
+            const double rf = __ldcg(&acc[ci.max_iter]);
+            rt->resf_2 = a.have_final ? rf : -1.0;
+            if (!finite) rt->status = -6;
+        } else {
+            rt->resf_2 = -1.0;
+        }
         rt->active = 0;
     }
 }
@@ -419,10 +456,10 @@ __device__ __forceinline__ void finalize_vertex(int i, float4* X, float4* V, con
     const float4 d = (used & 1) ? __ldcg(&B[i]) : __ldcg(&A[i]);
     const float4 y = __ldcg(&Y[i]);
     const float4 v = __ldcg(&V[i]);
-    const float h = ci.h, sc = 1.f - ci.damping, ih = 1.f / h;
-    V[i] = make_float4(sc * (v.x + h * ci.ext[0] + d.x * ih), sc * (v.y + h * ci.ext[1] + d.y * ih),
-                       sc * (v.z + h * ci.ext[2] + d.z * ih), 0.f);
-    X[i] = make_float4(y.x + d.x, y.y + d.y, y.z + d.z, 0.f);
+    const float h = ci.h, sc = 1.f - ci.damping, ih = fdiv(1.f, h);
+    V[i] = make_float4(fmul(sc, ffma(d.x, ih, ffma(h, ci.ext[0], v.x))), fmul(sc, ffma(d.y, ih, ffma(h, ci.ext[1], v.y))),
+                       fmul(sc, ffma(d.z, ih, ffma(h, ci.ext[2], v.z))), 0.f);
+    X[i] = make_float4(fadd(y.x, d.x), fadd(y.y, d.y), fadd(y.z, d.z), 0.f);
 }
 
 }  // namespace pdg

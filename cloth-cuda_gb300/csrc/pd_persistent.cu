@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(NT) k_persistent(PersistArgs p)
     const int gtid = blockIdx.x * NT + threadIdx.x, gstride = gridDim.x * NT;
 
     // predict + per-cloth reset
-    for (int c = gtid; c < a.ncloth; c += gstride) reset_rt(a.crt, c);
+    for (int c = blockIdx.x; c < a.ncloth; c += gridDim.x) reset_rt(a.crt, a.acc, a.acc_stride, c, threadIdx.x, NT);
     for (int i = gtid; i < p.n; i += gstride)
         predict_vertex(i, p.X, p.V, p.aux, p.mass, p.vcloth, a.cinfo, p.warm, p.Y, a.buf[0], a.buf[1]);
     if (!grid_barrier(p.bar, p.err, p.spin_budget)) return;
@@ -78,13 +78,10 @@ __global__ void __launch_bounds__(NT) k_persistent(PersistArgs p)
             }
             __syncthreads();
         }
-        // the residual slot of sweep k+1 was last read during sweep k-1
-        if (blockIdx.x == 0)
-            for (int c = threadIdx.x; c < a.ncloth; c += NT) a.crt[c].acc[(k + 1) % 3] = 0.0;
         if (!grid_barrier(p.bar, p.err, p.spin_budget)) return;
     }
 
-    for (int c = gtid; c < a.ncloth; c += gstride) frame_stats_cloth(a.cinfo, a.crt, c, p.have_final);
+    for (int c = gtid; c < a.ncloth; c += gstride) frame_stats_cloth(a, c);
     if (!grid_barrier(p.bar, p.err, p.spin_budget)) return;
     for (int i = gtid; i < p.n; i += gstride)
         finalize_vertex(i, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);

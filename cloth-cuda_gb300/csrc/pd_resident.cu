@@ -2,10 +2,17 @@
 // per block for the whole frame.  Each thread keeps its triangle and hinge
 // records in registers and its owned vertex's previous offset d^(k-1) in a
 // register; the patch's gather lists, y and d^k live in shared memory.  Per
-// sweep only the owned offsets go out to L2 and the halo offsets come back
-// in, then a bounded grid barrier separates sweeps.  Used when every patch
-// fits one block (nown <= NT, ntri <= MT*NT, nhinge <= MH*NT) and all patches
-// are co-resident.
+// sweep only the owned offsets go out to L2 and the halo offsets come back.
+//
+// Synchronisation between sweeps: with fixed sweep counts a block waits only
+// for the patches that own its halo vertices (per-patch completion marks in
+// global memory); with a residual tolerance every sweep ends in a grid
+// barrier, because the convergence decision needs the complete per-cloth
+// residual.  Every wait is bounded by a clock64 budget; on expiry the block
+// records an error code and leaves, and so do all others at their next wait.
+//
+// Used when every patch fits one block (nown <= NT, ntri <= MT*NT,
+// nhinge <= MH*NT) and all patches are co-resident.
 #include "pd_kernels.cuh"
 #include "pdg_kernels.h"
 
@@ -33,6 +40,41 @@ __device__ __forceinline__ bool grid_barrier_r(unsigned* bar, int* err, long lon
         }
         __threadfence();
         ok = (*(volatile int*)err == 0);
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Publish "this patch finished the sweep with mark m" after all of the
+// block's global writes.
+__device__ __forceinline__ void publish_mark(unsigned long long* pflag, unsigned long long m)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *(volatile unsigned long long*)&pflag[blockIdx.x] = m;
+    }
+}
+
+// Wait until every neighbouring patch published a mark >= m (first warp, one
+// lane per neighbour), bounded.  Returns false on timeout or a prior error.
+__device__ __forceinline__ bool wait_neighbours(const int* nb, int nnb, const unsigned long long* pflag,
+                                                unsigned long long m, int* err, long long budget)
+{
+    __shared__ int ok;
+    if (threadIdx.x < 32) {
+        bool good = true;
+        for (int j = threadIdx.x; j < nnb && good; j += 32) {
+            const volatile unsigned long long* f = pflag + nb[j];
+            const long long t0 = clock64();
+            while (*f < m) {
+                if (clock64() - t0 > budget || *(volatile int*)err != 0) { atomicCAS(err, 0, 3); good = false; break; }
+                __nanosleep(20);
+            }
+        }
+        __threadfence();
+        const unsigned all = __ballot_sync(0xffffffffu, good);
+        if (threadIdx.x == 0) ok = (all == 0xffffffffu);
     }
     __syncthreads();
     return ok != 0;
@@ -90,9 +132,10 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
     const int c = ph.cloth;
     const ClothInfo& ci = a.cinfo[c];
     const bool own = tid < nown;
+    const bool first = (int)blockIdx.x == ci.patch_begin;
     const int g = ph.vbegin + tid;
     float4 dprev = make_float4(0.f, 0.f, 0.f, 0.f);
-    if ((int)blockIdx.x == ci.patch_begin && tid == 0) reset_rt(a.crt, c);
+    if (first) reset_rt(a.crt, a.acc, a.acc_stride, c, tid, NT);
     if (own) {
         predict_vertex(g, p.X, p.V, p.aux, p.mass, p.vcloth, a.cinfo, p.warm, p.Y, a.buf[0], a.buf[1]);
         dprev = __ldcg(&a.buf[0][g]);
@@ -106,12 +149,18 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
 
     const float gamma = ci.gamma;
     const int nsweep = p.max_iter + (p.have_final ? 1 : 0);
+    const bool nbr = p.nbr_sync != 0;
+    const unsigned long long mark0 = p.frame_seq * (unsigned long long)(nsweep + 2);
+    const int* nb = p.nbr + p.nbr_ptr[blockIdx.x];
+    const int nnb = p.nbr_ptr[blockIdx.x + 1] - p.nbr_ptr[blockIdx.x];
+    double* acc = a.acc + (size_t)c * a.acc_stride;
     for (int k = 0; k < nsweep; ++k) {
         if (tid == 0) {
-            skip = cloth_done(a, c, k, (int)blockIdx.x == ci.patch_begin) ? 1 : 0;
+            skip = cloth_done(a, c, k, first, !nbr) ? 1 : 0;
             omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
         }
         if (k > 0) {   // halo offsets d^k written by the neighbouring blocks
+            if (nbr && !wait_neighbours(nb, nnb, p.pflag, mark0 + k, p.err, p.spin_budget)) return;
             const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
             for (int l = nown + tid; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
         }
@@ -131,39 +180,26 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
             __syncthreads();
             float r2 = 0.f;
             if (own) {
-                float fx = 0.f, fy = 0.f, fz = 0.f;
-                const int b = sptr[tid], e = sptr[tid + 1];
-                for (int q = b; q < e; ++q) {
-                    const int s = sent[q];
-                    fx += cx[s]; fy += cy[s]; fz += cz[s];
-                }
+                const float3 f = gather_slots(sent, sptr[tid], sptr[tid + 1], cx, cy, cz);
                 const float4 d = sd[tid];
                 const float4 y = sy[tid];
                 float4 o;
-                if (MODE == kModeConsistent) o = update_consistent(d, y, fx, fy, fz, dprev, gamma, omega, r2);
-                else                         o = update_literal(d, y, fx, fy, fz);
+                if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega, r2);
+                else                         o = update_literal(d, y, f);
                 if (!res_only) {
                     ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
                     sd[tid] = o;
                     dprev = d;
                 }
             }
-            if (MODE == kModeConsistent) {
-                r2 = warp_sum(r2);
-                if ((tid & 31) == 0) red[tid >> 5] = r2;
-                __syncthreads();
-                if (tid < 32) {
-                    float v = tid < NT / 32 ? red[tid] : 0.f;
-                    v = warp_sum(v);
-                    if (tid == 0) atomicAdd(&a.crt[c].acc[k % 3], (double)v);
-                }
-            }
+            if (MODE == kModeConsistent) block_residual<NT>(r2, red, acc + k);
         }
-        if (blockIdx.x == 0)
-            for (int cc = tid; cc < a.ncloth; cc += NT) a.crt[cc].acc[(k + 1) % 3] = 0.0;
-        if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+        if (nbr) publish_mark(p.pflag, mark0 + k + 1);
+        else if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
     }
-    if ((int)blockIdx.x == ci.patch_begin && tid == 0) frame_stats_cloth(a.cinfo, a.crt, c, p.have_final);
+    // every per-sweep sum is complete after this barrier
+    if (nbr && !grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+    if (first && tid == 0) frame_stats_cloth(a, c);
     if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
     if (own) finalize_vertex(g, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
 }

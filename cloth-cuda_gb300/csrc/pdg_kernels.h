@@ -9,12 +9,10 @@ namespace pdg {
 
 cudaError_t launch_iter(const IterArgs& a, int mode, int nt, int npatch, size_t smem, int k, int res_only,
                         cudaStream_t s);
-cudaError_t launch_predict(const float4* X, const float4* V, const float4* aux, const float* mass,
-                           const int* vcloth, const ClothInfo* cinfo, const float4* warm, float4* Y,
-                           float4* A, float4* B, ClothRT* crt, int n, int ncloth, cudaStream_t s);
-cudaError_t launch_finalize(float4* X, float4* V, const float4* Y, const float4* A, const float4* B,
-                            const float4* aux, const int* vcloth, const ClothInfo* cinfo, ClothRT* crt, int n,
-                            int ncloth, int have_final, cudaStream_t s);
+cudaError_t launch_predict(const IterArgs& a, const float4* X, const float4* V, const float4* aux,
+                           const float* mass, const int* vcloth, const float4* warm, int n, cudaStream_t s);
+cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float4* aux, const int* vcloth, int n,
+                            cudaStream_t s);
 cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s);
 cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s);
 cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P,
@@ -39,6 +37,12 @@ struct PersistArgs {
     unsigned* bar;       // [0] arrive counter, [1] generation
     int* err;            // set when a grid barrier times out
     long long spin_budget;  // clock64 cycles a barrier may wait
+    // neighbour synchronisation of the resident kernel (fixed sweep counts)
+    const int* nbr_ptr;  // npatch + 1
+    const int* nbr;      // patches owning halo vertices of each patch
+    unsigned long long* pflag;   // per patch: last (frame, sweep) mark completed
+    unsigned long long frame_seq;  // increments every frame
+    int nbr_sync;        // 1: sweeps wait for neighbour patches only
 };
 cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s);
 int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);

@@ -66,7 +66,6 @@ struct ClothRT {
     double res_y2;           // ||r(y_pinned)||^2
     double res0_2;           // ||r(x^0)||^2
     double resf_2;           // ||r(x^used)||^2, -1 if not evaluated
-    double acc[3];           // residual^2 accumulators, slot k % 3
 };
 
 // Arguments of one fused sweep.
@@ -83,6 +82,8 @@ struct IterArgs {
     int              omega_stride;
     const float4*    Y;           // inertial prediction, w = mass
     float4*          buf[2];      // iterate ping-pong, w = inv_diag (>= 0) or -1 (pinned)
+    double*          acc;         // ||r(x^k)||^2 per cloth and sweep k
+    int              acc_stride;  // sweeps + 1
     int              ncloth;
     int              have_final;  // evaluate r(x^max_iter) in an extra sweep
 };

@@ -39,6 +39,7 @@ struct HostLayout {
     std::vector<HingeRec> hinges;
     std::vector<int> csr_ptr;
     std::vector<uint16_t> csr_ent;
+    std::vector<int> nbr_ptr, nbr;  // patches owning each patch's halo vertices
 };
 
 bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout& L, std::string& err);
@@ -84,7 +85,12 @@ struct pdg_solver {
 
     pdg::DevBuf<float4> X, V, Y, A, B, aux, warm;
     pdg::DevBuf<float> mass, omega, stage_x, stage_v;
-    pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, err;
+    pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, err, nbr_ptr, nbr;
+    pdg::DevBuf<double> acc;
+    pdg::DevBuf<unsigned long long> pflag;
+    unsigned long long frame_seq = 0;
+    int acc_stride = 1;
+    int nbr_sync = 0;
     pdg::DevBuf<uint16_t> csr_ent;
     pdg::DevBuf<pdg::PatchHdr> patches;
     pdg::DevBuf<pdg::TriRec> tris;

@@ -59,7 +59,14 @@ int upload_all(pdg_solver* s)
     CK(s->tris.upload(L.tris, st));
     CK(s->hinges.upload(L.hinges, st));
     CK(s->cinfo.upload(L.cinfo, st));
+    CK(s->nbr_ptr.upload(L.nbr_ptr, st));
+    CK(s->nbr.upload(L.nbr, st));
     CK(s->crt.alloc(L.ncloth));
+    s->acc_stride = L.cap + 2;
+    CK(s->acc.alloc((size_t)L.ncloth * s->acc_stride));
+    CK(cudaMemsetAsync(s->acc.p, 0, sizeof(double) * (size_t)L.ncloth * s->acc_stride, st));
+    CK(s->pflag.alloc(L.npatch));
+    CK(cudaMemsetAsync(s->pflag.p, 0, sizeof(unsigned long long) * L.npatch, st));
     CK(s->X.alloc(L.ntot)); CK(s->V.alloc(L.ntot)); CK(s->Y.alloc(L.ntot));
     CK(s->A.alloc(L.ntot)); CK(s->B.alloc(L.ntot));
     CK(s->stage_x.alloc(3 * (size_t)L.ntot)); CK(s->stage_v.alloc(3 * (size_t)L.ntot));
@@ -89,6 +96,7 @@ IterArgs iter_args(pdg_solver* s)
     a.csr_ptr = s->csr_ptr.p; a.csr_ent = s->csr_ent.p; a.cinfo = s->cinfo.p; a.crt = s->crt.p;
     a.omega = s->omega.p; a.omega_stride = s->L.omega_stride;
     a.Y = s->Y.p; a.buf[0] = s->A.p; a.buf[1] = s->B.p; a.ncloth = s->L.ncloth;
+    a.acc = s->acc.p; a.acc_stride = s->acc_stride;
     a.have_final = s->have_final;
     return a;
 }
@@ -101,7 +109,10 @@ PersistArgs persist_args(pdg_solver* s)
     p.warm = s->warm_valid ? s->warm.p : nullptr; p.Y = s->Y.p;
     p.n = s->L.ntot; p.npatch = s->L.npatch; p.max_iter = s->L.cap; p.have_final = s->have_final;
     p.mode = s->mode; p.bar = s->bar.p; p.err = s->err.p;
-    p.spin_budget = 2000000000LL;   // ~1 s at 2 GHz per barrier
+    p.spin_budget = 2000000000LL;   // ~1 s at 2 GHz per wait
+    p.nbr_ptr = s->nbr_ptr.p; p.nbr = s->nbr.p; p.pflag = s->pflag.p;
+    p.frame_seq = ++s->frame_seq;
+    p.nbr_sync = s->nbr_sync;
     return p;
 }
 
@@ -110,13 +121,12 @@ int enqueue_frame(pdg_solver* s)
 {
     const HostLayout& L = s->L;
     cudaStream_t st = s->stream;
-    CK(launch_predict(s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, s->cinfo.p,
-                      s->warm_valid ? s->warm.p : nullptr, s->Y.p, s->A.p, s->B.p, s->crt.p, L.ntot, L.ncloth, st));
     const IterArgs a = iter_args(s);
+    CK(launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, s->warm_valid ? s->warm.p : nullptr,
+                      L.ntot, st));
     for (int k = 0; k < L.cap; ++k) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st));
     if (s->have_final) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st));
-    CK(launch_finalize(s->X.p, s->V.p, s->Y.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p, L.ntot,
-                       L.ncloth, s->have_final, st));
+    CK(launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st));
     return PDG_OK;
 }
 
@@ -191,6 +201,10 @@ int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, co
             s->patch_verts = P;
             s->nt = rnt;
             s->persist_grid = s->L.npatch;
+            // fixed sweep counts: neighbour-only synchronisation between sweeps
+            s->nbr_sync = 1;
+            for (const auto& c : s->cloths)
+                if (c.cfg.tolerance > 0.f) s->nbr_sync = 0;
         } else if (c0.kernel == PDG_KERNEL_RESIDENT) {
             return set_error(PDG_ERR_ARG, "resident kernel does not fit this problem (%d patches of %d vertices)",
                              s->L.npatch, P);
@@ -444,18 +458,15 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
             s->launches += 1;
             cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
         } else {
-            cudaError_t err = launch_predict(s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, s->cinfo.p,
-                                             s->warm_valid ? s->warm.p : nullptr, s->Y.p, s->A.p, s->B.p, s->crt.p,
-                                             L.ntot, L.ncloth, st);
-            cudaEventRecord(e[1], st);
             const IterArgs a = iter_args(s);
+            cudaError_t err = launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p,
+                                             s->warm_valid ? s->warm.p : nullptr, L.ntot, st);
+            cudaEventRecord(e[1], st);
             for (int k = 0; k < L.cap && err == cudaSuccess; ++k)
                 err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st);
             cudaEventRecord(e[2], st);
             if (err == cudaSuccess && s->have_final) err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st);
-            if (err == cudaSuccess)
-                err = launch_finalize(s->X.p, s->V.p, s->Y.p, s->A.p, s->B.p, s->aux.p, s->vcloth.p, s->cinfo.p, s->crt.p,
-                                      L.ntot, L.ncloth, s->have_final, st);
+            if (err == cudaSuccess) err = launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "frame launch: %s", cudaGetErrorString(err));
             s->launches += s->kernels_per_frame;
         }
