@@ -53,7 +53,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         glob.glob(os.path.join(ROOT, "include", "*.h")) + [os.path.abspath(__file__)]
     cxx_flags = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
-    nv_flags = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3",
+    # host code of the .cu files is compiled without FMA contraction too, so
+    # host-side arithmetic (Chebyshev weights) rounds the same on x86 and Arm
+    nv_flags = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-O3",
                 "--expt-relaxed-constexpr"]
     jobs = []
     objs = []

@@ -128,14 +128,14 @@ __device__ __forceinline__ float3 edge(const float4* sy, const float4* sd, int i
 // Triangle phase for one local triangle: writes the contributions of its
 // three corners.  Slots are corner-major (corner c of local triangle lt at
 // c*ntri + lt), so a warp's stores are unit-stride and free of bank conflicts.
+// Corner contributions of one triangle from its two edge vectors:
+// c_v = h^2 wA sum_col coef_{v,col} (R - F)_col (consistent) or with R alone
+// (literal), coef from Dm_inv G = (g00, g10, g01, g11).
 template <int MODE>
-__device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
-                                                 int ntri, float* cx, float* cy, float* cz)
+__device__ __forceinline__ void tri_force(float3 d1, float3 d2, float4 G, float h2wA, float3& c0, float3& c1,
+                                          float3& c2)
 {
-    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2;
-    const float g00 = r.G.x, g10 = r.G.y, g01 = r.G.z, g11 = r.G.w;
-    const float3 d1 = edge(sy, sd, i0, i1);
-    const float3 d2 = edge(sy, sd, i0, i2);
+    const float g00 = G.x, g10 = G.y, g01 = G.z, g11 = G.w;
     const float3 F0 = make_float3(ffma(d1.x, g00, fmul(d2.x, g10)), ffma(d1.y, g00, fmul(d2.y, g10)),
                                   ffma(d1.z, g00, fmul(d2.z, g10)));
     const float3 F1 = make_float3(ffma(d1.x, g01, fmul(d2.x, g11)), ffma(d1.y, g01, fmul(d2.y, g11)),
@@ -143,48 +143,66 @@ __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* 
     float3 R0, R1, q0, q1;
     if (MODE == kModeConsistent) {
         polar_consistent(F0, F1, R0, R1);
-        q0 = make_float3(fmul(r.h2wA, fsub(R0.x, F0.x)), fmul(r.h2wA, fsub(R0.y, F0.y)), fmul(r.h2wA, fsub(R0.z, F0.z)));
-        q1 = make_float3(fmul(r.h2wA, fsub(R1.x, F1.x)), fmul(r.h2wA, fsub(R1.y, F1.y)), fmul(r.h2wA, fsub(R1.z, F1.z)));
+        q0 = make_float3(fmul(h2wA, fsub(R0.x, F0.x)), fmul(h2wA, fsub(R0.y, F0.y)), fmul(h2wA, fsub(R0.z, F0.z)));
+        q1 = make_float3(fmul(h2wA, fsub(R1.x, F1.x)), fmul(h2wA, fsub(R1.y, F1.y)), fmul(h2wA, fsub(R1.z, F1.z)));
     } else {
         polar_literal(F0, F1, R0, R1);
-        q0 = scale3(R0, r.h2wA);
-        q1 = scale3(R1, r.h2wA);
+        q0 = scale3(R0, h2wA);
+        q1 = scale3(R1, h2wA);
     }
     const float s0 = -fadd(g00, g10), s1 = -fadd(g01, g11);
+    c0 = make_float3(ffma(s0, q0.x, fmul(s1, q1.x)), ffma(s0, q0.y, fmul(s1, q1.y)), ffma(s0, q0.z, fmul(s1, q1.z)));
+    c1 = make_float3(ffma(g00, q0.x, fmul(g01, q1.x)), ffma(g00, q0.y, fmul(g01, q1.y)), ffma(g00, q0.z, fmul(g01, q1.z)));
+    c2 = make_float3(ffma(g10, q0.x, fmul(g11, q1.x)), ffma(g10, q0.y, fmul(g11, q1.y)), ffma(g10, q0.z, fmul(g11, q1.z)));
+}
+
+template <int MODE>
+__device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
+                                                 int ntri, float* cx, float* cy, float* cz)
+{
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2;
+    float3 c0, c1, c2;
+    tri_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), r.G, r.h2wA, c0, c1, c2);
     const int b1 = ntri + lt, b2 = 2 * ntri + lt;
-    cx[lt] = ffma(s0, q0.x, fmul(s1, q1.x));  cy[lt] = ffma(s0, q0.y, fmul(s1, q1.y));  cz[lt] = ffma(s0, q0.z, fmul(s1, q1.z));
-    cx[b1] = ffma(g00, q0.x, fmul(g01, q1.x)); cy[b1] = ffma(g00, q0.y, fmul(g01, q1.y)); cz[b1] = ffma(g00, q0.z, fmul(g01, q1.z));
-    cx[b2] = ffma(g10, q0.x, fmul(g11, q1.x)); cy[b2] = ffma(g10, q0.y, fmul(g11, q1.y)); cz[b2] = ffma(g10, q0.z, fmul(g11, q1.z));
+    cx[lt] = c0.x; cy[lt] = c0.y; cz[lt] = c0.z;
+    cx[b1] = c1.x; cy[b1] = c1.y; cz[b1] = c1.z;
+    cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z;
 }
 
 // Hinge phase: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
 // n_rest <= 1e-10, src/pd_solver.cu:304-335); slot s gets h^2 k w_s (p - e)
 // (consistent) or h^2 k w_s p (literal).  Slot s of local hinge e sits at
 // hbase + s*nhin + e.
+// Bending "force" q of one hinge (slot s receives w_s q): e = sum w_i x_i
+// formed as sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0 from edge vectors.
 template <int MODE>
-__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int e_,
-                                              int hbase, int nhin, float* cx, float* cy, float* cz)
+__device__ __forceinline__ float3 hinge_force(float3 e1, float3 e2, float3 e3, float3 x0, float4 w, float h2k,
+                                              float nrest)
 {
-    // e = sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0
-    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
-    const float3 e1 = edge(sy, sd, i0, i1), e2 = edge(sy, sd, i0, i2), e3 = edge(sy, sd, i0, i3);
-    const float4 w = r.w;
     const float ws = fadd(fadd(w.x, w.y), fadd(w.z, w.w));
-    const float4 y0 = sy[i0], d0 = sd[i0];
-    const float3 x0 = make_float3(fadd(y0.x, d0.x), fadd(y0.y, d0.y), fadd(y0.z, d0.z));
     const float3 e = make_float3(ffma(w.y, e1.x, ffma(w.z, e2.x, ffma(w.w, e3.x, fmul(ws, x0.x)))),
                                  ffma(w.y, e1.y, ffma(w.z, e2.y, ffma(w.w, e3.y, fmul(ws, x0.y)))),
                                  ffma(w.y, e1.z, ffma(w.z, e2.z, ffma(w.w, e3.z, fmul(ws, x0.z)))));
     float3 p = make_float3(0.f, 0.f, 0.f);
-    if (r.nrest > 1e-10f) {
+    if (nrest > 1e-10f) {
         const float len = __fsqrt_rn(dot3(e, e));
-        if (len > 1e-10f) p = scale3(e, fdiv(r.nrest, len));
+        if (len > 1e-10f) p = scale3(e, fdiv(nrest, len));
     }
-    float3 q;
     if (MODE == kModeConsistent)
-        q = make_float3(fmul(r.h2k, fsub(p.x, e.x)), fmul(r.h2k, fsub(p.y, e.y)), fmul(r.h2k, fsub(p.z, e.z)));
-    else
-        q = scale3(p, r.h2k);
+        return make_float3(fmul(h2k, fsub(p.x, e.x)), fmul(h2k, fsub(p.y, e.y)), fmul(h2k, fsub(p.z, e.z)));
+    return scale3(p, h2k);
+}
+
+template <int MODE>
+__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int e_,
+                                              int hbase, int nhin, float* cx, float* cy, float* cz)
+{
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
+    const float4 y0 = sy[i0], d0 = sd[i0];
+    const float3 x0 = make_float3(fadd(y0.x, d0.x), fadd(y0.y, d0.y), fadd(y0.z, d0.z));
+    const float4 w = r.w;
+    const float3 q = hinge_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), edge(sy, sd, i0, i3), x0, w,
+                                       r.h2k, r.nrest);
     const int s0 = hbase + e_, s1 = s0 + nhin, s2 = s1 + nhin, s3 = s2 + nhin;
     cx[s0] = fmul(w.x, q.x); cy[s0] = fmul(w.x, q.y); cz[s0] = fmul(w.x, q.z);
     cx[s1] = fmul(w.y, q.x); cy[s1] = fmul(w.y, q.y); cz[s1] = fmul(w.y, q.z);

@@ -202,6 +202,33 @@ int  pdg_solver_launch_info(const pdg_solver* s, int* kernel, int* patch_verts,
                             int* block_threads, int* npatches);
 void pdg_solver_destroy(pdg_solver* s);
 
+/* ---------------- allocation-free frame ----------------------------------
+ * No counterpart in the reference.  One frame of the consistent solve (the
+ * arithmetic of pdg_solver_step, results equal to rounding) for callers that
+ * cannot call cudaMalloc: applications that own all device memory through
+ * their own pool and load this library as a plugin, and real-time loops that
+ * cannot afford the device-wide synchronisation of cudaMalloc/cudaFree.
+ * Inputs are the cloth in the reference's own device layout -- the arrays of
+ * ClothMesh (pos, vel, mass, tris, Dm_inv, rest area), SimConstraints
+ * (stretch k, Jacobi diagonal for cfg->dt, bend quads/w/n/k) and Constraints
+ * (pin indices and targets); d_pos and d_vel are updated in place.  It
+ * allocates nothing: its work arrays live in one static device array of about
+ * 8.4 MB that every GPU loading the library keeps until exit, so N is limited
+ * to PDG_NOALLOC_MAX_VERTS and the sweep count to PDG_NOALLOC_MAX_ITERS
+ * (larger sizes return PDG_ERR_ARG).  The first call on a device looks up the
+ * array's device address; make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU (other streams or host threads)
+ * race.  Only PDG_MODE_CONSISTENT with PDG_INIT_INERTIAL.  stats: NULL or one
+ * host struct (filling it synchronises the stream). */
+#define PDG_NOALLOC_MAX_VERTS 131072
+#define PDG_NOALLOC_MAX_ITERS 4096
+int  pdg_step_noalloc(const pdg_config* cfg, int N, float* d_pos, float* d_vel, const float* d_mass,
+                      const float* d_jacobi_diag, int T, const int* d_tris, const float* d_Dm_inv,
+                      const float* d_rest_area, const float* d_stretch_k, int E, const int* d_bend_quads,
+                      const float* d_bend_w, const float* d_bend_n, const float* d_bend_k, int P,
+                      const int* d_pin_idx, const float* d_pin_target, void* stream,
+                      pdg_frame_stats* stats);
+
 /* launch_apply_constraints_kernel (include/pd_solver.h:74-77): set
  * d_pos[idx] = target and d_vel[idx] = 0 for P pinned vertices, AoS xyz
  * device arrays, on `stream`. */
