@@ -1,0 +1,62 @@
+"""Synthetic workloads of the PD cloth solver (meshes, constraints, configs).
+
+All scenes are generated from seeds through the C ABI; no dataset is involved.
+
+  hanging(n, side, ...)   square cloth in the x-y plane, row 0 on top, two top
+                          corners pinned, alternating diagonals, z jitter
+                          N(0, 1e-4) -- the plain single-cloth workloads
+  batch(count, seed)      many cloths of uneven size: grid side n ~ U{17..129},
+                          size ~ U[0.5, 2] m, 1-4 random boundary pins, stretch
+                          k log-uniform [1e2, 1e4], bend k log-uniform
+                          [1e-3, 1e-1], constant wind N(0, 2 m/s^2) per axis
+"""
+from __future__ import annotations
+
+import numpy as np
+
+import pdg
+
+H = 1.0 / 60.0
+G = -9.81
+
+
+def hanging(n, side, ks=1e3, kb=1e-2, seed=0, mtype=1, jitter=1e-4, pins="corners"):
+    m = pdg.Mesh.hanging(n, side, mtype=mtype, jitter=jitter, seed=seed)
+    c = pdg.Constraints(m).build_stretch(ks)
+    if kb > 0:
+        c.build_bend(kb)
+    if pins == "corners":
+        c.pin_corners(n)
+    elif pins == "top":
+        c.pin_top_row(n)
+    return m, c
+
+
+def boundary_vertices(n):
+    """Indices of the boundary vertices of an n x n grid (generator order)."""
+    idx = [j for j in range(n)] + [(n - 1) * n + j for j in range(n)]
+    idx += [i * n for i in range(1, n - 1)] + [i * n + n - 1 for i in range(1, n - 1)]
+    return np.array(sorted(set(idx)), np.int32)
+
+
+def batch(count, seed=0, *, max_iterations=200, tolerance=1e-5, rho=0.99, n_range=(17, 129),
+          size_range=(0.5, 2.0), **cfg_kw):
+    """(meshes, constraints, configs, params) of `count` cloths drawn from
+    the batched-workload distribution."""
+    rng = np.random.default_rng(seed)
+    meshes, cons, cfgs, params = [], [], [], []
+    for i in range(count):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        size = float(rng.uniform(*size_range))
+        ks = float(10 ** rng.uniform(2, 4))
+        kb = float(10 ** rng.uniform(-3, -1))
+        wind = rng.normal(0.0, 2.0, 3).astype(np.float32)
+        npins = int(rng.integers(1, 5))
+        pins = rng.choice(boundary_vertices(n), size=npins, replace=False).astype(np.int32)
+        m = pdg.Mesh.hanging(n, size, mtype=1, jitter=1e-4, seed=int(rng.integers(1 << 31)))
+        c = pdg.Constraints(m).build_stretch(ks).build_bend(kb).set_pins(pins)
+        cfg = pdg.Config.default(max_iterations=max_iterations, tolerance=tolerance, rho=rho, dt=H, gravity=G,
+                                 wind=tuple(float(w) for w in wind), **cfg_kw)
+        meshes.append(m); cons.append(c); cfgs.append(cfg)
+        params.append(dict(n=n, size=size, ks=ks, kb=kb, wind=wind.tolist(), pins=pins.tolist()))
+    return meshes, cons, cfgs, params
