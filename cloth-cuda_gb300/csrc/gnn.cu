@@ -1,0 +1,451 @@
+// Learned warm start: host side and C ABI (no counterpart in the reference).
+// The kernels live in gnn_kernels.cuh; this file owns the parameters, the
+// activation buffers, the training step and the binding to a solver.
+#include "gnn_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+using namespace pdg;
+using namespace pdg::gnn;
+
+#define GK(call)                                                                                \
+    do {                                                                                        \
+        const cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                                  \
+            return set_error(e_ == cudaErrorMemoryAllocation ? PDG_ERR_ALLOC : PDG_ERR_CUDA,    \
+                             "warm start: %s: %s", #call, cudaGetErrorString(e_));              \
+    } while (0)
+
+struct pdg_warmstart {
+    Layout lay;
+    long long t = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    DevBuf<float> p, g, m, v, bdp;
+    DevBuf<bf16> wbuf;
+    Bf16Weights W{};
+    // graph and activations
+    int N = 0, E = 0;
+    DevBuf<int> ptr, adj, rev;
+    DevBuf<float> rest, deg_inv;
+    DevBuf<float4> ef, stat, Xn, Vn;
+    DevBuf<bf16> xin, cat[L], pq[L], uo[L], hfin;
+    DevBuf<float> out, target, freew, dout, dh, dtmp, dcat, dpq;
+    DevBuf<double> loss;
+    pdg_solver* solver = nullptr;
+    ~pdg_warmstart()
+    {
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+inline int nb(long long n, int b) { return (int)((n + b - 1) / b); }
+
+int refresh_bf16(pdg_warmstart* w, cudaStream_t st)
+{
+    const Layout& y = w->lay;
+    const float* p = w->p.p;
+    k_to_bf16<<<nb(H * NF, 256), 256, 0, st>>>(p + y.We, H, NF, w->W.We, NFP, nullptr, 0);
+    for (int l = 0; l < L; ++l) {
+        k_to_bf16<<<nb(H * H, 256), 256, 0, st>>>(p + y.A[l], H, H, w->W.AB[l], H, w->W.ABt[l], 2 * H);
+        k_to_bf16<<<nb(H * H, 256), 256, 0, st>>>(p + y.B[l], H, H, w->W.AB[l] + H * H, H, w->W.ABt[l] + H, 2 * H);
+        k_to_bf16<<<nb(H * 2 * H, 256), 256, 0, st>>>(p + y.U[l], H, 2 * H, w->W.U[l], 2 * H, w->W.Ut[l], H);
+    }
+    k_to_bf16<<<nb(NO * H, 256), 256, 0, st>>>(p + y.Wd, NO, H, w->W.Wd, H, w->W.Wdt, 16);
+    GK(cudaMemcpyAsync(w->bdp.p, p + y.bd, sizeof(float) * NO, cudaMemcpyDeviceToDevice, st));
+    GK(cudaGetLastError());
+    return PDG_OK;
+}
+
+int alloc_params(pdg_warmstart* w)
+{
+    const int n = w->lay.total;
+    GK(w->p.alloc(n)); GK(w->g.alloc(n)); GK(w->m.alloc(n)); GK(w->v.alloc(n)); GK(w->bdp.alloc(16));
+    // bf16 copies: We 64x16, per layer AB 128x64, ABt 64x128, U 64x128, Ut 128x64, Wd 16x64, Wdt 64x16
+    const size_t sizes[] = {(size_t)H * NFP, 2u * H * H, 2u * H * H, 2u * H * H, 2u * H * H, 16u * H, (size_t)H * 16};
+    size_t total = sizes[0] + L * (sizes[1] + sizes[2] + sizes[3] + sizes[4]) + sizes[5] + sizes[6];
+    GK(w->wbuf.alloc(total));
+    GK(cudaMemset(w->wbuf.p, 0, sizeof(bf16) * total));
+    GK(cudaMemset(w->bdp.p, 0, sizeof(float) * 16));
+    bf16* q = w->wbuf.p;
+    w->W.We = q; q += sizes[0];
+    for (int l = 0; l < L; ++l) {
+        w->W.AB[l] = q; q += sizes[1];
+        w->W.ABt[l] = q; q += sizes[2];
+        w->W.U[l] = q; q += sizes[3];
+        w->W.Ut[l] = q; q += sizes[4];
+    }
+    w->W.Wd = q; q += sizes[5];
+    w->W.Wdt = q;
+    GK(cudaMemset(w->g.p, 0, sizeof(float) * n));
+    GK(cudaMemset(w->m.p, 0, sizeof(float) * n));
+    GK(cudaMemset(w->v.p, 0, sizeof(float) * n));
+    return PDG_OK;
+}
+
+// activation buffers for N nodes and E directed edges
+int alloc_graph(pdg_warmstart* w, int N, int E)
+{
+    w->N = N; w->E = E;
+    GK(w->ptr.alloc(N + 1)); GK(w->adj.alloc(E)); GK(w->rev.alloc(E));
+    GK(w->rest.alloc(E)); GK(w->deg_inv.alloc(N)); GK(w->ef.alloc(E)); GK(w->stat.alloc(N));
+    GK(w->Xn.alloc(N)); GK(w->Vn.alloc(N));
+    GK(w->xin.alloc((size_t)N * NFP));
+    for (int l = 0; l < L; ++l) {
+        GK(w->cat[l].alloc((size_t)N * 2 * H)); GK(w->pq[l].alloc((size_t)N * 2 * H)); GK(w->uo[l].alloc((size_t)N * H));
+    }
+    GK(w->hfin.alloc((size_t)N * H));
+    GK(w->out.alloc((size_t)N * 16)); GK(w->target.alloc((size_t)N * 3)); GK(w->freew.alloc(N));
+    GK(w->dout.alloc((size_t)N * 16)); GK(w->dh.alloc((size_t)N * H)); GK(w->dtmp.alloc((size_t)N * H));
+    GK(w->dcat.alloc((size_t)N * 2 * H)); GK(w->dpq.alloc((size_t)N * 2 * H)); GK(w->loss.alloc(1));
+    return PDG_OK;
+}
+
+int forward(pdg_warmstart* w, cudaStream_t st)
+{
+    const int N = w->N, gb = nb(N, 64);
+    const Layout& y = w->lay;
+    const float* p = w->p.p;
+    k_gemm<bf16, NFP, H, EPI_RELU | EPI_STORE1><<<gb, 128, 0, st>>>(w->xin.p, NFP, N, w->W.We, p + y.be, nullptr, 0,
+                                                                    w->cat[0].p, 2 * H, nullptr, 0, nullptr, 0);
+    for (int l = 0; l < L; ++l) {
+        k_gemm<bf16, H, 2 * H, EPI_STORE1><<<gb, 128, 0, st>>>(w->cat[l].p, 2 * H, N, w->W.AB[l], nullptr, nullptr, 0,
+                                                               w->pq[l].p, 2 * H, nullptr, 0, nullptr, 0);
+        k_msg_fwd<<<nb((long long)N * 32, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->ef.p, w->deg_inv.p, w->pq[l].p,
+                                                             p + y.C[l], p + y.c[l], w->cat[l].p);
+        bf16* next = l + 1 < L ? w->cat[l + 1].p : w->hfin.p;
+        const int ldn = l + 1 < L ? 2 * H : H;
+        k_gemm<bf16, 2 * H, H, EPI_RELU | EPI_STORE1 | EPI_RESID2><<<gb, 128, 0, st>>>(
+            w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l], w->cat[l].p, 2 * H, w->uo[l].p, H, next, ldn, nullptr, 0);
+    }
+    k_gemm<bf16, H, 16, EPI_STOREF><<<gb, 128, 0, st>>>(w->hfin.p, H, N, w->W.Wd, w->bdp.p, nullptr, 0, nullptr, 0,
+                                                        nullptr, 0, w->out.p, 16);
+    GK(cudaGetLastError());
+    return PDG_OK;
+}
+
+int wgrad_grid(int M) { return std::max(1, std::min(304, nb(M, 32))); }
+
+// gradients of the loss w.r.t. all parameters into w->g (zeroed here);
+// loss accumulated into w->loss
+int backward(pdg_warmstart* w, float inv_cnt, cudaStream_t st)
+{
+    const int N = w->N, gb = nb(N, 64), gw = wgrad_grid(N);
+    const Layout& y = w->lay;
+    const float* p = w->p.p;
+    float* g = w->g.p;
+    GK(cudaMemsetAsync(g, 0, sizeof(float) * y.total, st));
+    GK(cudaMemsetAsync(w->loss.p, 0, sizeof(double), st));
+    k_loss<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, w->target.p, w->freew.p, inv_cnt, w->dout.p, w->loss.p);
+    k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dout.p, 16, NO, w->hfin.p, H, H, N, g + y.Wd, g + y.bd);
+    k_gemm<float, 16, H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dout.p, 16, N, w->W.Wdt, nullptr, nullptr, 0, nullptr, 0,
+                                                         nullptr, 0, w->dh.p, H);
+    for (int l = L - 1; l >= 0; --l) {
+        k_relu_bwd<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dh.p, H, w->uo[l].p, H, w->dtmp.p, H);
+        k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dtmp.p, H, H, w->cat[l].p, 2 * H, 2 * H, N, g + y.U[l], g + y.u[l]);
+        k_gemm<float, H, 2 * H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dtmp.p, H, N, w->W.Ut[l], nullptr, nullptr, 0,
+                                                                nullptr, 0, nullptr, 0, w->dcat.p, 2 * H);
+        k_add<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dcat.p, 2 * H, w->dh.p, H);
+        k_msg_bwd<<<std::max(1, std::min(4 * 152, nb(N, 8))), 256, 0, st>>>(
+            N, w->ptr.p, w->adj.p, w->rev.p, w->ef.p, w->deg_inv.p, w->pq[l].p, p + y.C[l], p + y.c[l], w->dcat.p,
+            w->dpq.p, g + y.C[l], g + y.c[l]);
+        k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dpq.p, 2 * H, 2 * H, w->cat[l].p, 2 * H, H, N, g + y.A[l], nullptr);
+        k_gemm<float, 2 * H, H, EPI_ACCF><<<gb, 128, 0, st>>>(w->dpq.p, 2 * H, N, w->W.ABt[l], nullptr, nullptr, 0,
+                                                              nullptr, 0, nullptr, 0, w->dh.p, H);
+    }
+    k_relu_bwd<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dh.p, H, w->cat[0].p, 2 * H, w->dtmp.p, H);
+    k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dtmp.p, H, H, w->xin.p, NFP, NF, N, g + y.We, g + y.be);
+    GK(cudaGetLastError());
+    return PDG_OK;
+}
+
+int adam_step(pdg_warmstart* w, float lr, cudaStream_t st)
+{
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    w->t += 1;
+    const float bc1 = 1.f - (float)std::pow((double)b1, (double)w->t);
+    const float bc2 = 1.f - (float)std::pow((double)b2, (double)w->t);
+    k_adam<<<nb(w->lay.total, 256), 256, 0, st>>>(w->lay.total, w->p.p, w->g.p, w->m.p, w->v.p, lr, b1, b2, eps, bc1,
+                                                  bc2);
+    GK(cudaGetLastError());
+    return refresh_bf16(w, st);
+}
+
+// reverse-edge index of a symmetric CSR; false if some edge has no reverse
+bool reverse_edges(int N, const std::vector<int>& ptr, const std::vector<int>& adj, std::vector<int>& rev)
+{
+    rev.assign(adj.size(), -1);
+    for (int i = 0; i < N; ++i)
+        for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+            const int j = adj[e];
+            if (j < 0 || j >= N) return false;
+            for (int f = ptr[j]; f < ptr[j + 1]; ++f)
+                if (adj[f] == i) { rev[e] = f; break; }
+            if (rev[e] < 0) return false;
+        }
+    return true;
+}
+
+int upload_graph(pdg_warmstart* w, const std::vector<int>& ptr, const std::vector<int>& adj, cudaStream_t st)
+{
+    const int N = (int)ptr.size() - 1;
+    std::vector<int> rev;
+    if (!reverse_edges(N, ptr, adj, rev)) return set_error(PDG_ERR_ARG, "warm start: adjacency is not symmetric");
+    std::vector<float> dinv(N);
+    for (int i = 0; i < N; ++i) dinv[i] = ptr[i + 1] > ptr[i] ? 1.f / (float)(ptr[i + 1] - ptr[i]) : 0.f;
+    const int rc = alloc_graph(w, N, (int)adj.size());
+    if (rc) return rc;
+    GK(cudaMemcpyAsync(w->ptr.p, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, st));
+    if (!adj.empty()) {
+        GK(cudaMemcpyAsync(w->adj.p, adj.data(), sizeof(int) * adj.size(), cudaMemcpyHostToDevice, st));
+        GK(cudaMemcpyAsync(w->rev.p, rev.data(), sizeof(int) * rev.size(), cudaMemcpyHostToDevice, st));
+    }
+    GK(cudaMemcpyAsync(w->deg_inv.p, dinv.data(), sizeof(float) * N, cudaMemcpyHostToDevice, st));
+    GK(cudaStreamSynchronize(st));
+    return PDG_OK;
+}
+
+}  // namespace
+
+// ---- solver-side hooks (declared in pdg_solver.h) -------------------------
+namespace pdg {
+
+int warm_infer_enqueue(pdg_warmstart* w, pdg_solver* s)
+{
+    cudaStream_t st = s->stream;
+    const int N = w->N;
+    k_node_feat<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->V.p, s->Y.p, s->aux.p, w->stat.p, s->vcloth.p, s->cinfo.p,
+                                            w->xin.p);
+    k_edge_feat<<<nb(N, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rest.p, s->Y.p, w->ef.p);
+    const int rc = forward(w, st);
+    if (rc) return rc;
+    k_warm_out<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, s->A.p, s->warm.p);
+    GK(cudaGetLastError());
+    return PDG_OK;
+}
+
+int warm_kernel_count() { return 3 + 1 + 3 * L + 1; }
+
+void warm_detach(pdg_warmstart* w)
+{
+    if (w) w->solver = nullptr;
+}
+
+}  // namespace pdg
+
+extern "C" {
+
+int pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out)
+{
+    if (!out) return set_error(PDG_ERR_ARG, "pdg_warmstart_create: null output");
+    std::unique_ptr<pdg_warmstart> w(new pdg_warmstart);
+    GK(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+    w->own_stream = true;
+    int rc = alloc_params(w.get());
+    if (rc) return rc;
+    // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases; the
+    // decoder starts 10x smaller so the first predictions sit near y
+    const Layout& y = w->lay;
+    std::vector<float> h(y.total, 0.f);
+    std::mt19937_64 rng(seed);
+    auto fill = [&](int off, int rows, int cols, float gain) {
+        std::uniform_real_distribution<float> U(-gain / std::sqrt((float)cols), gain / std::sqrt((float)cols));
+        for (int i = 0; i < rows * cols; ++i) h[off + i] = U(rng);
+    };
+    fill(y.We, H, NF, 1.f);
+    for (int l = 0; l < L; ++l) {
+        fill(y.A[l], H, H, 1.f); fill(y.B[l], H, H, 1.f); fill(y.C[l], H, EF, 1.f); fill(y.U[l], H, 2 * H, 1.f);
+    }
+    fill(y.Wd, NO, H, 0.1f);
+    GK(cudaMemcpy(w->p.p, h.data(), sizeof(float) * y.total, cudaMemcpyHostToDevice));
+    rc = refresh_bf16(w.get(), w->stream);
+    if (rc) return rc;
+    GK(cudaStreamSynchronize(w->stream));
+    *out = w.release();
+    return PDG_OK;
+}
+
+int pdg_warmstart_param_count(const pdg_warmstart* w, int* n)
+{
+    if (!w || !n) return set_error(PDG_ERR_ARG, "null argument");
+    *n = w->lay.total;
+    return PDG_OK;
+}
+
+int pdg_warmstart_get_params(pdg_warmstart* w, float* host)
+{
+    if (!w || !host) return set_error(PDG_ERR_ARG, "null argument");
+    GK(cudaStreamSynchronize(w->stream));
+    if (w->solver) GK(cudaStreamSynchronize(w->solver->stream));
+    GK(cudaMemcpy(host, w->p.p, sizeof(float) * w->lay.total, cudaMemcpyDeviceToHost));
+    return PDG_OK;
+}
+
+int pdg_warmstart_set_params(pdg_warmstart* w, const float* host)
+{
+    if (!w || !host) return set_error(PDG_ERR_ARG, "null argument");
+    for (int i = 0; i < w->lay.total; ++i)
+        if (!std::isfinite(host[i])) return set_error(PDG_ERR_ARG, "non-finite parameter %d", i);
+    GK(cudaStreamSynchronize(w->stream));
+    if (w->solver) GK(cudaStreamSynchronize(w->solver->stream));
+    GK(cudaMemcpy(w->p.p, host, sizeof(float) * w->lay.total, cudaMemcpyHostToDevice));
+    GK(cudaMemset(w->m.p, 0, sizeof(float) * w->lay.total));
+    GK(cudaMemset(w->v.p, 0, sizeof(float) * w->lay.total));
+    w->t = 0;
+    const int rc = refresh_bf16(w, w->stream);
+    if (rc) return rc;
+    GK(cudaStreamSynchronize(w->stream));
+    return PDG_OK;
+}
+
+int pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr, const int* adj, const float* ef,
+                       const float* target, const float* freew, float* out, float* loss, float* grads)
+{
+    if (!w || N <= 0 || !x || !ptr || !target || !freew) return set_error(PDG_ERR_ARG, "pdg_warmstart_eval: bad arguments");
+    if (w->solver) return set_error(PDG_ERR_STATE, "pdg_warmstart_eval: the network is attached to a solver");
+    const int E = ptr[N];
+    if (E < 0 || (E > 0 && (!adj || !ef))) return set_error(PDG_ERR_ARG, "pdg_warmstart_eval: bad adjacency");
+    cudaStream_t st = w->stream;
+    std::vector<int> hp(ptr, ptr + N + 1), ha(adj, adj + E);
+    int rc = upload_graph(w, hp, ha, st);
+    if (rc) return rc;
+    std::vector<bf16> xb((size_t)N * NFP);
+    for (int i = 0; i < N; ++i)
+        for (int k = 0; k < NFP; ++k) xb[(size_t)i * NFP + k] = __float2bfloat16_rn(k < NF ? x[(size_t)i * NF + k] : 0.f);
+    GK(cudaMemcpyAsync(w->xin.p, xb.data(), sizeof(bf16) * xb.size(), cudaMemcpyHostToDevice, st));
+    if (E) GK(cudaMemcpyAsync(w->ef.p, ef, sizeof(float4) * E, cudaMemcpyHostToDevice, st));
+    GK(cudaMemcpyAsync(w->target.p, target, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, st));
+    GK(cudaMemcpyAsync(w->freew.p, freew, sizeof(float) * N, cudaMemcpyHostToDevice, st));
+    double cnt = 0.0;
+    for (int i = 0; i < N; ++i) cnt += freew[i] > 0.f ? 3.0 : 0.0;
+    rc = forward(w, st);
+    if (rc) return rc;
+    rc = backward(w, (float)(1.0 / std::max(cnt, 1.0)), st);
+    if (rc) return rc;
+    std::vector<float> o((size_t)N * 16);
+    double l = 0.0;
+    GK(cudaMemcpyAsync(o.data(), w->out.p, sizeof(float) * o.size(), cudaMemcpyDeviceToHost, st));
+    GK(cudaMemcpyAsync(&l, w->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (grads) GK(cudaMemcpyAsync(grads, w->g.p, sizeof(float) * w->lay.total, cudaMemcpyDeviceToHost, st));
+    GK(cudaStreamSynchronize(st));
+    if (out)
+        for (int i = 0; i < N; ++i)
+            for (int c = 0; c < NO; ++c) out[3 * i + c] = o[(size_t)i * 16 + c];
+    if (loss) *loss = (float)l;
+    return PDG_OK;
+}
+
+int pdg_warmstart_adam_step(pdg_warmstart* w, float lr)
+{
+    if (!w || !(lr > 0.f)) return set_error(PDG_ERR_ARG, "pdg_warmstart_adam_step: bad arguments");
+    cudaStream_t st = w->solver ? w->solver->stream : w->stream;
+    const int rc = adam_step(w, lr, st);
+    if (rc) return rc;
+    GK(cudaStreamSynchronize(st));
+    return PDG_OK;
+}
+
+int pdg_warmstart_attach(pdg_warmstart* w, pdg_solver* s)
+{
+    if (!w || !s) return set_error(PDG_ERR_ARG, "pdg_warmstart_attach: null argument");
+    if (s->kernel != PDG_KERNEL_GRAPH)
+        return set_error(PDG_ERR_STATE, "pdg_warmstart_attach: the solver must use the per-sweep (graph) kernels");
+    const HostLayout& Lh = s->L;
+    const int N = Lh.ntot;
+    // mesh adjacency in the solver's (reordered) numbering, both directions
+    std::vector<std::vector<std::pair<int, float>>> nbr(N);
+    std::vector<float4> stat(N);
+    std::vector<int> iperm(N);
+    for (int g = 0; g < N; ++g) iperm[Lh.perm_global[g]] = g;   // batch caller index -> reordered
+    int vbase = 0;
+    for (const auto& c : s->cloths) {
+        const Topology& t = *c.topo;
+        const size_t nE = t.edges.size() / 4;
+        for (size_t e = 0; e < nE; ++e) {
+            const int a = iperm[vbase + t.edges[4 * e]], b = iperm[vbase + t.edges[4 * e + 1]];
+            const float r = std::max(t.rest_len[e], 1e-12f);
+            nbr[a].push_back({b, r});
+            nbr[b].push_back({a, r});
+        }
+        double ks = 0.0, kb = 0.0;
+        for (float k : c.cons.k_stretch) ks += k;
+        for (float k : c.cons.bend_k) kb += k;
+        ks = c.cons.k_stretch.empty() ? 1.0 : ks / c.cons.k_stretch.size();
+        kb = c.cons.bend_k.empty() ? 1e-3 : kb / c.cons.bend_k.size();
+        for (int i = 0; i < c.mesh->N; ++i) {
+            const int gidx = iperm[vbase + i];
+            const float m = std::max(c.mesh->mass[i], 1e-12f);
+            stat[gidx] = make_float4((std::log(m) + 11.f) / 2.f, (float)((std::log(std::max(ks, 1e-6)) - 6.9) / 1.2),
+                                     (float)((std::log(std::max(kb, 1e-9)) + 4.6) / 1.2), 0.f);
+        }
+        vbase += c.mesh->N;
+    }
+    std::vector<int> ptr(N + 1, 0), adj;
+    std::vector<float> rest;
+    for (int i = 0; i < N; ++i) {
+        std::sort(nbr[i].begin(), nbr[i].end(), [](const std::pair<int, float>& a, const std::pair<int, float>& b) {
+            return a.first < b.first;
+        });
+        for (auto& q : nbr[i]) { adj.push_back(q.first); rest.push_back(q.second); }
+        ptr[i + 1] = (int)adj.size();
+    }
+    cudaStream_t st = s->stream;
+    int rc = upload_graph(w, ptr, adj, st);
+    if (rc) return rc;
+    if (!rest.empty()) GK(cudaMemcpyAsync(w->rest.p, rest.data(), sizeof(float) * rest.size(), cudaMemcpyHostToDevice, st));
+    GK(cudaMemcpyAsync(w->stat.p, stat.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, st));
+    GK(s->warm.alloc(N));
+    GK(cudaMemsetAsync(s->warm.p, 0, sizeof(float4) * N, st));
+    GK(cudaStreamSynchronize(st));
+    w->solver = s;
+    s->ws = w;
+    if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    return PDG_OK;
+}
+
+int pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* loss)
+{
+    if (!w || !s || w->solver != s) return set_error(PDG_ERR_STATE, "pdg_warmstart_train_frame: not attached to this solver");
+    cudaStream_t st = s->stream;
+    const int N = w->N;
+    GK(cudaMemcpyAsync(w->Xn.p, s->X.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    GK(cudaMemcpyAsync(w->Vn.p, s->V.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    int rc = pdg_solver_step(s, 1, nullptr);
+    if (rc) return rc;
+    // inputs from (x_n, v_n, y), target (x* - y)/s from the solve
+    k_node_feat<<<nb(N, 256), 256, 0, st>>>(N, w->Xn.p, w->Vn.p, s->Y.p, s->aux.p, w->stat.p, s->vcloth.p, s->cinfo.p,
+                                            w->xin.p);
+    k_edge_feat<<<nb(N, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rest.p, s->Y.p, w->ef.p);
+    k_target<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->Y.p, s->aux.p, w->target.p, w->freew.p);
+    int nfree = 0;
+    for (const auto& a : s->L.aux) nfree += a.w >= 0.f ? 1 : 0;
+    rc = forward(w, st);
+    if (rc) return rc;
+    rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), st);
+    if (rc) return rc;
+    if (lr > 0.f) {
+        rc = adam_step(w, lr, st);
+        if (rc) return rc;
+    }
+    s->launches += 8 + 3 * L + 6 * L + 4;
+    double l = 0.0;
+    GK(cudaMemcpyAsync(&l, w->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    GK(cudaStreamSynchronize(st));
+    if (loss) *loss = (float)l;
+    return PDG_OK;
+}
+
+void pdg_warmstart_destroy(pdg_warmstart* w)
+{
+    if (!w) return;
+    if (w->solver) { w->solver->ws = nullptr; if (w->solver->graph) { cudaGraphExecDestroy(w->solver->graph); w->solver->graph = nullptr; } }
+    delete w;
+}
+
+}  // extern "C"

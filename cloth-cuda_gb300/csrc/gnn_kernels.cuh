@@ -1,0 +1,379 @@
+// Learned warm start for the PD solve (no counterpart in the reference).
+//
+// A 2-layer mesh message-passing network (hidden 64) predicts, per vertex,
+// the offset d = x* - y of the converged position from the inertial
+// prediction.  Node GEMMs run on the tensor cores (bf16 mma.sync m16n8k16,
+// fp32 accumulation, bf16 activations); edge messages are warp-per-node
+// gathers over the mesh adjacency (deterministic, no atomics); weight
+// gradients are fp32 block reductions; Adam keeps fp32 master weights and
+// refreshes their bf16 copies after each step.
+//
+// Network (x: 10 node features, e_ij: 4 edge features):
+//   h0 = relu(We x + be)
+//   per layer: P = A h, Q = B h;  m_ij = relu(P_i + Q_j + C e_ij + c);
+//              a_i = mean_j m_ij;  h <- h + relu(U [h; a] + u)
+//   out = Wd h + bd     (offset / kOffsetScale)
+#include "gnn.cuh"
+#include "pdg_solver.h"
+
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+namespace pdg {
+namespace gnn {
+
+using bf16 = __nv_bfloat16;
+
+enum { EPI_RELU = 1, EPI_STORE1 = 2, EPI_RESID2 = 4, EPI_STOREF = 8, EPI_ACCF = 16 };
+
+__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ uint32_t ld_pair(const float* p)
+{
+    const float2 f = *reinterpret_cast<const float2*>(p);
+    __nv_bfloat162 b = __floats2bfloat162_rn(f.x, f.y);
+    return *reinterpret_cast<uint32_t*>(&b);
+}
+
+__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// Y[M x NOUT] = X[M x K] W^T (+ bias), W stored [NOUT][K] bf16.  Each warp
+// computes 16 rows; W is staged in shared memory with a padded row stride
+// (K + 8 elements) so the B-fragment loads are bank-conflict free.
+// Epilogue: optional ReLU; Y1 <- bf16(v); Y2 <- bf16(R + v); Yf <- v or += v.
+template <typename TA, int K, int NOUT, int EPI>
+__global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx, int M, const bf16* __restrict__ W,
+                                              const float* __restrict__ bias, const bf16* __restrict__ R, int ldr,
+                                              bf16* __restrict__ Y1, int ld1, bf16* __restrict__ Y2, int ld2,
+                                              float* __restrict__ Yf, int ldf)
+{
+    __shared__ __align__(16) bf16 sW[NOUT * (K + 8)];
+    for (int i = threadIdx.x; i < NOUT * K; i += 128) sW[(i / K) * (K + 8) + i % K] = W[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int r0 = (blockIdx.x * 4 + warp) * 16;
+    if (r0 >= M) return;
+    float acc[NOUT / 8][4];
+    #pragma unroll
+    for (int n = 0; n < NOUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+    const bool ok0 = r0 + g < M, ok1 = r0 + g + 8 < M;
+    const TA* x0 = X + (size_t)(r0 + g) * ldx;
+    const TA* x1 = X + (size_t)(r0 + g + 8) * ldx;
+    #pragma unroll
+    for (int ks = 0; ks < K / 16; ++ks) {
+        const int c0 = ks * 16 + 2 * t;
+        const uint32_t a0 = ok0 ? ld_pair(x0 + c0) : 0u;
+        const uint32_t a1 = ok1 ? ld_pair(x1 + c0) : 0u;
+        const uint32_t a2 = ok0 ? ld_pair(x0 + c0 + 8) : 0u;
+        const uint32_t a3 = ok1 ? ld_pair(x1 + c0 + 8) : 0u;
+        #pragma unroll
+        for (int n = 0; n < NOUT / 8; ++n) {
+            const bf16* wr = sW + (n * 8 + g) * (K + 8) + c0;
+            mma_bf16(acc[n], a0, a1, a2, a3, *reinterpret_cast<const uint32_t*>(wr),
+                     *reinterpret_cast<const uint32_t*>(wr + 8));
+        }
+    }
+    #pragma unroll
+    for (int n = 0; n < NOUT / 8; ++n)
+        #pragma unroll
+        for (int hf = 0; hf < 2; ++hf) {
+            const int row = r0 + g + 8 * hf;
+            if (row >= M) continue;
+            const int col = n * 8 + 2 * t;
+            float v0 = acc[n][2 * hf], v1 = acc[n][2 * hf + 1];
+            if (bias) { v0 += bias[col]; v1 += bias[col + 1]; }
+            if (EPI & EPI_RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+            if (EPI & EPI_STORE1)
+                *reinterpret_cast<__nv_bfloat162*>(Y1 + (size_t)row * ld1 + col) = __floats2bfloat162_rn(v0, v1);
+            if (EPI & EPI_RESID2) {
+                const __nv_bfloat162 r = *reinterpret_cast<const __nv_bfloat162*>(R + (size_t)row * ldr + col);
+                *reinterpret_cast<__nv_bfloat162*>(Y2 + (size_t)row * ld2 + col) =
+                    __floats2bfloat162_rn(__bfloat162float(r.x) + v0, __bfloat162float(r.y) + v1);
+            }
+            if (EPI & EPI_STOREF) *reinterpret_cast<float2*>(Yf + (size_t)row * ldf + col) = make_float2(v0, v1);
+            if (EPI & EPI_ACCF) {
+                float2* p = reinterpret_cast<float2*>(Yf + (size_t)row * ldf + col);
+                const float2 o = *p;
+                *p = make_float2(o.x + v0, o.y + v1);
+            }
+        }
+}
+
+__device__ __forceinline__ float tofloat(float v) { return v; }
+__device__ __forceinline__ float tofloat(bf16 v) { return __bfloat162float(v); }
+
+// dW[nout][k] += sum_rows dY[r][n] X[r][k];  db[n] += sum_rows dY[r][n].
+// Grid-stride over tiles of 32 rows; each thread owns up to 32 outputs in
+// registers; one atomic per output per block at the end.
+template <typename TY, typename TX>
+__global__ void __launch_bounds__(256) k_wgrad(const TY* __restrict__ dY, int ldy, int nout, const TX* __restrict__ X,
+                                               int ldx, int K, int M, float* __restrict__ dW,
+                                               float* __restrict__ db)
+{
+    constexpr int RT = 32, NT = 256, MAXO = 32;
+    __shared__ float sy[RT][2 * H + 1];
+    __shared__ float sx[RT][2 * H + 1];
+    const int nouts = nout * K;
+    float acc[MAXO];
+    float bacc = 0.f;
+    #pragma unroll
+    for (int j = 0; j < MAXO; ++j) acc[j] = 0.f;
+    for (int r0 = blockIdx.x * RT; r0 < M; r0 += gridDim.x * RT) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < RT * nout; i += NT) {
+            const int r = i / nout, n = i % nout;
+            sy[r][n] = r0 + r < M ? tofloat(dY[(size_t)(r0 + r) * ldy + n]) : 0.f;
+        }
+        for (int i = threadIdx.x; i < RT * K; i += NT) {
+            const int r = i / K, k = i % K;
+            sx[r][k] = r0 + r < M ? tofloat(X[(size_t)(r0 + r) * ldx + k]) : 0.f;
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int j = 0; j < MAXO; ++j) {
+            const int o = threadIdx.x + j * NT;
+            if (o < nouts) {
+                const int n = o / K, k = o % K;
+                float s = 0.f;
+                #pragma unroll 8
+                for (int r = 0; r < RT; ++r) s += sy[r][n] * sx[r][k];
+                acc[j] += s;
+            }
+        }
+        if (db && threadIdx.x < nout)
+            for (int r = 0; r < RT; ++r) bacc += sy[r][threadIdx.x];
+    }
+    #pragma unroll
+    for (int j = 0; j < MAXO; ++j) {
+        const int o = threadIdx.x + j * NT;
+        if (o < nouts) atomicAdd(&dW[o], acc[j]);
+    }
+    if (db && threadIdx.x < nout) atomicAdd(&db[threadIdx.x], bacc);
+}
+
+// Messages of layer l, warp per node, lane owns channels 2*lane, 2*lane+1:
+// a_i = deg_inv_i * sum_j relu(P_i + Q_j + C e_ij + c), written to cat[:, H:2H].
+__global__ void k_msg_fwd(int N, const int* __restrict__ ptr, const int* __restrict__ adj,
+                          const float4* __restrict__ ef, const float* __restrict__ deg_inv,
+                          const bf16* __restrict__ PQ, const float* __restrict__ C, const float* __restrict__ cb,
+                          bf16* __restrict__ cat)
+{
+    const int node = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (node >= N) return;
+    const int ch = 2 * lane;
+    const float2 P = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)node * 2 * H + ch));
+    const float4 C0 = *reinterpret_cast<const float4*>(C + ch * EF), C1 = *reinterpret_cast<const float4*>(C + (ch + 1) * EF);
+    const float c0 = cb[ch], c1 = cb[ch + 1];
+    float s0 = 0.f, s1 = 0.f;
+    for (int e = ptr[node]; e < ptr[node + 1]; ++e) {
+        const int j = adj[e];
+        const float4 f = ef[e];
+        const float2 Q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)j * 2 * H + H + ch));
+        const float z0 = P.x + Q.x + C0.x * f.x + C0.y * f.y + C0.z * f.z + C0.w * f.w + c0;
+        const float z1 = P.y + Q.y + C1.x * f.x + C1.y * f.y + C1.z * f.z + C1.w * f.w + c1;
+        s0 += fmaxf(z0, 0.f);
+        s1 += fmaxf(z1, 0.f);
+    }
+    const float di = deg_inv[node];
+    *reinterpret_cast<__nv_bfloat162*>(cat + (size_t)node * 2 * H + H + ch) = __floats2bfloat162_rn(s0 * di, s1 * di);
+}
+
+// Backward of the messages: dP_i = sum_j g_ij, dQ_j = sum_i g_ij with
+// g_ij = [z_ij > 0] da_i / deg_i (da = dcat[:, H:2H]); dC, dc reduced per
+// block.  Each warp handles node n as receiver (dP) and as sender (dQ, via
+// the reverse edge's features).
+__global__ void __launch_bounds__(256) k_msg_bwd(int N, const int* __restrict__ ptr, const int* __restrict__ adj,
+                                                 const int* __restrict__ rev, const float4* __restrict__ ef,
+                                                 const float* __restrict__ deg_inv, const bf16* __restrict__ PQ,
+                                                 const float* __restrict__ C, const float* __restrict__ cb,
+                                                 const float* __restrict__ dcat, float* __restrict__ dpq,
+                                                 float* __restrict__ dC, float* __restrict__ dc)
+{
+    __shared__ float red[8][H * (EF + 1)];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, ch = 2 * lane;
+    const float4 C0 = *reinterpret_cast<const float4*>(C + ch * EF), C1 = *reinterpret_cast<const float4*>(C + (ch + 1) * EF);
+    const float c0 = cb[ch], c1 = cb[ch + 1];
+    float gC[2][EF] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    float gc0 = 0.f, gc1 = 0.f;
+    for (int node = blockIdx.x * 8 + warp; node < N; node += gridDim.x * 8) {
+        const float2 Pn = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)node * 2 * H + ch));
+        const float2 Qn = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)node * 2 * H + H + ch));
+        const float2 dan = *reinterpret_cast<const float2*>(dcat + (size_t)node * 2 * H + H + ch);
+        const float din = deg_inv[node];
+        float dP0 = 0.f, dP1 = 0.f, dQ0 = 0.f, dQ1 = 0.f;
+        for (int e = ptr[node]; e < ptr[node + 1]; ++e) {
+            const int j = adj[e];
+            // node as receiver of j
+            {
+                const float4 f = ef[e];
+                const float2 Q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)j * 2 * H + H + ch));
+                const float z0 = Pn.x + Q.x + C0.x * f.x + C0.y * f.y + C0.z * f.z + C0.w * f.w + c0;
+                const float z1 = Pn.y + Q.y + C1.x * f.x + C1.y * f.y + C1.z * f.z + C1.w * f.w + c1;
+                const float g0 = z0 > 0.f ? dan.x * din : 0.f, g1 = z1 > 0.f ? dan.y * din : 0.f;
+                dP0 += g0; dP1 += g1;
+                gC[0][0] += g0 * f.x; gC[0][1] += g0 * f.y; gC[0][2] += g0 * f.z; gC[0][3] += g0 * f.w;
+                gC[1][0] += g1 * f.x; gC[1][1] += g1 * f.y; gC[1][2] += g1 * f.z; gC[1][3] += g1 * f.w;
+                gc0 += g0; gc1 += g1;
+            }
+            // node as sender to j: edge (j <- node) is rev[e] in j's list
+            {
+                const float4 f = ef[rev[e]];
+                const float2 P = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)j * 2 * H + ch));
+                const float2 da = *reinterpret_cast<const float2*>(dcat + (size_t)j * 2 * H + H + ch);
+                const float dj = deg_inv[j];
+                const float z0 = P.x + Qn.x + C0.x * f.x + C0.y * f.y + C0.z * f.z + C0.w * f.w + c0;
+                const float z1 = P.y + Qn.y + C1.x * f.x + C1.y * f.y + C1.z * f.z + C1.w * f.w + c1;
+                dQ0 += z0 > 0.f ? da.x * dj : 0.f;
+                dQ1 += z1 > 0.f ? da.y * dj : 0.f;
+            }
+        }
+        *reinterpret_cast<float2*>(dpq + (size_t)node * 2 * H + ch) = make_float2(dP0, dP1);
+        *reinterpret_cast<float2*>(dpq + (size_t)node * 2 * H + H + ch) = make_float2(dQ0, dQ1);
+    }
+    for (int f = 0; f < EF; ++f) { red[warp][ch * EF + f] = gC[0][f]; red[warp][(ch + 1) * EF + f] = gC[1][f]; }
+    red[warp][H * EF + ch] = gc0;
+    red[warp][H * EF + ch + 1] = gc1;
+    __syncthreads();
+    for (int i = threadIdx.x; i < H * (EF + 1); i += 256) {
+        float s = 0.f;
+        for (int w = 0; w < 8; ++w) s += red[w][i];
+        if (i < H * EF) atomicAdd(&dC[i], s); else atomicAdd(&dc[i - H * EF], s);
+    }
+}
+
+// out[:, 0:3] vs target over free vertices: loss += sum sq / cnt; dout = 2 diff / cnt.
+__global__ void k_loss(int N, const float* __restrict__ out, const float* __restrict__ target,
+                       const float* __restrict__ freew, float inv_cnt, float* __restrict__ dout,
+                       double* __restrict__ loss)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float s = 0.f;
+    if (i < N) {
+        const float w = freew[i];
+        for (int c = 0; c < 16; ++c) {
+            float d = 0.f;
+            if (c < NO) {
+                d = (out[(size_t)i * 16 + c] - target[(size_t)i * 3 + c]) * w;
+                s += d * d;
+            }
+            dout[(size_t)i * 16 + c] = 2.f * d * inv_cnt;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0 && s != 0.f) atomicAdd(loss, (double)s * inv_cnt);
+}
+
+// dst = src * mask(ref > 0) (ReLU backward; ref is the bf16 ReLU output)
+__global__ void k_relu_bwd(int N, int cols, const float* __restrict__ src, int lds, const bf16* __restrict__ ref,
+                           int ldr, float* __restrict__ dst, int ldd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N * cols) return;
+    const int r = i / cols, c = i % cols;
+    dst[(size_t)r * ldd + c] = __bfloat162float(ref[(size_t)r * ldr + c]) > 0.f ? src[(size_t)r * lds + c] : 0.f;
+}
+
+// dst[:, 0:cols] += src[:, 0:cols]
+__global__ void k_add(int N, int cols, const float* __restrict__ src, int lds, float* __restrict__ dst, int ldd)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N * cols) return;
+    const int r = i / cols, c = i % cols;
+    dst[(size_t)r * ldd + c] += src[(size_t)r * lds + c];
+}
+
+__global__ void k_adam(int n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1, float bc2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+// bf16 copy of a [rows][cols] fp32 tensor into dst[rows_pad][ld] (and its
+// transpose into dstT[cols][ldT]); padding rows/cols are left as zero.
+__global__ void k_to_bf16(const float* __restrict__ src, int rows, int cols, bf16* __restrict__ dst, int ld,
+                          bf16* __restrict__ dstT, int ldT)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * cols) return;
+    const int r = i / cols, c = i % cols;
+    const bf16 b = __float2bfloat16_rn(src[i]);
+    if (dst) dst[(size_t)r * ld + c] = b;
+    if (dstT) dstT[(size_t)c * ldT + r] = b;
+}
+
+// ---- solver-side feature kernels -----------------------------------------
+// node features: (y - x)/s, h v / s, pinned, scaled log mass / log stretch k / log bend k
+__global__ void k_node_feat(int N, const float4* __restrict__ X, const float4* __restrict__ V,
+                            const float4* __restrict__ Y, const float4* __restrict__ aux,
+                            const float4* __restrict__ stat, const int* __restrict__ vcloth,
+                            const ClothInfo* __restrict__ cinfo, bf16* __restrict__ xin)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float4 x = X[i], v = V[i], y = Y[i], s = stat[i];
+    const float h = cinfo[vcloth[i]].h, is = 1.f / kOffsetScale;
+    float f[NFP];
+    f[0] = (y.x - x.x) * is; f[1] = (y.y - x.y) * is; f[2] = (y.z - x.z) * is;
+    f[3] = h * v.x * is; f[4] = h * v.y * is; f[5] = h * v.z * is;
+    f[6] = aux[i].w < 0.f ? 1.f : 0.f;
+    f[7] = s.x; f[8] = s.y; f[9] = s.z;
+    for (int k = NF; k < NFP; ++k) f[k] = 0.f;
+    for (int k = 0; k < NFP; k += 2)
+        *reinterpret_cast<__nv_bfloat162*>(xin + (size_t)i * NFP + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
+}
+
+// edge features of (i <- j): log(rest / 1 cm), (y_j - y_i) / rest
+__global__ void k_edge_feat(int N, const int* __restrict__ ptr, const int* __restrict__ adj,
+                            const float* __restrict__ rest, const float4* __restrict__ Y, float4* __restrict__ ef)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float4 yi = Y[i];
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+        const float4 yj = Y[adj[e]];
+        const float r = rest[e], ir = 1.f / r;
+        ef[e] = make_float4(logf(r / kLenScale), (yj.x - yi.x) * ir, (yj.y - yi.y) * ir, (yj.z - yi.z) * ir);
+    }
+}
+
+// target (x* - y)/s and free weight from the solver's result
+__global__ void k_target(int N, const float4* __restrict__ Xs, const float4* __restrict__ Y,
+                         const float4* __restrict__ aux, float* __restrict__ target, float* __restrict__ freew)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float4 x = Xs[i], y = Y[i];
+    const float is = 1.f / kOffsetScale;
+    target[3 * i] = (x.x - y.x) * is; target[3 * i + 1] = (x.y - y.y) * is; target[3 * i + 2] = (x.z - y.z) * is;
+    freew[i] = aux[i].w < 0.f ? 0.f : 1.f;
+}
+
+// predicted start offsets (pinned vertices keep the inertial start's target offset)
+__global__ void k_warm_out(int N, const float* __restrict__ out, const float4* __restrict__ A, float4* __restrict__ warm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float4 a = A[i];
+    warm[i] = a.w < 0.f ? a
+                        : make_float4(out[(size_t)i * 16] * kOffsetScale, out[(size_t)i * 16 + 1] * kOffsetScale,
+                                      out[(size_t)i * 16 + 2] * kOffsetScale, a.w);
+}
+
+}  // namespace gnn
+}  // namespace pdg

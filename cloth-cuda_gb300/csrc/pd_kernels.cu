@@ -42,6 +42,48 @@ __global__ void __launch_bounds__(NT) k_iter(IterArgs a, int k, int res_only)
     process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, omega, sx, cx, cy, cz, red);
 }
 
+// Residual of the offsets D (no update) into acc[cloth][slot]: one block per patch.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_res_eval(IterArgs a, const float4* D, int slot)
+{
+    extern __shared__ float4 smem[];
+    __shared__ PatchHdr ph;
+    __shared__ float red[NT / 32];
+    if (threadIdx.x == 0) ph = a.patches[blockIdx.x];
+    __syncthreads();
+    IterArgs b = a;
+    b.buf[0] = b.buf[1] = const_cast<float4*>(D);
+    b.acc = a.acc + slot;
+    float4* sx = smem;
+    float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
+    float* cy = cx + ph.nslot;
+    float* cz = cy + ph.nslot;
+    process_patch<kModeConsistent, NT>(b, ph, 0, true, 1.f, sx, cx, cy, cz, red);
+}
+
+// Keep the learned start of a cloth only if its residual is below the
+// inertial start's; record r(y) as the frame's normaliser.
+__global__ void k_select_cloth(IterArgs a, int slot_y, int slot_w)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncloth) return;
+    const double r2y = a.acc[(size_t)c * a.acc_stride + slot_y];
+    const double r2w = a.acc[(size_t)c * a.acc_stride + slot_w];
+    ClothRT& rt = a.crt[c];
+    rt.warm = (a.cinfo[c].init == 2 && isfinite(r2w) && r2w < r2y) ? 1 : 0;
+    rt.res_y2 = r2y;
+}
+
+__global__ void k_select_vertex(int n, const int* __restrict__ vcloth, const ClothRT* __restrict__ crt,
+                                const float4* __restrict__ warm, float4* __restrict__ A, float4* __restrict__ B)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !crt[vcloth[i]].warm) return;
+    const float4 w = warm[i];
+    A[i] = w;
+    B[i] = w;
+}
+
 __global__ void k_predict(const float4* __restrict__ X, const float4* __restrict__ V,
                           const float4* __restrict__ aux, const float* __restrict__ mass,
                           const int* __restrict__ vcloth, const ClothInfo* __restrict__ cinfo,
@@ -155,6 +197,30 @@ cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float
 {
     k_frame_stats<<<nblk(a.ncloth, 128), 128, 0, s>>>(a);
     k_finalize<<<nblk(n, 256), 256, 0, s>>>(X, V, a.Y, a.buf[0], a.buf[1], aux, vcloth, a.cinfo, a.crt, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t smem, const float4* warm,
+                               const int* vcloth, int n, cudaStream_t s)
+{
+    const int slot_y = a.acc_stride - 2, slot_w = a.acc_stride - 1;
+    static bool attr_set[3] = {false, false, false};
+    const int ti = nt == 128 ? 0 : (nt == 256 ? 1 : 2);
+    void* f = nt == 128 ? (void*)k_res_eval<128> : (nt == 256 ? (void*)k_res_eval<256> : (void*)k_res_eval<512>);
+    if (!attr_set[ti]) {
+        const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+        attr_set[ti] = true;
+    }
+    for (int which = 0; which < 2; ++which) {
+        const float4* D = which == 0 ? a.buf[0] : warm;
+        const int slot = which == 0 ? slot_y : slot_w;
+        if (nt == 128) k_res_eval<128><<<npatch, 128, smem, s>>>(a, D, slot);
+        else if (nt == 256) k_res_eval<256><<<npatch, 256, smem, s>>>(a, D, slot);
+        else k_res_eval<512><<<npatch, 512, smem, s>>>(a, D, slot);
+    }
+    k_select_cloth<<<nblk(a.ncloth, 128), 128, 0, s>>>(a, slot_y, slot_w);
+    k_select_vertex<<<nblk(n, 256), 256, 0, s>>>(n, vcloth, a.crt, warm, a.buf[0], a.buf[1]);
     return cudaGetLastError();
 }
 

@@ -359,10 +359,14 @@ __device__ __forceinline__ bool cloth_done(const IterArgs& a, int c, int k, bool
     if (check && k >= 1 && ci.mode == kModeConsistent) {
         const double acc0 = __ldcg(&acc[0]);
         const double rk2 = __ldcg(&acc[k - 1]);          // ||r(x^(k-1))||^2
-        const double ry2 = (k == 1 && ci.init == 0) ? acc0 : __ldcg(&rt->res_y2);
+        // normaliser: the residual of the inertial start, measured by the
+        // warm-start selection when a learned start was evaluated, else the
+        // residual of the start iterate itself
+        const bool own_start = !(ci.init == 2 && a.warm_active);
+        const double ry2 = (k == 1 && own_start) ? acc0 : __ldcg(&rt->res_y2);
         if (k == 1 && designated) {
             rt->res0_2 = acc0;
-            if (ci.init == 0) rt->res_y2 = acc0;
+            if (own_start) rt->res_y2 = acc0;
         }
         if (!isfinite(rk2)) {
             if (designated) { rt->status = -6; rt->used = k - 1; rt->resf_2 = rk2; rt->active = 0; }
@@ -432,7 +436,7 @@ __device__ __forceinline__ void frame_stats_cloth(const IterArgs& a, int c)
     const double* acc = a.acc + (size_t)c * a.acc_stride;
     if (ci.mode == kModeConsistent) {
         rt->res0_2 = __ldcg(&acc[0]);
-        if (ci.init == 0) rt->res_y2 = rt->res0_2;
+        if (!(ci.init == 2 && a.warm_active)) rt->res_y2 = rt->res0_2;
     }
     if (__ldcg(&rt->active)) {
         rt->used = ci.max_iter;

@@ -13,6 +13,10 @@ cudaError_t launch_predict(const IterArgs& a, const float4* X, const float4* V, 
                            const float* mass, const int* vcloth, const float4* warm, int n, cudaStream_t s);
 cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float4* aux, const int* vcloth, int n,
                             cudaStream_t s);
+// Residuals of the inertial start (buf[0]) and of the learned start `warm`,
+// then the per-cloth choice between them (slots acc_stride-2 / -1).
+cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t smem, const float4* warm,
+                               const int* vcloth, int n, cudaStream_t s);
 cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s);
 cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s);
 cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P,

@@ -86,6 +86,7 @@ struct IterArgs {
     int              acc_stride;  // sweeps + 1
     int              ncloth;
     int              have_final;  // evaluate r(x^max_iter) in an extra sweep
+    int              warm_active; // learned start evaluated this frame (res_y2 set by the selection)
 };
 
 }  // namespace pdg

@@ -102,6 +102,15 @@ struct pdg_solver {
     cudaGraphExec_t graph = nullptr;
     std::vector<pdg::ClothRT> h_rt;
     bool warm_valid = false;
+    pdg_warmstart* ws = nullptr;   // attached learned warm start (not owned)
+    bool any_warm = false;         // some cloth asks for PDG_INIT_WARMSTART
 
     ~pdg_solver();
 };
+
+namespace pdg {
+// learned warm start hooks (gnn.cu): features + forward into s->warm
+int warm_infer_enqueue(pdg_warmstart* w, pdg_solver* s);
+int warm_kernel_count();
+void warm_detach(pdg_warmstart* w);
+}  // namespace pdg

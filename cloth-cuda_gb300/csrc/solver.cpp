@@ -18,6 +18,7 @@ using namespace pdg;
 
 pdg_solver::~pdg_solver()
 {
+    if (ws) warm_detach(ws);
     if (graph) cudaGraphExecDestroy(graph);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
@@ -62,7 +63,7 @@ int upload_all(pdg_solver* s)
     CK(s->nbr_ptr.upload(L.nbr_ptr, st));
     CK(s->nbr.upload(L.nbr, st));
     CK(s->crt.alloc(L.ncloth));
-    s->acc_stride = L.cap + 2;
+    s->acc_stride = L.cap + 4;   // sweeps 0..cap, then r(y) and r(learned start)
     CK(s->acc.alloc((size_t)L.ncloth * s->acc_stride));
     CK(cudaMemsetAsync(s->acc.p, 0, sizeof(double) * (size_t)L.ncloth * s->acc_stride, st));
     CK(s->pflag.alloc(L.npatch));
@@ -98,6 +99,7 @@ IterArgs iter_args(pdg_solver* s)
     a.Y = s->Y.p; a.buf[0] = s->A.p; a.buf[1] = s->B.p; a.ncloth = s->L.ncloth;
     a.acc = s->acc.p; a.acc_stride = s->acc_stride;
     a.have_final = s->have_final;
+    a.warm_active = (s->ws && s->any_warm) ? 1 : 0;
     return a;
 }
 
@@ -106,7 +108,7 @@ PersistArgs persist_args(pdg_solver* s)
     PersistArgs p;
     p.it = iter_args(s);
     p.X = s->X.p; p.Xw = s->X.p; p.V = s->V.p; p.aux = s->aux.p; p.mass = s->mass.p; p.vcloth = s->vcloth.p;
-    p.warm = s->warm_valid ? s->warm.p : nullptr; p.Y = s->Y.p;
+    p.warm = nullptr; p.Y = s->Y.p;
     p.n = s->L.ntot; p.npatch = s->L.npatch; p.max_iter = s->L.cap; p.have_final = s->have_final;
     p.mode = s->mode; p.bar = s->bar.p; p.err = s->err.p;
     p.spin_budget = 2000000000LL;   // ~1 s at 2 GHz per wait
@@ -122,8 +124,12 @@ int enqueue_frame(pdg_solver* s)
     const HostLayout& L = s->L;
     cudaStream_t st = s->stream;
     const IterArgs a = iter_args(s);
-    CK(launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, s->warm_valid ? s->warm.p : nullptr,
-                      L.ntot, st));
+    CK(launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, nullptr, L.ntot, st));
+    if (a.warm_active) {   // learned start: predict, measure both starts, keep the better per cloth
+        const int rc = warm_infer_enqueue(s->ws, s);
+        if (rc) return rc;
+        CK(launch_warm_select(a, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st));
+    }
     for (int k = 0; k < L.cap; ++k) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st));
     if (s->have_final) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st));
     CK(launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st));
@@ -175,6 +181,9 @@ int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, co
     if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
     if (c0.kernel < PDG_KERNEL_AUTO || c0.kernel > PDG_KERNEL_RESIDENT) return set_error(PDG_ERR_ARG, "unknown kernel");
     s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_GRAPH : c0.kernel;
+    for (const auto& c : s->cloths) s->any_warm = s->any_warm || c.cfg.init == PDG_INIT_WARMSTART;
+    if (s->any_warm && (c0.kernel == PDG_KERNEL_PERSISTENT || c0.kernel == PDG_KERNEL_RESIDENT))
+        return set_error(PDG_ERR_ARG, "the learned warm start runs with the per-sweep (graph) kernels only");
 
     int dev = 0;
     CK(cudaGetDevice(&dev));
@@ -182,7 +191,7 @@ int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, co
     CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     std::string err;
-    if (c0.kernel == PDG_KERNEL_AUTO || c0.kernel == PDG_KERNEL_RESIDENT) {
+    if ((c0.kernel == PDG_KERNEL_AUTO && !s->any_warm) || c0.kernel == PDG_KERNEL_RESIDENT) {
         // Resident kernel: one patch per SM-sized block, every patch co-resident.
         int rnt = 0, rmt = 0, rmh = 0;
         resident_limits(&rnt, &rmt, &rmh);
@@ -306,7 +315,7 @@ int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
                 if (rc) return rc;
             }
             CK(cudaGraphLaunch(s->graph, s->stream));
-            s->launches += s->kernels_per_frame;
+            s->launches += s->kernels_per_frame + ((s->ws && s->any_warm) ? warm_kernel_count() + 4 : 0);
         }
     }
     if (stats) {
@@ -459,8 +468,12 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
             cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
         } else {
             const IterArgs a = iter_args(s);
-            cudaError_t err = launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p,
-                                             s->warm_valid ? s->warm.p : nullptr, L.ntot, st);
+            cudaError_t err = launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, nullptr, L.ntot, st);
+            if (err == cudaSuccess && a.warm_active) {
+                const int wrc = warm_infer_enqueue(s->ws, s);
+                if (wrc) { rc = wrc; break; }
+                err = launch_warm_select(a, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st);
+            }
             cudaEventRecord(e[1], st);
             for (int k = 0; k < L.cap && err == cudaSuccess; ++k)
                 err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st);
@@ -468,7 +481,7 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
             if (err == cudaSuccess && s->have_final) err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st);
             if (err == cudaSuccess) err = launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "frame launch: %s", cudaGetErrorString(err));
-            s->launches += s->kernels_per_frame;
+            s->launches += s->kernels_per_frame + ((s->ws && s->any_warm) ? warm_kernel_count() + 4 : 0);
         }
         cudaEventRecord(e[3], st);
         cudaError_t se = cudaEventSynchronize(e[3]);

@@ -312,6 +312,58 @@ class Solver:
         return dict(kernel=k.value, patch_verts=pv.value, block_threads=nt.value, npatches=npch.value)
 
 
+class WarmStart:
+    """Learned warm start (mesh message-passing network on the GPU)."""
+
+    def __init__(self, seed=0):
+        self.h = C.c_void_p()
+        _check(lib().pdg_warmstart_create(C.c_ulonglong(seed), C.byref(self.h)))
+        n = C.c_int()
+        _check(lib().pdg_warmstart_param_count(self.h, C.byref(n)))
+        self.count = n.value
+        self.solver = None
+
+    def close(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.pdg_warmstart_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def get_params(self):
+        p = np.zeros(self.count, np.float32)
+        _check(lib().pdg_warmstart_get_params(self.h, _p(p)))
+        return p
+
+    def set_params(self, p):
+        p = _f32(p)
+        assert p.size == self.count
+        _check(lib().pdg_warmstart_set_params(self.h, _p(p)))
+
+    def eval(self, x, ptr, adj, ef, target, freew):
+        x = _f32(x).reshape(-1, 10); ptr = _i32(ptr); adj = _i32(adj); ef = _f32(ef).reshape(-1, 4)
+        target = _f32(target).reshape(-1, 3); freew = _f32(freew)
+        N = len(x)
+        out = np.zeros((N, 3), np.float32); grads = np.zeros(self.count, np.float32); loss = C.c_float()
+        _check(lib().pdg_warmstart_eval(self.h, N, _p(x), _p(ptr), _p(adj) if adj.size else None,
+                                        _p(ef) if ef.size else None, _p(target), _p(freew), _p(out),
+                                        C.byref(loss), _p(grads)))
+        return out, loss.value, grads
+
+    def adam_step(self, lr):
+        _check(lib().pdg_warmstart_adam_step(self.h, C.c_float(lr)))
+
+    def attach(self, solver):
+        _check(lib().pdg_warmstart_attach(self.h, solver.h))
+        self.solver = solver   # keep alive
+
+    def train_frame(self, solver, lr):
+        loss = C.c_float()
+        _check(lib().pdg_warmstart_train_frame(self.h, solver.h, C.c_float(lr), C.byref(loss)))
+        return loss.value
+
+
 def exported_symbols():
     """Names declared in include/pdg.h (parsed from the header)."""
     import re

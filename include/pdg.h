@@ -202,6 +202,36 @@ int  pdg_solver_launch_info(const pdg_solver* s, int* kernel, int* patch_verts,
                             int* block_threads, int* npatches);
 void pdg_solver_destroy(pdg_solver* s);
 
+/* ---------------- learned warm start (no counterpart in the reference) ----
+ * A 2-layer mesh message-passing network (hidden 64, bf16 weights and
+ * activations, fp32 accumulation) predicts each vertex's offset x* - y of
+ * the converged position from the inertial prediction.  Attached to a solver
+ * whose cloths use cfg.init = PDG_INIT_WARMSTART, every frame evaluates the
+ * prediction and the inertial start and keeps, per cloth, the one with the
+ * lower residual (plain PD remains the fallback).  Parameter layout: see
+ * pdg_warmstart_get_params (We[64][10] be[64] {A[64][64] B[64][64] C[64][4]
+ * c[64] U[64][128] u[64]} x 2 Wd[3][64] bd[3], fp32). */
+int  pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out);
+int  pdg_warmstart_param_count(const pdg_warmstart* w, int* n);
+int  pdg_warmstart_get_params(pdg_warmstart* w, float* host);
+int  pdg_warmstart_set_params(pdg_warmstart* w, const float* host);
+/* Forward + backward on a caller graph (host arrays): x N*10 node features,
+ * symmetric CSR ptr (N+1) / adj, ef 4 features per directed edge, target
+ * N*3, free weights N.  Returns out N*3, the MSE loss and the gradients
+ * (param_count floats).  Not while attached to a solver. */
+int  pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr, const int* adj,
+                        const float* ef, const float* target, const float* freew, float* out,
+                        float* loss, float* grads);
+/* One Adam step (beta 0.9/0.999) with the gradients of the last eval/train. */
+int  pdg_warmstart_adam_step(pdg_warmstart* w, float lr);
+/* Bind to a solver (per-sweep kernels); its frames then use the prediction
+ * for cloths with cfg.init == PDG_INIT_WARMSTART. */
+int  pdg_warmstart_attach(pdg_warmstart* w, pdg_solver* s);
+/* Training on data the solver generates: one frame of `s` from its current
+ * state, then one Adam step (lr > 0) on (x_n, v_n, y) -> (x_{n+1} - y). */
+int  pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* loss);
+void pdg_warmstart_destroy(pdg_warmstart* w);
+
 /* ---------------- allocation-free frame ----------------------------------
  * No counterpart in the reference.  One frame of the consistent solve (the
  * arithmetic of pdg_solver_step, results equal to rounding) for callers that

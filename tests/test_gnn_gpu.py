@@ -1,0 +1,101 @@
+"""Warm-start network kernels against the float64 oracle (GPU).
+
+The GPU computes node GEMMs in bf16 on the tensor cores with fp32
+accumulation and keeps activations in bf16, so it is compared with the
+float64 oracle at bf16 tolerance: 2e-2 relative on the loss and outputs, and
+per parameter tensor a relative L2 error below 6e-2 with cosine > 0.995.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16_round(a):
+    a = np.ascontiguousarray(a, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def problem(seed=0, n=30):
+    from test_gnn_oracle import grid_graph
+    import gnn_oracle as G
+    rng = np.random.default_rng(seed)
+    ptr, adj, dst, src, deg = grid_graph(n)
+    N = n * n
+    x = rng.normal(size=(N, G.NF)).astype(np.float32)
+    e = rng.normal(size=(len(adj), G.EF)).astype(np.float32)
+    target = rng.normal(size=(N, 3)).astype(np.float32)
+    free = (rng.random(N) > 0.1).astype(np.float32)
+    p = {k: rng.normal(scale=0.25, size=s) for k, s in G.shapes()}
+    return G, p, x, e, src, dst, deg, target, free, ptr, adj
+
+
+def test_forward_backward_match_oracle(pdg):
+    G, p, x, e, src, dst, deg, target, free, ptr, adj = problem(0)
+    flat = G.flatten(p).astype(np.float32)
+    w = pdg.WarmStart(seed=1)
+    assert w.count == G.count()
+    w.set_params(flat)
+    assert np.array_equal(w.get_params(), flat)
+    out, loss, grads = w.eval(x, ptr, adj, e, target, free)
+    # the oracle on the GPU's bf16-rounded inputs and GEMM weights
+    pb = dict(G.unflatten(flat))
+    for k in pb:
+        if k[0] in "WABU":
+            pb[k] = bf16_round(pb[k]).astype(np.float64)
+    lo, go, oo = G.loss_and_grad(pb, bf16_round(x).astype(np.float64), e.astype(np.float64), src, dst, deg,
+                                 target.astype(np.float64), free.astype(np.float64))
+    assert abs(loss - lo) <= 2e-2 * lo
+    assert np.linalg.norm(out - oo) <= 2e-2 * np.linalg.norm(oo)
+    gg = G.unflatten(grads)
+    for name, _ in G.shapes():
+        a, b = gg[name].reshape(-1), go[name].reshape(-1)
+        nb_ = np.linalg.norm(b)
+        if nb_ == 0:
+            assert np.linalg.norm(a) < 1e-6
+            continue
+        cos = float(a @ b / (np.linalg.norm(a) * nb_ + 1e-30))
+        assert np.linalg.norm(a - b) <= 6e-2 * nb_, name
+        assert cos > 0.995, (name, cos)
+
+
+def test_adam_step_matches_oracle(pdg):
+    G, p, x, e, src, dst, deg, target, free, ptr, adj = problem(1, n=12)
+    flat = G.flatten(p).astype(np.float32)
+    w = pdg.WarmStart(seed=2)
+    w.set_params(flat)
+    m = np.zeros(len(flat)); v = np.zeros(len(flat)); cur = flat.astype(np.float64)
+    for t in range(1, 4):
+        _, _, grads = w.eval(x, ptr, adj, e, target, free)
+        w.adam_step(1e-3)
+        cur, m, v = G.adam(cur, grads.astype(np.float64), m, v, t, 1e-3)
+        got = w.get_params().astype(np.float64)
+        assert np.abs(got - cur).max() <= 1e-6 + 1e-5 * np.abs(cur).max()
+        cur = got
+
+
+def test_training_on_solver_data_lowers_loss_and_start_residual(pdg):
+    import scenes
+    ms, cs, cfgs, _ = scenes.batch(6, seed=3, max_iterations=300, tolerance=1e-6, n_range=(17, 25),
+                                   kernel=pdg.KERNEL_GRAPH)
+    train = pdg.Solver(cfgs, ms, cs)
+    w = pdg.WarmStart(seed=0)
+    w.attach(train)
+    losses = [w.train_frame(train, 2e-3) for _ in range(80)]
+    assert np.mean(losses[-10:]) < 0.5 * np.mean(losses[:10])
+    # held-out cloths: the learned start is kept where it lowers the start residual
+    ms2, cs2, cfgs2, _ = scenes.batch(6, seed=99, max_iterations=40, tolerance=0.0, n_range=(17, 25),
+                                      kernel=pdg.KERNEL_GRAPH, init=pdg.INIT_WARMSTART)
+    eval_s = pdg.Solver(cfgs2, ms2, cs2)
+    params = w.get_params()
+    w2 = pdg.WarmStart(seed=0)
+    w2.set_params(params)
+    w2.attach(eval_s)
+    for _ in range(5):
+        st = eval_s.step(1)
+    used = [s["warm_start_used"] for s in st]
+    ratio = [s["res_initial"] / s["res_inertial"] for s in st]
+    assert all(r <= 1.0 + 1e-6 for r in ratio)   # never worse than the inertial start
+    assert sum(used) >= 1 and min(ratio) < 1.0
