@@ -21,7 +21,7 @@ constexpr int L = 2;       // message-passing layers
 constexpr float kOffsetScale = 2.725e-3f;
 constexpr float kLenScale = 0.01f;
 
-// Flat fp32 parameter vector, in this order (the oracle uses the same):
+// Flat fp32 parameter vector, in this order (the order of pdg_warmstart_get_params):
 // We[H][NF] be[H] {A[H][H] B[H][H] C[H][EF] c[H] U[H][2H] u[H]} x L  Wd[NO][H] bd[NO]
 struct Layout {
     int We, be, A[L], B[L], C[L], c[L], U[L], u[L], Wd, bd, total;
