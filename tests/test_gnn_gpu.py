@@ -82,14 +82,27 @@ def test_training_on_solver_data_lowers_loss_and_start_residual(pdg):
                                    kernel=pdg.KERNEL_GRAPH)
     train = pdg.Solver(cfgs, ms, cs)
     w = pdg.WarmStart(seed=0)
+    untrained = w.get_params()
     w.attach(train)
-    losses = [w.train_frame(train, 2e-3) for _ in range(80)]
-    assert np.mean(losses[-10:]) < 0.5 * np.mean(losses[:10])
+    for _ in range(120):
+        w.train_frame(train, 2e-3)
+    params = w.get_params()
+    # the same held-out trajectories scored (lr = 0) by the trained and the
+    # untrained network: the solver's frames do not depend on the network
+    ms3, cs3, cfgs3, _ = scenes.batch(6, seed=7, max_iterations=300, tolerance=1e-6, n_range=(17, 25),
+                                      kernel=pdg.KERNEL_GRAPH)
+    scores = []
+    for prm in (untrained, params):
+        s3 = pdg.Solver(cfgs3, ms3, cs3)
+        w3 = pdg.WarmStart(seed=0)
+        w3.set_params(prm)
+        w3.attach(s3)
+        scores.append(np.mean([w3.train_frame(s3, 0.0) for _ in range(20)]))
+    assert scores[1] < 0.5 * scores[0], scores
     # held-out cloths: the learned start is kept where it lowers the start residual
     ms2, cs2, cfgs2, _ = scenes.batch(6, seed=99, max_iterations=40, tolerance=0.0, n_range=(17, 25),
                                       kernel=pdg.KERNEL_GRAPH, init=pdg.INIT_WARMSTART)
     eval_s = pdg.Solver(cfgs2, ms2, cs2)
-    params = w.get_params()
     w2 = pdg.WarmStart(seed=0)
     w2.set_params(params)
     w2.attach(eval_s)
