@@ -1,0 +1,128 @@
+"""Train and evaluate the learned warm start on data the PD solver generates.
+
+    python cloth-cuda_gb300/train_warmstart.py [--trajectories 256] [--frames 64]
+        [--batch 32] [--lr 1e-3] [--eval-seeds 128] [--out params.npy] [--json result.json]
+
+Training data: trajectories of cloths drawn from the batched-workload
+distribution (scenes.batch), `batch` cloths per solver; every frame of every
+trajectory is one training batch: inputs (x_n, v_n, y), target the solver's
+frame result x_{n+1} - y, computed with a deep solve (cap 400 sweeps, relative
+residual 1e-6) so the target is close to the converged positions.  MSE loss,
+Adam.  Evaluation on `eval_seeds` held-out cloths: for each, the same frames
+are solved from the inertial start and from the learned start (kept only
+where its residual is lower), to relative residual 1e-5 with cap 200; the
+script reports the start-residual ratio, iterations, convergence and the
+vertex-steps/s of both.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import pdg  # noqa: E402
+import scenes  # noqa: E402
+
+
+def train(args, log=print):
+    w = pdg.WarmStart(seed=args.seed)
+    nbatches = max(1, args.trajectories // args.batch)
+    losses = []
+    t0 = time.time()
+    for b in range(nbatches):
+        ms, cs, cfgs, _ = scenes.batch(args.batch, seed=1000 + b, max_iterations=args.target_cap,
+                                       tolerance=args.target_tol, kernel=pdg.KERNEL_GRAPH, n_range=args.n_range)
+        s = pdg.Solver(cfgs, ms, cs)
+        w.attach(s)
+        bl = [w.train_frame(s, args.lr) for _ in range(args.frames)]
+        losses.append(float(np.mean(bl)))
+        log("batch %d/%d  mean loss %.4f  (%.1f s)" % (b + 1, nbatches, losses[-1], time.time() - t0))
+        s.close()
+        w.solver = None
+    return w, losses
+
+
+def evaluate(params, args, log=print):
+    res = {"inertial": [], "learned": []}
+    times = {"inertial": 0.0, "learned": 0.0}
+    verts = {"inertial": 0, "learned": 0}
+    nb = max(1, args.eval_seeds // args.batch)
+    for b in range(nb):
+        for mode in ("inertial", "learned"):
+            init = pdg.INIT_WARMSTART if mode == "learned" else pdg.INIT_INERTIAL
+            ms, cs, cfgs, _ = scenes.batch(args.batch, seed=900000 + b, max_iterations=200, tolerance=1e-5,
+                                           kernel=pdg.KERNEL_GRAPH, init=init, n_range=args.n_range)
+            s = pdg.Solver(cfgs, ms, cs)
+            w = None
+            if mode == "learned":
+                w = pdg.WarmStart(seed=0)
+                w.set_params(params)
+                w.attach(s)
+            N = sum(m.N for m in ms)
+            for f in range(args.eval_frames):
+                t0 = time.perf_counter()
+                st = s.step(1)
+                times[mode] += time.perf_counter() - t0
+                verts[mode] += N
+                res[mode] += [dict(frame=f, **x) for x in st]
+            s.close()
+            if w is not None:
+                w.close()
+    out = {}
+    for mode in res:
+        r = res[mode]
+        out[mode] = dict(
+            iterations_mean=float(np.mean([x["iterations"] for x in r])),
+            converged_fraction=float(np.mean([x["converged"] for x in r])),
+            start_ratio_mean=float(np.mean([x["res_initial"] / max(x["res_inertial"], 1e-30) for x in r])),
+            rel_residual_median=float(np.median([x["rel_residual"] for x in r])),
+            learned_start_kept=float(np.mean([x["warm_start_used"] for x in r])),
+            vertex_steps_per_s_host_timed=verts[mode] / max(times[mode], 1e-9))
+        log(mode, json.dumps(out[mode]))
+    conv_i = [x["iterations"] for x in res["inertial"]]
+    conv_l = [x["iterations"] for x in res["learned"]]
+    both = [(a, b) for a, b, xi, xl in zip(conv_i, conv_l, res["inertial"], res["learned"])
+            if xi["converged"] and xl["converged"]]
+    out["iterations_saved_on_frames_both_converge"] = (
+        float(1 - np.sum([b for _, b in both]) / max(np.sum([a for a, _ in both]), 1)) if both else None)
+    out["frames_both_converge"] = len(both)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--trajectories", type=int, default=256)
+    ap.add_argument("--frames", type=int, default=64)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--target-cap", type=int, default=400)
+    ap.add_argument("--target-tol", type=float, default=1e-6)
+    ap.add_argument("--eval-seeds", type=int, default=128)
+    ap.add_argument("--eval-frames", type=int, default=16)
+    ap.add_argument("--n-min", type=int, default=17)
+    ap.add_argument("--n-max", type=int, default=129)
+    ap.add_argument("--out", default="")
+    ap.add_argument("--json", default="")
+    args = ap.parse_args()
+    args.n_range = (args.n_min, args.n_max)
+    w, losses = train(args)
+    params = w.get_params()
+    if args.out:
+        np.save(args.out, params)
+    ev = evaluate(params, args)
+    result = dict(args={k: v for k, v in vars(args).items() if k != "n_range"}, train_loss=losses, eval=ev)
+    print(json.dumps(result))
+    if args.json:
+        json.dump(result, open(args.json, "w"), indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -61,7 +61,7 @@ def test_oracle_literal_reproduces_reference_kernels(oracle, path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("path", [f for f in FILES if "_s1" in f], ids=lambda f: os.path.basename(f)[4:-4])
+@pytest.mark.parametrize("path", [f for f in FILES if f.endswith("_s1.npz")], ids=lambda f: os.path.basename(f)[4:-4])
 def test_library_literal_mode_reproduces_reference_kernels(pdg, oracle, path):
     sc, pos, d, meta = load(oracle, path)
     p = meta["params"]
