@@ -49,6 +49,21 @@ def train(args, log=print):
     return w, losses
 
 
+def score(params, args, seeds=2, frames=32, base_seed=500000):
+    """Mean training loss (lr = 0) of `params` on held-out trajectories."""
+    out = []
+    for b in range(seeds):
+        ms, cs, cfgs, _ = scenes.batch(args.batch, seed=base_seed + b, max_iterations=args.target_cap,
+                                       tolerance=args.target_tol, kernel=pdg.KERNEL_GRAPH, n_range=args.n_range)
+        s = pdg.Solver(cfgs, ms, cs)
+        w = pdg.WarmStart(seed=0)
+        w.set_params(params)
+        w.attach(s)
+        out += [w.train_frame(s, 0.0) for _ in range(frames)]
+        s.close(); w.close()
+    return float(np.mean(out))
+
+
 def evaluate(params, args, log=print):
     res = {"inertial": [], "learned": []}
     times = {"inertial": 0.0, "learned": 0.0}
@@ -117,8 +132,12 @@ def main():
     params = w.get_params()
     if args.out:
         np.save(args.out, params)
+    held_out = score(params, args, frames=args.frames)
+    zero = score(np.zeros_like(params), args, frames=args.frames)
+    print("held-out loss: trained %.4f, zero predictor (inertial start) %.4f" % (held_out, zero))
     ev = evaluate(params, args)
-    result = dict(args={k: v for k, v in vars(args).items() if k != "n_range"}, train_loss=losses, eval=ev)
+    result = dict(args={k: v for k, v in vars(args).items() if k != "n_range"}, train_loss=losses,
+                  held_out_loss=held_out, zero_predictor_loss=zero, eval=ev)
     print(json.dumps(result))
     if args.json:
         json.dump(result, open(args.json, "w"), indent=1)
