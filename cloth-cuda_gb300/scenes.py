@@ -39,6 +39,18 @@ def boundary_vertices(n):
     return np.array(sorted(set(idx)), np.int32)
 
 
+def shard(sizes, rank, world):
+    """Contiguous split of cloths (vertex counts `sizes`) over `world` ranks,
+    balanced by vertices: rank r gets the cloths whose cumulative vertex
+    count midpoint falls in [r/world, (r+1)/world) of the total.  Cloths are
+    independent, so a sharded batch needs no exchange between ranks."""
+    sizes = np.asarray(sizes, np.float64)
+    total = sizes.sum()
+    mid = (np.cumsum(sizes) - 0.5 * sizes) / max(total, 1.0)
+    owner = np.minimum((mid * world).astype(int), world - 1)
+    return [i for i in range(len(sizes)) if owner[i] == rank]
+
+
 def batch(count, seed=0, *, max_iterations=200, tolerance=1e-5, rho=0.99, n_range=(17, 129),
           size_range=(0.5, 2.0), **cfg_kw):
     """(meshes, constraints, configs, params) of `count` cloths drawn from
