@@ -28,7 +28,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, long long 
         } else {
             const long long t0 = clock64();
             while (*vgen == gen) {
-                if (clock64() - t0 > budget) { atomicCAS(err, 0, 1); break; }
+                if (clock64() - t0 > budget || *(volatile int*)err != 0) { atomicCAS(err, 0, 1); break; }
                 __nanosleep(64);
             }
         }

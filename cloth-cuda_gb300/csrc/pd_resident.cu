@@ -34,7 +34,7 @@ __device__ __forceinline__ bool grid_barrier_r(unsigned* bar, int* err, long lon
         } else {
             const long long t0 = clock64();
             while (*vgen == gen) {
-                if (clock64() - t0 > budget) { atomicCAS(err, 0, 2); break; }
+                if (clock64() - t0 > budget || *(volatile int*)err != 0) { atomicCAS(err, 0, 2); break; }
                 __nanosleep(32);
             }
         }

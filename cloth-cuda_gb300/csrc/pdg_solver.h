@@ -81,11 +81,12 @@ struct pdg_solver {
     int have_final = 1;
     int persist_grid = 0;
     long long launches = 0;
+    long long wait_budget = 2000000000LL;   // clock64 cycles per bounded wait (~1 s)
     int kernels_per_frame = 0;
 
     pdg::DevBuf<float4> X, V, Y, A, B, aux, warm;
     pdg::DevBuf<float> mass, omega, stage_x, stage_v;
-    pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, err, nbr_ptr, nbr;
+    pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, nbr_ptr, nbr;
     pdg::DevBuf<double> acc;
     pdg::DevBuf<unsigned long long> pflag;
     unsigned long long frame_seq = 0;

@@ -71,9 +71,8 @@ int upload_all(pdg_solver* s)
     CK(s->X.alloc(L.ntot)); CK(s->V.alloc(L.ntot)); CK(s->Y.alloc(L.ntot));
     CK(s->A.alloc(L.ntot)); CK(s->B.alloc(L.ntot));
     CK(s->stage_x.alloc(3 * (size_t)L.ntot)); CK(s->stage_v.alloc(3 * (size_t)L.ntot));
-    CK(s->bar.alloc(2)); CK(s->err.alloc(1));
-    CK(cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st));
-    CK(cudaMemsetAsync(s->err.p, 0, sizeof(int), st));
+    CK(s->bar.alloc(4));   // [0] arrivals, [1] generation, [2] error word
+    CK(cudaMemsetAsync(s->bar.p, 0, 4 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(s->crt.p, 0, sizeof(ClothRT) * L.ncloth, st));
     CK(cudaMemsetAsync(s->Y.p, 0, sizeof(float4) * L.ntot, st));
     CK(cudaMemsetAsync(s->V.p, 0, sizeof(float4) * L.ntot, st));
@@ -110,8 +109,8 @@ PersistArgs persist_args(pdg_solver* s)
     p.X = s->X.p; p.Xw = s->X.p; p.V = s->V.p; p.aux = s->aux.p; p.mass = s->mass.p; p.vcloth = s->vcloth.p;
     p.warm = nullptr; p.Y = s->Y.p;
     p.n = s->L.ntot; p.npatch = s->L.npatch; p.max_iter = s->L.cap; p.have_final = s->have_final;
-    p.mode = s->mode; p.bar = s->bar.p; p.err = s->err.p;
-    p.spin_budget = 2000000000LL;   // ~1 s at 2 GHz per wait
+    p.mode = s->mode; p.bar = s->bar.p; p.err = reinterpret_cast<int*>(s->bar.p + 2);
+    p.spin_budget = s->wait_budget;
     p.nbr_ptr = s->nbr_ptr.p; p.nbr = s->nbr.p; p.pflag = s->pflag.p;
     p.frame_seq = ++s->frame_seq;
     p.nbr_sync = s->nbr_sync;
@@ -297,17 +296,31 @@ int pdg_solver_cloth_counts(const pdg_solver* s, int cloth, int* N, int* T)
     return PDG_OK;
 }
 
+// Reads and clears the error word of the bounded waits (stream synchronised).
+static int take_wait_error(pdg_solver* s)
+{
+    int e = 0;
+    CK(cudaMemcpy(&e, s->bar.p + 2, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!e) return PDG_OK;
+    CK(cudaMemset(s->bar.p + 2, 0, sizeof(int)));
+    return set_error(PDG_ERR_TIMEOUT, "bounded wait ran out (%s)",
+                     e == 1 ? "grid barrier" : e == 2 ? "resident grid barrier" : "neighbour mark");
+}
+
 int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
 {
     if (!s || nframes < 0) return set_error(PDG_ERR_ARG, "pdg_solver_step: bad arguments");
     for (int f = 0; f < nframes; ++f) {
-        if (s->kernel == PDG_KERNEL_PERSISTENT) {
+        if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
+            // barrier counter and generation start clean every frame; the
+            // error word stays set until it is reported, and a kernel that
+            // finds it set leaves at its first barrier
+            CK(cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), s->stream));
             const PersistArgs p = persist_args(s);
-            CK(launch_persistent(p, s->nt, s->persist_grid, s->L.smem_bytes, s->stream));
-            s->launches += 1;
-        } else if (s->kernel == PDG_KERNEL_RESIDENT) {
-            const PersistArgs p = persist_args(s);
-            CK(launch_resident(p, s->persist_grid, s->L.smem_resident, s->stream));
+            if (s->kernel == PDG_KERNEL_PERSISTENT)
+                CK(launch_persistent(p, s->nt, s->persist_grid, s->L.smem_bytes, s->stream));
+            else
+                CK(launch_resident(p, s->persist_grid, s->L.smem_resident, s->stream));
             s->launches += 1;
         } else {
             if (!s->graph) {
@@ -322,9 +335,8 @@ int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
         CK(cudaMemcpyAsync(s->h_rt.data(), s->crt.p, sizeof(ClothRT) * s->L.ncloth, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
-            int e = 0;
-            CK(cudaMemcpy(&e, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
-            if (e) return set_error(PDG_ERR_TIMEOUT, "grid barrier timed out (code %d)", e);
+            const int rc = take_wait_error(s);
+            if (rc) return rc;
         }
         for (int c = 0; c < s->L.ncloth; ++c) {
             const ClothRT& r = s->h_rt[c];
@@ -459,6 +471,8 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
     for (int f = 0; f < nframes && rc == PDG_OK; ++f) {
         cudaEventRecord(e[0], st);
         if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
+            cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st);
+            cudaEventRecord(e[0], st);   // the frame's events bracket the launch only
             const PersistArgs p = persist_args(s);
             cudaError_t err = s->kernel == PDG_KERNEL_RESIDENT
                                   ? launch_resident(p, s->persist_grid, L.smem_resident, st)
@@ -494,10 +508,21 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
     }
     for (auto& ev : e) cudaEventDestroy(ev);
     if (rc) return rc;
+    if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
+        rc = take_wait_error(s);
+        if (rc) return rc;
+    }
     if (frame_ms) *frame_ms = (float)(tf / nframes);
     const bool one_launch = s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT;
     const int sweeps = std::max(1, L.cap + (one_launch && s->have_final ? 1 : 0));
     if (sweep_ms) *sweep_ms = (float)(ts / nframes / sweeps);
+    return PDG_OK;
+}
+
+int pdg_solver_set_wait_budget(pdg_solver* s, long long cycles)
+{
+    if (!s || cycles < 0) return set_error(PDG_ERR_ARG, "pdg_solver_set_wait_budget: bad arguments");
+    s->wait_budget = cycles;
     return PDG_OK;
 }
 

@@ -311,6 +311,11 @@ class Solver:
         _check(lib().pdg_solver_launch_info(self.h, C.byref(k), C.byref(pv), C.byref(nt), C.byref(npch)))
         return dict(kernel=k.value, patch_verts=pv.value, block_threads=nt.value, npatches=npch.value)
 
+    def set_wait_budget(self, cycles):
+        """clock64 cycles each grid-barrier / neighbour wait may spin before
+        the one-launch-per-frame kernels give up with ERR_TIMEOUT."""
+        _check(lib().pdg_solver_set_wait_budget(self.h, C.c_longlong(int(cycles))))
+
 
 class WarmStart:
     """Learned warm start (mesh message-passing network on the GPU)."""

@@ -194,6 +194,14 @@ int  pdg_solver_launch_count(const pdg_solver* s, long long* n);
  * average frame; sweep_ms: average duration of one fused sweep (the events
  * bracket the sweep launches; persistent kernel: frame time / sweeps). */
 int  pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* sweep_ms);
+/* Wait budget (GPU clock cycles) of every grid-barrier / neighbour wait in
+ * the persistent and resident kernels (default 2e9, about 1 s).  When a wait
+ * runs out the kernel records an error and every block leaves at its next
+ * wait.  The error stays recorded (later frames of the same call leave at
+ * their first barrier) until pdg_solver_step with stats or
+ * pdg_solver_time_frames reports it as PDG_ERR_TIMEOUT and clears it; the
+ * solver state is then undefined until pdg_solver_set_state. */
+int  pdg_solver_set_wait_budget(pdg_solver* s, long long cycles);
 /* Stream the solver works on (a cudaStream_t). */
 int  pdg_solver_stream(const pdg_solver* s, void** stream);
 /* Launch shape the solver picked: kernel (PDG_KERNEL_*), patch_verts,

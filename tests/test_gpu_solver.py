@@ -266,3 +266,26 @@ def test_zero_iterations(pdg, oracle):
     y = sc.predict(a["rest"], np.zeros_like(a["rest"])).reshape(-1, 3)
     y[[0, 8]] = a["rest"][[0, 8]]
     assert np.allclose(x, y, atol=1e-7) and st["iterations"] == 0
+
+
+@pytest.mark.parametrize("kernel", ["persistent", "resident"])
+def test_bounded_waits_run_out_cleanly(pdg, oracle, kernel):
+    # failure detection without a GPU fault: a wait budget of one cycle makes
+    # every grid-barrier / neighbour wait run out; the kernel records the
+    # error, all blocks leave, the host reads PDG_ERR_TIMEOUT, and the next
+    # frame with a normal budget runs on the same context
+    m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=8)
+    cfg.kernel = pdg.KERNEL_PERSISTENT if kernel == "persistent" else pdg.KERNEL_RESIDENT
+    s = pdg.Solver(cfg, m, c)
+    s.set_wait_budget(1)
+    with pytest.raises(pdg.PDGError) as e:
+        s.step(1)
+    assert e.value.code == pdg.ERR_TIMEOUT
+    s.set_wait_budget(2_000_000_000)
+    s.set_state(a["rest"], np.zeros_like(a["rest"]))
+    st = s.step(1)[0]
+    x, v = s.get_state()
+    cfg.kernel = pdg.KERNEL_GRAPH
+    ref = pdg.Solver(cfg, m, c)
+    ref.step(1, stats=False)
+    assert np.array_equal(x, ref.get_state()[0]) and st["status"] == 0
