@@ -201,6 +201,7 @@ def run_ours(args, rank, world, local_rank):
     T = sum(m.T for m in meshes)
     E = sum(len(c.arrays()["w"]) for c in cons)
     info = s.launch_info()
+    tune = s.tune_results()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
 
     # warm-up (includes graph capture)
@@ -308,6 +309,10 @@ def run_ours(args, rank, world, local_rank):
                        "kernel": {1: "graph", 2: "persistent", 3: "resident"}[info["kernel"]],
                        "patch_verts": info["patch_verts"], "block_threads": info["block_threads"],
                        "patches": info["npatches"], "l2": "flushed before every timed step (512 MB write)",
+                       "launch_plan": "autotuned" if args.kernel == 4 else "fixed by --kernel",
+                       "autotune_ms_per_frame": {"%s/%d/%d" % ({1: "graph", 2: "persistent", 3: "resident"}
+                                                              [t["kernel"]], t["patch_verts"], t["block_threads"]):
+                                                 round(t["frame_ms"], 4) for t in tune if t["frame_ms"] >= 0},
                        "parallelism": "replica per GPU" if world > 1 else "single GPU",
                        "iterations_mean": float(np.mean(iters)), "converged_fraction": float(np.mean(conv)),
                        "rel_residual_median": float(np.median(rels)), "rel_residual_max": float(np.max(rels))},
@@ -336,7 +341,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain257", choices=sorted(WORKLOADS))
-    ap.add_argument("--kernel", type=int, default=0)
+    ap.add_argument("--kernel", type=int, default=4, help="0 auto, 1 graph, 2 persistent, 3 resident, 4 autotune")
     ap.add_argument("--patch-verts", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

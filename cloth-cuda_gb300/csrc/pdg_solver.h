@@ -105,11 +105,18 @@ struct pdg_solver {
     bool warm_valid = false;
     pdg_warmstart* ws = nullptr;   // attached learned warm start (not owned)
     bool any_warm = false;         // some cloth asks for PDG_INIT_WARMSTART
+    std::vector<pdg_tune_entry> tune;   // autotuner candidate table
 
     ~pdg_solver();
 };
 
 namespace pdg {
+// solver creation with a concrete launch plan (solver.cpp) and through the
+// autotuner (tune.cpp)
+int create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                  void* stream, pdg_solver** out);
+int autotune_create(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                    void* stream, pdg_solver** out);
 // learned warm start hooks (gnn.cu): features + forward into s->warm
 int warm_infer_enqueue(pdg_warmstart* w, pdg_solver* s);
 int warm_kernel_count();

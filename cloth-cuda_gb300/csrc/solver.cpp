@@ -150,8 +150,10 @@ int build_graph(pdg_solver* s)
     return PDG_OK;
 }
 
-int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
-                void* stream, pdg_solver** out)
+}  // namespace
+
+int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                       void* stream, pdg_solver** out)
 {
     if (!out || n <= 0 || !cfgs || !meshes || !cons) return set_error(PDG_ERR_ARG, "solver create: bad arguments");
     std::unique_ptr<pdg_solver> s(new pdg_solver);
@@ -178,6 +180,7 @@ int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, co
         return set_error(PDG_ERR_ARG, "block_threads must be 128, 256 or 512");
     s->patch_verts = c0.patch_verts ? c0.patch_verts : 256;
     if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
+    if (c0.kernel == PDG_KERNEL_AUTOTUNE) return autotune_create(n, cfgs, meshes, cons, stream, out);
     if (c0.kernel < PDG_KERNEL_AUTO || c0.kernel > PDG_KERNEL_RESIDENT) return set_error(PDG_ERR_ARG, "unknown kernel");
     s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_GRAPH : c0.kernel;
     for (const auto& c : s->cloths) s->any_warm = s->any_warm || c.cfg.init == PDG_INIT_WARMSTART;
@@ -246,6 +249,8 @@ int create_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, co
     return PDG_OK;
 }
 
+namespace {
+
 int cloth_range(const pdg_solver* s, int cloth, int* vb, int* n)
 {
     if (!s || cloth < 0 || cloth >= s->L.ncloth) return set_error(PDG_ERR_ARG, "cloth index out of range");
@@ -263,7 +268,7 @@ int pdg_solver_create(const pdg_config* cfg, const pdg_mesh* m, const pdg_constr
 {
     try {
         if (!cfg) return set_error(PDG_ERR_ARG, "null config");
-        return create_impl(1, cfg, &m, &c, stream, out);
+        return pdg::create_solver(1, cfg, &m, &c, stream, out);
     } catch (const std::bad_alloc&) {
         return set_error(PDG_ERR_ALLOC, "host allocation failed");
     }
@@ -273,7 +278,7 @@ int pdg_solver_create_batch(int n, const pdg_config* cfgs, const pdg_mesh* const
                             const pdg_constraints* const* cons, void* stream, pdg_solver** out)
 {
     try {
-        return create_impl(n, cfgs, meshes, cons, stream, out);
+        return pdg::create_solver(n, cfgs, meshes, cons, stream, out);
     } catch (const std::bad_alloc&) {
         return set_error(PDG_ERR_ALLOC, "host allocation failed");
     }

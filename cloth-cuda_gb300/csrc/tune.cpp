@@ -1,0 +1,175 @@
+// Autotuner of the per-frame launch plan.
+//
+// A launch plan is (launch structure, owned vertices per patch, threads per
+// block): one fused launch per sweep replayed from a CUDA graph, one
+// cooperative launch per frame with a grid barrier after every sweep, or the
+// resident launch that keeps each patch's records on chip and synchronises
+// only with neighbouring patches.  Which is fastest depends on the problem
+// size against the SM count and the shared-memory capacity, so the tuner
+// builds the solver once per candidate plan, runs one untimed frame (graph
+// instantiation, cold caches) and three timed frames from the rest state, and
+// builds the final solver with the fastest plan.  All plans compute the same
+// iterates bit for bit, so the choice never changes results.
+//
+// The choice is cached per (device, problem shape) for the life of the
+// process; a cache hit creates the solver directly.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pdg_solver.h"
+
+namespace pdg {
+
+int set_error(int code, const char* fmt, ...);
+
+namespace {
+
+struct Plan {
+    int kernel, patch_verts, block_threads;
+};
+
+struct CacheEntry {
+    Plan plan;
+    std::vector<pdg_tune_entry> table;
+};
+
+std::mutex g_mu;
+std::map<std::string, CacheEntry> g_cache;
+
+constexpr int kWarmFrames = 1;
+constexpr int kTimedFrames = 3;
+
+std::string problem_key(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, dev);
+    long long nv = 0, nt = 0;
+    int cap = 0, tol = 0, warm = 0, final_res = 0;
+    for (int i = 0; i < n; ++i) {
+        nv += meshes[i]->data->N;
+        nt += meshes[i]->data->T;
+        cap = std::max(cap, cfgs[i].max_iterations);
+        tol |= cfgs[i].tolerance > 0.f;
+        warm |= cfgs[i].init == PDG_INIT_WARMSTART;
+        final_res |= cfgs[i].compute_final_residual;
+    }
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s/%d/%d|n%d v%lld t%lld cap%d tol%d warm%d fin%d mode%d", prop.name,
+                  prop.multiProcessorCount, dev, n, nv, nt, cap, tol, warm, final_res, cfgs[0].mode);
+    return buf;
+}
+
+std::vector<Plan> candidates(bool warm)
+{
+    std::vector<Plan> c;
+    if (!warm) {
+        c.push_back({PDG_KERNEL_RESIDENT, 0, 0});
+        c.push_back({PDG_KERNEL_PERSISTENT, 256, 256});
+        c.push_back({PDG_KERNEL_PERSISTENT, 512, 512});
+    }
+    for (Plan p : {Plan{PDG_KERNEL_GRAPH, 128, 128}, Plan{PDG_KERNEL_GRAPH, 256, 256}, Plan{PDG_KERNEL_GRAPH, 512, 256},
+                   Plan{PDG_KERNEL_GRAPH, 512, 512}, Plan{PDG_KERNEL_GRAPH, 1024, 512}})
+        c.push_back(p);
+    return c;
+}
+
+int create_with(const Plan& p, int n, const pdg_config* cfgs, const pdg_mesh* const* meshes,
+                const pdg_constraints* const* cons, void* stream, pdg_solver** out)
+{
+    std::vector<pdg_config> c(cfgs, cfgs + n);
+    for (auto& x : c) {
+        x.kernel = p.kernel;
+        x.patch_verts = p.patch_verts;
+        x.block_threads = p.block_threads;
+    }
+    return create_solver(n, c.data(), meshes, cons, stream, out);
+}
+
+}  // namespace
+
+int autotune_create(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                    void* stream, pdg_solver** out)
+{
+    if (!out || n <= 0 || !cfgs || !meshes || !cons) return set_error(PDG_ERR_ARG, "solver create: bad arguments");
+    for (int i = 0; i < n; ++i)
+        if (!meshes[i] || !cons[i]) return set_error(PDG_ERR_ARG, "cloth %d: null mesh or constraints", i);
+    const std::string key = problem_key(n, cfgs, meshes);
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_cache.find(key);
+        if (it != g_cache.end()) {
+            const CacheEntry e = it->second;
+            const int rc = create_with(e.plan, n, cfgs, meshes, cons, stream, out);
+            if (rc) return rc;
+            (*out)->tune = e.table;
+            for (auto& t : (*out)->tune) t.cached = 1;
+            return PDG_OK;
+        }
+    }
+    bool warm = false;
+    for (int i = 0; i < n; ++i) warm = warm || cfgs[i].init == PDG_INIT_WARMSTART;
+
+    std::vector<pdg_tune_entry> table;
+    int best = -1;
+    for (const Plan& p : candidates(warm)) {
+        pdg_solver* s = nullptr;
+        pdg_tune_entry t{p.kernel, p.patch_verts, p.block_threads, -1.f, 0, 0};
+        if (create_with(p, n, cfgs, meshes, cons, stream, &s) != PDG_OK) {   // plan does not fit
+            table.push_back(t);
+            continue;
+        }
+        int k = 0, pv = 0, nt = 0, np = 0;
+        pdg_solver_launch_info(s, &k, &pv, &nt, &np);
+        t.kernel = k; t.patch_verts = pv; t.block_threads = nt;
+        // the per-sweep plans shrink an oversized patch; skip duplicates
+        bool dup = false;
+        for (const auto& o : table)
+            dup = dup || (o.frame_ms >= 0.f && o.kernel == k && o.patch_verts == pv && o.block_threads == nt);
+        if (dup) { pdg_solver_destroy(s); continue; }
+        int rc = pdg_solver_step(s, kWarmFrames, nullptr);
+        float ms = 0.f;
+        if (rc == PDG_OK) rc = pdg_solver_time_frames(s, kTimedFrames, &ms, nullptr);
+        pdg_solver_destroy(s);
+        if (rc != PDG_OK) return rc;   // a failure of a plan that fits is a real error
+        t.frame_ms = ms;
+        table.push_back(t);
+        if (best < 0 || ms < table[best].frame_ms) best = (int)table.size() - 1;
+    }
+    if (best < 0) return set_error(PDG_ERR_ARG, "autotuner: no launch plan fits this problem");
+    table[best].chosen = 1;
+    const Plan win{table[best].kernel, table[best].patch_verts, table[best].block_threads};
+    const int rc = create_with(win, n, cfgs, meshes, cons, stream, out);
+    if (rc) return rc;
+    (*out)->tune = table;
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_cache[key] = CacheEntry{win, table};
+    return PDG_OK;
+}
+
+}  // namespace pdg
+
+extern "C" {
+
+int pdg_solver_tune_results(const pdg_solver* s, pdg_tune_entry* out, int cap, int* n)
+{
+    if (!s || !n || cap < 0 || (cap > 0 && !out)) return pdg::set_error(PDG_ERR_ARG, "pdg_solver_tune_results: bad arguments");
+    *n = (int)s->tune.size();
+    for (int i = 0; i < std::min(cap, *n); ++i) out[i] = s->tune[i];
+    return PDG_OK;
+}
+
+void pdg_autotune_clear_cache(void)
+{
+    std::lock_guard<std::mutex> lk(pdg::g_mu);
+    pdg::g_cache.clear();
+}
+
+}  // extern "C"

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "libpdg.so")
 OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_STATE, ERR_TIMEOUT, ERR_NUMERIC, ERR_IO = 0, -1, -2, -3, -4, -5, -6, -7
 MODE_CONSISTENT, MODE_REFERENCE_LITERAL = 0, 1
 INIT_INERTIAL, INIT_PREVIOUS, INIT_WARMSTART = 0, 1, 2
-KERNEL_AUTO, KERNEL_GRAPH, KERNEL_PERSISTENT, KERNEL_RESIDENT = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_GRAPH, KERNEL_PERSISTENT, KERNEL_RESIDENT, KERNEL_AUTOTUNE = 0, 1, 2, 3, 4
 
 
 class PDGError(RuntimeError):
@@ -62,6 +62,18 @@ class FrameStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("kernel", C.c_int), ("patch_verts", C.c_int), ("block_threads", C.c_int),
+                ("frame_ms", C.c_float), ("chosen", C.c_int), ("cached", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def autotune_clear_cache():
+    lib().pdg_autotune_clear_cache()
 
 
 _lib = None
@@ -310,6 +322,14 @@ class Solver:
         k = C.c_int(); pv = C.c_int(); nt = C.c_int(); npch = C.c_int()
         _check(lib().pdg_solver_launch_info(self.h, C.byref(k), C.byref(pv), C.byref(nt), C.byref(npch)))
         return dict(kernel=k.value, patch_verts=pv.value, block_threads=nt.value, npatches=npch.value)
+
+    def tune_results(self):
+        """Candidate table of the autotuner (empty unless created with KERNEL_AUTOTUNE)."""
+        n = C.c_int()
+        _check(lib().pdg_solver_tune_results(self.h, None, 0, C.byref(n)))
+        out = (TuneEntry * max(1, n.value))()
+        _check(lib().pdg_solver_tune_results(self.h, out, n.value, C.byref(n)))
+        return [out[i].as_dict() for i in range(n.value)]
 
     def set_wait_budget(self, cycles):
         """clock64 cycles each grid-barrier / neighbour wait may spin before

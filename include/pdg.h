@@ -44,10 +44,15 @@ extern "C" {
                                  residual is below the inertial start's     */
 
 /* Launch structure of the iteration loop. */
-#define PDG_KERNEL_AUTO       0  /* autotuner picks                         */
+#define PDG_KERNEL_AUTO       0  /* resident when it fits, else graph (no timing) */
 #define PDG_KERNEL_GRAPH      1  /* one fused launch per iteration, frame in a CUDA graph */
 #define PDG_KERNEL_PERSISTENT 2  /* one cooperative launch per frame, bounded grid barrier */
 #define PDG_KERNEL_RESIDENT   3  /* persistent, one patch per block, records kept on chip */
+#define PDG_KERNEL_AUTOTUNE   4  /* time every launch plan that fits (launch
+                                    structure, patch size, threads per block)
+                                    on this problem and keep the fastest;
+                                    the choice is cached per device and
+                                    problem shape for the process           */
 
 /* Solver configuration.  Mirrors PDSolverConfig (include/pd_solver.h:4-15);
  * fields after `damping` extend it. */
@@ -68,8 +73,8 @@ typedef struct pdg_config {
     int   mode;               /* PDG_MODE_* (CONSISTENT)                      */
     int   init;               /* PDG_INIT_* (INERTIAL)                        */
     int   kernel;             /* PDG_KERNEL_* (AUTO)                          */
-    int   patch_verts;        /* owned vertices per patch, 0 = autotune       */
-    int   block_threads;      /* threads per patch block, 0 = autotune        */
+    int   patch_verts;        /* owned vertices per patch, 0 = solver's choice */
+    int   block_threads;      /* threads per patch block, 0 = solver's choice  */
     int   compute_final_residual; /* evaluate r(x) of the returned iterate (1) */
 } pdg_config;
 
@@ -209,6 +214,26 @@ int  pdg_solver_stream(const pdg_solver* s, void** stream);
 int  pdg_solver_launch_info(const pdg_solver* s, int* kernel, int* patch_verts,
                             int* block_threads, int* npatches);
 void pdg_solver_destroy(pdg_solver* s);
+
+/* ---------------- autotuner (no counterpart in the reference) -------------
+ * PDG_KERNEL_AUTOTUNE creates the solver once per candidate launch plan,
+ * runs one untimed and three timed frames from the rest state (CUDA events
+ * on the solver's stream), and builds the final solver with the fastest
+ * plan.  Every plan computes bitwise the same iterates, so the choice
+ * changes the speed only.  The candidate table is kept in the solver. */
+typedef struct pdg_tune_entry {
+    int   kernel;             /* PDG_KERNEL_GRAPH / _PERSISTENT / _RESIDENT   */
+    int   patch_verts;        /* owned vertices per patch                     */
+    int   block_threads;      /* threads per block                            */
+    float frame_ms;           /* mean frame time; < 0: plan does not fit      */
+    int   chosen;             /* 1 for the plan the solver runs               */
+    int   cached;             /* 1 when the choice came from the cache        */
+} pdg_tune_entry;
+/* Copies up to `cap` entries of the candidate table; *n = table size (0 for
+ * solvers not created with PDG_KERNEL_AUTOTUNE). */
+int  pdg_solver_tune_results(const pdg_solver* s, pdg_tune_entry* out, int cap, int* n);
+/* Forgets every cached choice of this process. */
+void pdg_autotune_clear_cache(void);
 
 /* ---------------- learned warm start (no counterpart in the reference) ----
  * A 2-layer mesh message-passing network (hidden 64, bf16 weights and

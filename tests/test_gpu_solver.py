@@ -289,3 +289,29 @@ def test_bounded_waits_run_out_cleanly(pdg, oracle, kernel):
     ref = pdg.Solver(cfg, m, c)
     ref.step(1, stats=False)
     assert np.array_equal(x, ref.get_state()[0]) and st["status"] == 0
+
+
+def test_autotuner_picks_a_plan_and_keeps_the_bits(pdg, oracle):
+    # every candidate plan computes the same iterates, so the tuned solver
+    # must equal the per-sweep graph solver bit for bit; the second creation
+    # of the same problem shape comes from the cache
+    pdg.autotune_clear_cache()
+    m, c, cfg, sc, a = scene(pdg, oracle, n=65, max_iterations=12, kernel=pdg.KERNEL_AUTOTUNE)
+    s = pdg.Solver(cfg, m, c)
+    table = s.tune_results()
+    timed = [t for t in table if t["frame_ms"] >= 0]
+    assert len(timed) >= 2 and sum(t["chosen"] for t in table) == 1
+    best = min(timed, key=lambda t: t["frame_ms"])
+    info = s.launch_info()
+    assert best["chosen"] == 1 and (info["kernel"], info["patch_verts"], info["block_threads"]) == \
+        (best["kernel"], best["patch_verts"], best["block_threads"])
+    assert not any(t["cached"] for t in table)
+    s.step(2, stats=False)
+    cfg.kernel = pdg.KERNEL_GRAPH
+    g = pdg.Solver(cfg, m, c)
+    g.step(2, stats=False)
+    assert all(np.array_equal(u, w) for u, w in zip(s.get_state(), g.get_state()))
+    cfg.kernel = pdg.KERNEL_AUTOTUNE
+    s2 = pdg.Solver(cfg, m, c)
+    assert all(t["cached"] for t in s2.tune_results())
+    assert s2.launch_info() == info
