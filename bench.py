@@ -44,12 +44,15 @@ WORKLOADS = {
     "plain257": dict(kind="plain", n=257, side=2.0, ks=1e3, kb=1e-2, iters=32, tol=0.0),
     "large1025": dict(kind="plain", n=1025, side=4.0, ks=1e4, kb=1e-2, iters=200, tol=1e-6, wind=1.0),
     "batch512": dict(kind="batch", count=512, iters=200, tol=1e-5),
+    # profiling case of the streaming sweep: 165 MB per sweep (> 129 MB L2)
+    "stream769": dict(kind="plain", n=769, side=3.0, ks=1e4, kb=1e-2, iters=8, tol=0.0, wind=1.0),
 }
 METRICS = {
     "plain257": "vertex-steps/s (plain fused PD, 257x257 cloth, 32 Chebyshev-Jacobi sweeps per frame), 1xGB300",
     "hang33": "vertex-steps/s (plain fused PD, 33x33 cloth, 10 Chebyshev-Jacobi sweeps per frame), 1xGB300",
     "batch512": "vertex-steps/s (batched PD, 512 cloths, to rel. residual 1e-5 cap 200), 1xGB300",
     "large1025": "vertex-steps/s (plain fused PD, 1025x1025 cloth, to rel. residual 1e-6 cap 200), 1xGB300",
+    "stream769": "vertex-steps/s (plain fused PD, 769x769 cloth, 8 Chebyshev-Jacobi sweeps per frame), 1xGB300",
 }
 
 
