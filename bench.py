@@ -258,7 +258,7 @@ def run_ours(args, rank, world, local_rank):
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        kname = {1: "k_iter", 2: "k_persistent", 3: "k_resident"}[info["kernel"]]
+        kname = {1: "k_iter", 2: "k_persistent", 3: "k_resident", 5: "k_stream"}[info["kernel"]]
         traffic = json.load(open(tp)).get(args.workload, {}).get(kname)
 
     if args.quick:   # profiling runs: device-timed region only
@@ -309,11 +309,11 @@ def run_ours(args, rank, world, local_rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "cloths": len(meshes), "vertices": N, "triangles": T, "hinges": E,
                        "sweep_cap": cap, "tolerance": wl["tol"], "rho": 0.99, "h": 1 / 60,
-                       "kernel": {1: "graph", 2: "persistent", 3: "resident"}[info["kernel"]],
+                       "kernel": {1: "graph", 2: "persistent", 3: "resident", 5: "stream"}[info["kernel"]],
                        "patch_verts": info["patch_verts"], "block_threads": info["block_threads"],
                        "patches": info["npatches"], "l2": "flushed before every timed step (512 MB write)",
                        "launch_plan": "autotuned" if args.kernel == 4 else "fixed by --kernel",
-                       "autotune_ms_per_frame": {"%s/%d/%d" % ({1: "graph", 2: "persistent", 3: "resident"}
+                       "autotune_ms_per_frame": {"%s/%d/%d" % ({1: "graph", 2: "persistent", 3: "resident", 5: "stream"}
                                                               [t["kernel"]], t["patch_verts"], t["block_threads"]):
                                                  round(t["frame_ms"], 4) for t in tune if t["frame_ms"] >= 0},
                        "parallelism": "replica per GPU" if world > 1 else "single GPU",
@@ -324,7 +324,8 @@ def run_ours(args, rank, world, local_rank):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": {1: "k_iter (one fused sweep per launch)", 2: "k_persistent (one frame per launch)",
-                                    3: "k_resident (one frame per launch)"}[info["kernel"]],
+                                    3: "k_resident (one frame per launch)",
+                                    5: "k_stream (one fused sweep per launch, bulk-copy prefetch)"}[info["kernel"]],
                          "algorithmic_bytes_per_launch": launch_bytes, "launch_us": launch_ms * 1e3,
                          "bytes_per_sweep_all_cloths": Bs_full, "sweep_us": sweep_ms * 1e3,
                          "note": ("working set %.1f MB per sweep is L2-resident (L2 129 MB), so the fraction of the "

@@ -354,7 +354,7 @@ int pdg_warmstart_adam_step(pdg_warmstart* w, float lr)
 int pdg_warmstart_attach(pdg_warmstart* w, pdg_solver* s)
 {
     if (!w || !s) return set_error(PDG_ERR_ARG, "pdg_warmstart_attach: null argument");
-    if (s->kernel != PDG_KERNEL_GRAPH)
+    if (s->kernel != PDG_KERNEL_GRAPH && s->kernel != PDG_KERNEL_STREAM)
         return set_error(PDG_ERR_STATE, "pdg_warmstart_attach: the solver must use the per-sweep (graph) kernels");
     const HostLayout& Lh = s->L;
     const int N = Lh.ntot;

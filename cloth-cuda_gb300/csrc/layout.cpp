@@ -181,6 +181,11 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                 err = "patch too large for 16-bit local indices; lower patch_verts";
                 return false;
             }
+            // halo, gather pointers and gather entries of every patch start
+            // on a 16-byte boundary, so a patch's lists can be bulk-copied
+            while (L.halo.size() % 4) L.halo.push_back(0);
+            while (L.csr_ptr.size() % 4) L.csr_ptr.push_back(0);
+            while (L.csr_ent.size() % 8) L.csr_ent.push_back(0);
             PatchHdr ph{};
             ph.cloth = ci;
             ph.vbegin = vbase + p0;
@@ -245,6 +250,9 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                     const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
                     if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
                 }
+            ph.nent = cnt[nown];
+            L.max_nent = std::max(L.max_nent, cnt[nown]);
+            L.max_nhalo = std::max(L.max_nhalo, nlocal - nown);
             L.max_nlocal = std::max(L.max_nlocal, nlocal);
             L.max_nslot = std::max(L.max_nslot, nslot);
             L.max_nown = std::max(L.max_nown, nown);
@@ -259,6 +267,9 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
         vbase += N;
     }
     L.npatch = (int)L.patches.size();
+    // a copy rounded up to 16 bytes never reads past the end
+    for (int q = 0; q < 4; ++q) { L.halo.push_back(0); L.csr_ptr.push_back(0); }
+    for (int q = 0; q < 8; ++q) L.csr_ent.push_back(0);
     // neighbour patches: the owners of each patch's halo vertices
     {
         std::vector<int> vpatch(ntot, -1);

@@ -57,4 +57,22 @@ int resident_limits(int* nt, int* mt, int* mh);
 int resident_max_blocks(int mode, size_t smem);
 cudaError_t launch_resident(const PersistArgs& p, int grid, size_t smem, cudaStream_t s);
 
+// Streaming per-sweep kernel (pd_stream.cu): persistent grid, patches
+// double-buffered in shared memory by bulk copies.  Byte offsets of the
+// regions of one stage; the contribution slots follow the two stages.
+struct StreamArgs {
+    int o_tri, o_hin, o_ptr, o_ent, o_hidx, o_y, o_d, o_dp;
+    int stage_bytes;
+    int slot_off;
+    int max_nslot;
+    int npatch;
+    int* err;               // set when a copy wait times out
+    long long spin_budget;  // clock64 cycles a wait may take
+};
+bool stream_layout(int max_ntri, int max_nhinge, int max_nown, int max_nent, int max_nhalo, int max_nlocal,
+                   int max_nslot, StreamArgs& sa, size_t& smem);
+int stream_max_blocks(int mode, int nt, size_t smem);
+cudaError_t launch_stream(const IterArgs& a, const StreamArgs& sa, int mode, int nt, int grid, size_t smem, int k,
+                          int res_only, cudaStream_t s);
+
 }  // namespace pdg

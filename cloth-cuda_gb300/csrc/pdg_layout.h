@@ -25,7 +25,8 @@ struct PatchHdr {            // 64 B
     int csr_off;             // into csr_ptr[] (nown + 1 entries, relative to ent_off)
     int ent_off;             // into csr_ent[]
     int nslot;               // 3*ntri + 4*nhinge contribution slots
-    int pad[4];
+    int nent;                // gather-list entries of the owned vertices
+    int pad[3];
 };
 
 struct TriRec {              // 32 B

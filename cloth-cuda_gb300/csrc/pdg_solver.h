@@ -23,7 +23,7 @@ struct ClothSetup {
 
 struct HostLayout {
     int ntot = 0, ncloth = 0, npatch = 0, cap = 0, omega_stride = 1;
-    int max_nlocal = 0, max_nslot = 0, max_nown = 0, max_ntri = 0, max_nhinge = 0;
+    int max_nlocal = 0, max_nslot = 0, max_nown = 0, max_ntri = 0, max_nhinge = 0, max_nent = 0, max_nhalo = 0;
     size_t smem_bytes = 0;          // per-sweep kernels
     size_t smem_resident = 0;       // resident kernel: + gather lists
     std::vector<int> perm_global;   // reordered vertex -> index in the batch's caller order
@@ -79,7 +79,9 @@ struct pdg_solver {
     int nt = 256;
     int mode = PDG_MODE_CONSISTENT;
     int have_final = 1;
-    int persist_grid = 0;
+    int persist_grid = 0;           // persistent / resident / streaming grid
+    pdg::StreamArgs sargs{};        // streaming kernel: stage layout
+    size_t stream_smem = 0;
     long long launches = 0;
     long long wait_budget = 2000000000LL;   // clock64 cycles per bounded wait (~1 s)
     int kernels_per_frame = 0;

@@ -117,6 +117,16 @@ PersistArgs persist_args(pdg_solver* s)
     return p;
 }
 
+// Sweep k of the per-sweep launch structures.
+cudaError_t launch_sweep(pdg_solver* s, const IterArgs& a, int k, int res_only, cudaStream_t st)
+{
+    if (s->kernel == PDG_KERNEL_STREAM) {
+        s->sargs.spin_budget = s->wait_budget;
+        return launch_stream(a, s->sargs, s->mode, s->nt, s->persist_grid, s->stream_smem, k, res_only, st);
+    }
+    return launch_iter(a, s->mode, s->nt, s->L.npatch, s->L.smem_bytes, k, res_only, st);
+}
+
 // One frame as a sequence of stream-ordered launches.
 int enqueue_frame(pdg_solver* s)
 {
@@ -129,8 +139,8 @@ int enqueue_frame(pdg_solver* s)
         if (rc) return rc;
         CK(launch_warm_select(a, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st));
     }
-    for (int k = 0; k < L.cap; ++k) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st));
-    if (s->have_final) CK(launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st));
+    for (int k = 0; k < L.cap; ++k) CK(launch_sweep(s, a, k, 0, st));
+    if (s->have_final) CK(launch_sweep(s, a, L.cap, 1, st));
     CK(launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st));
     return PDG_OK;
 }
@@ -181,7 +191,8 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     s->patch_verts = c0.patch_verts ? c0.patch_verts : 256;
     if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
     if (c0.kernel == PDG_KERNEL_AUTOTUNE) return autotune_create(n, cfgs, meshes, cons, stream, out);
-    if (c0.kernel < PDG_KERNEL_AUTO || c0.kernel > PDG_KERNEL_RESIDENT) return set_error(PDG_ERR_ARG, "unknown kernel");
+    if (c0.kernel < PDG_KERNEL_AUTO || (c0.kernel > PDG_KERNEL_RESIDENT && c0.kernel != PDG_KERNEL_STREAM))
+        return set_error(PDG_ERR_ARG, "unknown kernel");
     s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_GRAPH : c0.kernel;
     for (const auto& c : s->cloths) s->any_warm = s->any_warm || c.cfg.init == PDG_INIT_WARMSTART;
     if (s->any_warm && (c0.kernel == PDG_KERNEL_PERSISTENT || c0.kernel == PDG_KERNEL_RESIDENT))
@@ -223,7 +234,14 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     }
     for (; s->kernel != PDG_KERNEL_RESIDENT;) {
         if (!build_layout(s->cloths, s->patch_verts, s->L, err)) return set_error(PDG_ERR_ARG, "%s", err.c_str());
-        if (s->L.smem_bytes + 1024 <= (size_t)std::min(smem_optin, 200 * 1024)) break;
+        if (s->kernel == PDG_KERNEL_STREAM) {
+            const HostLayout& L = s->L;
+            stream_layout(L.max_ntri, L.max_nhinge, L.max_nown, L.max_nent, L.max_nhalo, L.max_nlocal, L.max_nslot,
+                          s->sargs, s->stream_smem);
+            if (s->stream_smem + 2048 <= (size_t)smem_optin) break;
+        } else if (s->L.smem_bytes + 1024 <= (size_t)std::min(smem_optin, 200 * 1024)) {
+            break;
+        }
         if (s->patch_verts <= 16) return set_error(PDG_ERR_ARG, "mesh too dense for the shared-memory patch layout");
         s->patch_verts /= 2;
     }
@@ -237,6 +255,16 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     if (rc) return rc;
     s->h_rt.resize(s->L.ncloth);
     s->kernels_per_frame = 4 + s->L.cap + (s->have_final ? 1 : 0);
+    if (s->kernel == PDG_KERNEL_STREAM) {
+        const int maxb = stream_max_blocks(s->mode, s->nt, s->stream_smem);
+        if (maxb <= 0)
+            return set_error(PDG_ERR_CUDA, "streaming kernel cannot be resident with %zu B of shared memory",
+                             s->stream_smem);
+        s->persist_grid = std::min(maxb, s->L.npatch);
+        s->sargs.npatch = s->L.npatch;
+        s->sargs.err = reinterpret_cast<int*>(s->bar.p + 2);
+        s->sargs.spin_budget = s->wait_budget;
+    }
     if (s->kernel == PDG_KERNEL_PERSISTENT) {
         int per_sm = 0;
         const int maxb = persistent_max_blocks(s->mode, s->nt, s->L.smem_bytes, &per_sm);
@@ -339,7 +367,7 @@ int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
     if (stats) {
         CK(cudaMemcpyAsync(s->h_rt.data(), s->crt.p, sizeof(ClothRT) * s->L.ncloth, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
-        if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
+        if (s->kernel != PDG_KERNEL_GRAPH) {   // bounded waits of the one-launch and streaming kernels
             const int rc = take_wait_error(s);
             if (rc) return rc;
         }
@@ -494,10 +522,9 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
                 err = launch_warm_select(a, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st);
             }
             cudaEventRecord(e[1], st);
-            for (int k = 0; k < L.cap && err == cudaSuccess; ++k)
-                err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, k, 0, st);
+            for (int k = 0; k < L.cap && err == cudaSuccess; ++k) err = launch_sweep(s, a, k, 0, st);
             cudaEventRecord(e[2], st);
-            if (err == cudaSuccess && s->have_final) err = launch_iter(a, s->mode, s->nt, L.npatch, L.smem_bytes, L.cap, 1, st);
+            if (err == cudaSuccess && s->have_final) err = launch_sweep(s, a, L.cap, 1, st);
             if (err == cudaSuccess) err = launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "frame launch: %s", cudaGetErrorString(err));
             s->launches += s->kernels_per_frame + ((s->ws && s->any_warm) ? warm_kernel_count() + 4 : 0);
@@ -513,7 +540,7 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
     }
     for (auto& ev : e) cudaEventDestroy(ev);
     if (rc) return rc;
-    if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
+    if (s->kernel != PDG_KERNEL_GRAPH) {
         rc = take_wait_error(s);
         if (rc) return rc;
     }

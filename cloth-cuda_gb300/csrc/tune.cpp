@@ -1,11 +1,13 @@
 // Autotuner of the per-frame launch plan.
 //
 // A launch plan is (launch structure, owned vertices per patch, threads per
-// block): one fused launch per sweep replayed from a CUDA graph, one
-// cooperative launch per frame with a grid barrier after every sweep, or the
-// resident launch that keeps each patch's records on chip and synchronises
-// only with neighbouring patches.  Which is fastest depends on the problem
-// size against the SM count and the shared-memory capacity, so the tuner
+// block): one fused launch per sweep replayed from a CUDA graph (one block
+// per patch, or a persistent grid whose blocks prefetch their next patch
+// with bulk copies), one cooperative launch per frame with a grid barrier
+// after every sweep, or the resident launch that keeps each patch's records
+// on chip and synchronises only with neighbouring patches.  Which is fastest
+// depends on the problem size against the SM count and the shared-memory
+// capacity, so the tuner
 // builds the solver once per candidate plan, runs one untimed frame (graph
 // instantiation, cold caches) and three timed frames from the rest state, and
 // builds the final solver with the fastest plan.  All plans compute the same
@@ -76,7 +78,9 @@ std::vector<Plan> candidates(bool warm)
         c.push_back({PDG_KERNEL_PERSISTENT, 512, 512});
     }
     for (Plan p : {Plan{PDG_KERNEL_GRAPH, 128, 128}, Plan{PDG_KERNEL_GRAPH, 256, 256}, Plan{PDG_KERNEL_GRAPH, 512, 256},
-                   Plan{PDG_KERNEL_GRAPH, 512, 512}, Plan{PDG_KERNEL_GRAPH, 1024, 512}})
+                   Plan{PDG_KERNEL_GRAPH, 512, 512}, Plan{PDG_KERNEL_GRAPH, 1024, 512},
+                   Plan{PDG_KERNEL_STREAM, 64, 128}, Plan{PDG_KERNEL_STREAM, 128, 128}, Plan{PDG_KERNEL_STREAM, 128, 256},
+                   Plan{PDG_KERNEL_STREAM, 256, 256}, Plan{PDG_KERNEL_STREAM, 512, 512}})
         c.push_back(p);
     return c;
 }

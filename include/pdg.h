@@ -53,6 +53,10 @@ extern "C" {
                                     on this problem and keep the fastest;
                                     the choice is cached per device and
                                     problem shape for the process           */
+#define PDG_KERNEL_STREAM     5  /* one launch per iteration (CUDA graph) on a
+                                    persistent grid; each block prefetches its
+                                    next patch with bulk copies (TMA) while it
+                                    solves the current one                   */
 
 /* Solver configuration.  Mirrors PDSolverConfig (include/pd_solver.h:4-15);
  * fields after `damping` extend it. */
@@ -222,7 +226,7 @@ void pdg_solver_destroy(pdg_solver* s);
  * plan.  Every plan computes bitwise the same iterates, so the choice
  * changes the speed only.  The candidate table is kept in the solver. */
 typedef struct pdg_tune_entry {
-    int   kernel;             /* PDG_KERNEL_GRAPH / _PERSISTENT / _RESIDENT   */
+    int   kernel;             /* PDG_KERNEL_GRAPH/_PERSISTENT/_RESIDENT/_STREAM */
     int   patch_verts;        /* owned vertices per patch                     */
     int   block_threads;      /* threads per block                            */
     float frame_ms;           /* mean frame time; < 0: plan does not fit      */

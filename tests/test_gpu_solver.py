@@ -105,14 +105,18 @@ def test_reference_literal_sensitivity_bound(pdg, oracle):
     assert rel(xg, xo) < max(10 * spread, 1e-5)
 
 
-@pytest.mark.parametrize("kernel", ["persistent", "resident"])
+KERNELS = {"persistent": 2, "resident": 3, "stream": 5}
+
+
+@pytest.mark.parametrize("kernel", ["persistent", "resident", "stream"])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_launch_structures_agree_bitwise(pdg, oracle, kernel, mode):
-    # one launch per sweep (CUDA graph), one cooperative launch per frame, and
-    # the resident kernel run the same per-vertex arithmetic in the same order
+    # one launch per sweep (CUDA graph), one cooperative launch per frame, the
+    # resident kernel and the streaming kernel run the same per-vertex
+    # arithmetic in the same order
     m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=16, mode=mode, kernel=pdg.KERNEL_GRAPH)
     s1 = pdg.Solver(cfg, m, c)
-    cfg.kernel = pdg.KERNEL_PERSISTENT if kernel == "persistent" else pdg.KERNEL_RESIDENT
+    cfg.kernel = KERNELS[kernel]
     s2 = pdg.Solver(cfg, m, c)
     assert s1.launch_info()["kernel"] == pdg.KERNEL_GRAPH
     assert s2.launch_info()["kernel"] == cfg.kernel
@@ -268,14 +272,14 @@ def test_zero_iterations(pdg, oracle):
     assert np.allclose(x, y, atol=1e-7) and st["iterations"] == 0
 
 
-@pytest.mark.parametrize("kernel", ["persistent", "resident"])
+@pytest.mark.parametrize("kernel", ["persistent", "resident", "stream"])
 def test_bounded_waits_run_out_cleanly(pdg, oracle, kernel):
     # failure detection without a GPU fault: a wait budget of one cycle makes
     # every grid-barrier / neighbour wait run out; the kernel records the
     # error, all blocks leave, the host reads PDG_ERR_TIMEOUT, and the next
     # frame with a normal budget runs on the same context
     m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=8)
-    cfg.kernel = pdg.KERNEL_PERSISTENT if kernel == "persistent" else pdg.KERNEL_RESIDENT
+    cfg.kernel = KERNELS[kernel]
     s = pdg.Solver(cfg, m, c)
     s.set_wait_budget(1)
     with pytest.raises(pdg.PDGError) as e:
@@ -315,3 +319,33 @@ def test_autotuner_picks_a_plan_and_keeps_the_bits(pdg, oracle):
     s2 = pdg.Solver(cfg, m, c)
     assert all(t["cached"] for t in s2.tune_results())
     assert s2.launch_info() == info
+
+
+def test_stream_kernel_walks_many_patches_per_block(pdg, oracle):
+    # 513x513 cloth in 64-vertex patches: several thousand patches over at
+    # most a few blocks per SM, so every block double-buffers several patches
+    m, c, cfg, sc, a = scene(pdg, oracle, n=513, side=2.0, max_iterations=8, kernel=pdg.KERNEL_GRAPH,
+                             patch_verts=64, block_threads=128)
+    g = pdg.Solver(cfg, m, c)
+    cfg.kernel = pdg.KERNEL_STREAM
+    s = pdg.Solver(cfg, m, c)
+    info = s.launch_info()
+    assert info["kernel"] == pdg.KERNEL_STREAM and info["npatches"] > 3 * 152
+    stg = g.step(2); sts = s.step(2)
+    assert all(np.array_equal(u, w) for u, w in zip(g.get_state(), s.get_state()))
+    assert abs(stg[0]["res_final"] - sts[0]["res_final"]) <= 1e-5 * stg[0]["res_final"]
+
+
+def test_stream_kernel_tolerance_batch(pdg, oracle):
+    scenes = [scene(pdg, oracle, n=n, seed=n, side=0.5, ks=20.0, kb=1e-3, rho=0.9, max_iterations=400,
+                    tolerance=1e-4) for n in (9, 10, 11, 40)]
+    outs = []
+    for kern in (pdg.KERNEL_GRAPH, pdg.KERNEL_STREAM):
+        for sc_ in scenes:
+            sc_[2].kernel = kern
+        b = pdg.Solver([sc_[2] for sc_ in scenes], [sc_[0] for sc_ in scenes], [sc_[1] for sc_ in scenes])
+        assert b.launch_info()["kernel"] == kern
+        st = b.step(2)
+        outs.append((b.get_state_all(), [s_["iterations"] for s_ in st]))
+    assert np.array_equal(outs[0][0][0], outs[1][0][0]) and np.array_equal(outs[0][0][1], outs[1][0][1])
+    assert outs[0][1] == outs[1][1]
