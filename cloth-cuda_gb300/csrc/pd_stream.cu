@@ -53,13 +53,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return done != 0;
 }
 
-// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait for the phase with the given parity to complete: one
+// non-blocking probe, then try_wait (which may suspend the thread for a
+// while in hardware) until the clock64 budget is spent.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long budget)
 {
+    if (mbar_test_wait(bar, parity)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
+    for (;;) {
         if (clock64() - t0 > budget) return false;
-    return true;
+        if (mbar_try_wait(bar, parity)) return true;
+    }
 }
 
 // Order this thread's earlier generic-proxy accesses of shared memory before

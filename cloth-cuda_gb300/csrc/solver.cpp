@@ -555,6 +555,8 @@ int pdg_solver_set_wait_budget(pdg_solver* s, long long cycles)
 {
     if (!s || cycles < 0) return set_error(PDG_ERR_ARG, "pdg_solver_set_wait_budget: bad arguments");
     s->wait_budget = cycles;
+    // the streaming kernel's budget is a launch argument inside the graph
+    if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
     return PDG_OK;
 }
 

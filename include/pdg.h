@@ -203,8 +203,9 @@ int  pdg_solver_launch_count(const pdg_solver* s, long long* n);
  * average frame; sweep_ms: average duration of one fused sweep (the events
  * bracket the sweep launches; persistent kernel: frame time / sweeps). */
 int  pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* sweep_ms);
-/* Wait budget (GPU clock cycles) of every grid-barrier / neighbour wait in
- * the persistent and resident kernels (default 2e9, about 1 s).  When a wait
+/* Wait budget (GPU clock cycles) of every grid-barrier / neighbour / copy
+ * wait in the persistent, resident and streaming kernels (default 2e9,
+ * about 1 s).  When a wait
  * runs out the kernel records an error and every block leaves at its next
  * wait.  The error stays recorded (later frames of the same call leave at
  * their first barrier) until pdg_solver_step with stats or
