@@ -77,10 +77,14 @@ std::vector<Plan> candidates(bool warm)
         c.push_back({PDG_KERNEL_PERSISTENT, 256, 256});
         c.push_back({PDG_KERNEL_PERSISTENT, 512, 512});
     }
-    for (Plan p : {Plan{PDG_KERNEL_GRAPH, 128, 128}, Plan{PDG_KERNEL_GRAPH, 256, 256}, Plan{PDG_KERNEL_GRAPH, 512, 256},
-                   Plan{PDG_KERNEL_GRAPH, 512, 512}, Plan{PDG_KERNEL_GRAPH, 1024, 512},
-                   Plan{PDG_KERNEL_STREAM, 64, 128}, Plan{PDG_KERNEL_STREAM, 128, 128}, Plan{PDG_KERNEL_STREAM, 128, 256},
-                   Plan{PDG_KERNEL_STREAM, 256, 256}, Plan{PDG_KERNEL_STREAM, 512, 512}})
+    // per-sweep plans: patch sizes from 64 to 1024 vertices at 1-4 threads
+    // per owned vertex (more threads hide more of the latency of the local
+    // step's dependent arithmetic)
+    for (Plan p : {Plan{PDG_KERNEL_GRAPH, 64, 128}, Plan{PDG_KERNEL_GRAPH, 128, 128}, Plan{PDG_KERNEL_GRAPH, 128, 256},
+                   Plan{PDG_KERNEL_GRAPH, 256, 256}, Plan{PDG_KERNEL_GRAPH, 256, 512}, Plan{PDG_KERNEL_GRAPH, 512, 512},
+                   Plan{PDG_KERNEL_GRAPH, 1024, 512}, Plan{PDG_KERNEL_STREAM, 64, 128},
+                   Plan{PDG_KERNEL_STREAM, 128, 256}, Plan{PDG_KERNEL_STREAM, 256, 256},
+                   Plan{PDG_KERNEL_STREAM, 256, 512}})
         c.push_back(p);
     return c;
 }
