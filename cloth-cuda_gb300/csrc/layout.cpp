@@ -162,6 +162,16 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             }
             std::sort(ltri.begin(), ltri.end());
             std::sort(lhin.begin(), lhin.end());
+            // records whose corners are all owned first: a kernel that runs
+            // them before the halo arrives then splits on warp boundaries
+            auto owned = [&](int o) { const int n = iperm[o]; return n >= p0 && n < p1; };
+            std::stable_partition(ltri.begin(), ltri.end(), [&](int t) {
+                return owned(m.tris[3 * t]) && owned(m.tris[3 * t + 1]) && owned(m.tris[3 * t + 2]);
+            });
+            std::stable_partition(lhin.begin(), lhin.end(), [&](int e) {
+                return owned(cd.quads[4 * e]) && owned(cd.quads[4 * e + 1]) && owned(cd.quads[4 * e + 2]) &&
+                       owned(cd.quads[4 * e + 3]);
+            });
             auto touch = [&](int o) {
                 const int n = iperm[o];
                 if (n >= p0 && n < p1) return;
