@@ -231,7 +231,14 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                 L.hinges.push_back(r);
             }
             // gather lists: owned vertex l sums the slots of its corners in
-            // triangle order, then hinge order
+            // global triangle order, then global hinge order -- independent
+            // of where the records sit in the patch, so every patch size and
+            // launch structure adds in the same order
+            std::vector<int> ot(ntri), oh(nhin);
+            for (int q = 0; q < ntri; ++q) ot[q] = q;
+            for (int q = 0; q < nhin; ++q) oh[q] = q;
+            std::sort(ot.begin(), ot.end(), [&](int u, int w) { return ltri[u] < ltri[w]; });
+            std::sort(oh.begin(), oh.end(), [&](int u, int w) { return lhin[u] < lhin[w]; });
             cnt.assign(nown + 1, 0);
             for (int lt = 0; lt < ntri; ++lt)
                 for (int a = 0; a < 3; ++a) {
@@ -250,12 +257,12 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             std::vector<int> fill(cnt.begin(), cnt.end() - 1);
             // slots are corner-major: triangle corner a at a*ntri + lt, hinge
             // slot a at 3*ntri + a*nhin + lh
-            for (int lt = 0; lt < ntri; ++lt)
+            for (int lt : ot)
                 for (int a = 0; a < 3; ++a) {
                     const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
                     if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(a * ntri + lt);
                 }
-            for (int lh = 0; lh < nhin; ++lh)
+            for (int lh : oh)
                 for (int a = 0; a < 4; ++a) {
                     const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
                     if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
