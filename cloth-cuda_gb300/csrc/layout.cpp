@@ -162,16 +162,6 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             }
             std::sort(ltri.begin(), ltri.end());
             std::sort(lhin.begin(), lhin.end());
-            // records whose corners are all owned first: a kernel that runs
-            // them before the halo arrives then splits on warp boundaries
-            auto owned = [&](int o) { const int n = iperm[o]; return n >= p0 && n < p1; };
-            std::stable_partition(ltri.begin(), ltri.end(), [&](int t) {
-                return owned(m.tris[3 * t]) && owned(m.tris[3 * t + 1]) && owned(m.tris[3 * t + 2]);
-            });
-            std::stable_partition(lhin.begin(), lhin.end(), [&](int e) {
-                return owned(cd.quads[4 * e]) && owned(cd.quads[4 * e + 1]) && owned(cd.quads[4 * e + 2]) &&
-                       owned(cd.quads[4 * e + 3]);
-            });
             auto touch = [&](int o) {
                 const int n = iperm[o];
                 if (n >= p0 && n < p1) return;
@@ -184,6 +174,23 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             std::sort(halo.begin(), halo.end());
             for (int l = 0; l < nown; ++l) vloc[p0 + l] = l;
             for (size_t q = 0; q < halo.size(); ++q) vloc[halo[q]] = nown + (int)q;
+            // record placement follows the Morton order of the lowest local
+            // corner, so the lanes of a warp touch neighbouring vertices and
+            // neighbouring slots (fewer shared-memory bank conflicts); the
+            // summation order is fixed separately below
+            {
+                auto lo_t = [&](int t) {
+                    return std::min(vloc[iperm[m.tris[3 * t]]],
+                                    std::min(vloc[iperm[m.tris[3 * t + 1]]], vloc[iperm[m.tris[3 * t + 2]]]));
+                };
+                auto lo_h = [&](int e) {
+                    int lo = vloc[iperm[cd.quads[4 * e]]];
+                    for (int a = 1; a < 4; ++a) lo = std::min(lo, vloc[iperm[cd.quads[4 * e + a]]]);
+                    return lo;
+                };
+                std::stable_sort(ltri.begin(), ltri.end(), [&](int u, int w) { return lo_t(u) < lo_t(w); });
+                std::stable_sort(lhin.begin(), lhin.end(), [&](int u, int w) { return lo_h(u) < lo_h(w); });
+            }
             const int nlocal = nown + (int)halo.size();
             const int ntri = (int)ltri.size(), nhin = (int)lhin.size();
             const int nslot = 3 * ntri + 4 * nhin;

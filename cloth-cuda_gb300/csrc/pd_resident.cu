@@ -122,25 +122,6 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
         const int e = tid + j * NT;
         if (e < nhin) rh[j] = a.hinges[ph.hinge_off + e];
     }
-    // records touching a halo vertex (bit j: triangle j, bit MT + j: hinge j)
-    unsigned halo_mask = 0;
-    #pragma unroll
-    for (int j = 0; j < MT; ++j) {
-        const int t = tri_index<NT, MT>(tid, j);
-        if (t < ntri) {
-            const int hi = max(max((int)(rt[j].l01 & 0xffffu), (int)(rt[j].l01 >> 16)), (int)rt[j].l2);
-            if (hi >= nown) halo_mask |= 1u << j;
-        }
-    }
-    #pragma unroll
-    for (int j = 0; j < MH; ++j) {
-        const int e = tid + j * NT;
-        if (e < nhin) {
-            const int hi = max(max((int)(rh[j].l01 & 0xffffu), (int)(rh[j].l01 >> 16)),
-                               max((int)(rh[j].l23 & 0xffffu), (int)(rh[j].l23 >> 16)));
-            if (hi >= nown) halo_mask |= 1u << (MT + j);
-        }
-    }
     // gather lists in shared memory
     for (int l = tid; l <= nown; l += NT) sptr[l] = a.csr_ptr[ph.csr_off + l];
     __syncthreads();
@@ -178,40 +159,24 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
             skip = cloth_done(a, c, k, first, !nbr) ? 1 : 0;
             omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
         }
+        if (k > 0) {   // halo offsets d^k written by the neighbouring blocks
+            if (nbr && !wait_neighbours(nb, nnb, p.pflag, mark0 + k, p.err, p.spin_budget)) return;
+            const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
+            for (int l = nown + tid; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
+        }
         __syncthreads();
-        // With neighbour synchronisation the records that touch owned
-        // vertices only run (pass 0) before the wait for the neighbours' d^k,
-        // so the exchange overlaps them; the others run (pass 1) once the
-        // halo is in.  Without it every record runs in pass 1.
-        const bool split = nbr && k > 0;
-        const unsigned sel = split ? 1u : 0u;
-        for (int pass = split ? 0 : 1; pass < 2; ++pass) {
-            if (pass == 1) {
-                if (k > 0) {   // halo offsets d^k written by the neighbouring blocks
-                    if (nbr && !wait_neighbours(nb, nnb, p.pflag, mark0 + k, p.err, p.spin_budget)) return;
-                    const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
-                    for (int l = nown + tid; l < nlocal; l += NT)
-                        sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
-                }
-                __syncthreads();
-            }
-            if (skip) continue;
-            const unsigned want = (split && pass == 1) ? 1u : 0u;
+        const bool res_only = k >= ci.max_iter;
+        if (!skip) {
             #pragma unroll
             for (int j = 0; j < MT; ++j) {
                 const int t = tri_index<NT, MT>(tid, j);
-                if (t < ntri && ((halo_mask >> j) & sel) == want)
-                    triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
+                if (t < ntri) triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
             }
             #pragma unroll
             for (int j = 0; j < MH; ++j) {
                 const int e = tid + j * NT;
-                if (e < nhin && ((halo_mask >> (MT + j)) & sel) == want)
-                    hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
+                if (e < nhin) hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
             }
-        }
-        const bool res_only = k >= ci.max_iter;
-        if (!skip) {
             __syncthreads();
             float r2 = 0.f;
             if (own) {
