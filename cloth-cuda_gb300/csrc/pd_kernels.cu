@@ -26,20 +26,21 @@ __global__ void __launch_bounds__(NT) k_iter(IterArgs a, int k, int res_only)
     __shared__ float red[NT / 32];
     __shared__ int skip;
     __shared__ float omega;
+    if (threadIdx.x == 0) ph = a.patches[blockIdx.x];
+    __syncthreads();
+    // thread 0 takes the per-cloth decision while the others stage the patch
     if (threadIdx.x == 0) {
-        ph = a.patches[blockIdx.x];
         const int c = ph.cloth;
         const ClothInfo& ci = a.cinfo[c];
         skip = cloth_done(a, c, k, (int)blockIdx.x == ci.patch_begin) ? 1 : 0;
         omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
     }
-    __syncthreads();
-    if (skip) return;
     float4* sx = smem;
     float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
     float* cy = cx + ph.nslot;
     float* cz = cy + ph.nslot;
-    process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, omega, sx, cx, cy, cz, red);
+    process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, 1.f, sx, cx, cy, cz, red,
+                            &skip, &omega);
 }
 
 // Residual of the offsets D (no update) into acc[cloth][slot]: one block per patch.

@@ -291,7 +291,8 @@ __device__ __forceinline__ void block_residual(float r2, float* red, double* acc
 template <int MODE, int NT>
 __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr& ph, int k, bool res_only,
                                               float omega, float4* sy, float* cx, float* cy, float* cz,
-                                              float* red)
+                                              float* red, const int* skip_s = nullptr,
+                                              const float* omega_s = nullptr)
 {
     // select, not index: a dynamic index into the parameter struct would
     // copy it to local memory
@@ -307,6 +308,9 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
         sd[l] = __ldcg(&Dk[g]);
     }
     __syncthreads();
+    // a skip decision and weight taken by thread 0 while the block staged
+    if (skip_s && *(const volatile int*)skip_s) return;
+    if (omega_s) omega = *(const volatile float*)omega_s;
 
     // 2. local step: triangles then hinges, contributions to shared slots
     const TriRec* __restrict__ tr = a.tris + ph.tri_off;

@@ -45,19 +45,29 @@ __device__ __forceinline__ bool grid_barrier_r(unsigned* bar, int* err, long lon
     return ok != 0;
 }
 
+__device__ __forceinline__ void st_release_gpu(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
 // Publish "this patch finished the sweep with mark m" after all of the
-// block's global writes.
+// block's global writes (the barrier orders them before thread 0's release).
 __device__ __forceinline__ void publish_mark(unsigned long long* pflag, unsigned long long m)
 {
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        *(volatile unsigned long long*)&pflag[blockIdx.x] = m;
-    }
+    if (threadIdx.x == 0) st_release_gpu(&pflag[blockIdx.x], m);
 }
 
 // Wait until every neighbouring patch published a mark >= m (first warp, one
-// lane per neighbour), bounded.  Returns false on timeout or a prior error.
+// lane per neighbour, acquire loads), bounded.  Returns false on timeout or a
+// prior error.
 __device__ __forceinline__ bool wait_neighbours(const int* nb, int nnb, const unsigned long long* pflag,
                                                 unsigned long long m, int* err, long long budget)
 {
@@ -65,14 +75,13 @@ __device__ __forceinline__ bool wait_neighbours(const int* nb, int nnb, const un
     if (threadIdx.x < 32) {
         bool good = true;
         for (int j = threadIdx.x; j < nnb && good; j += 32) {
-            const volatile unsigned long long* f = pflag + nb[j];
+            const unsigned long long* f = pflag + nb[j];
             const long long t0 = clock64();
-            while (*f < m) {
+            while (ld_acquire_gpu(f) < m) {
                 if (clock64() - t0 > budget || *(volatile int*)err != 0) { atomicCAS(err, 0, 3); good = false; break; }
                 __nanosleep(20);
             }
         }
-        __threadfence();
         const unsigned all = __ballot_sync(0xffffffffu, good);
         if (threadIdx.x == 0) ok = (all == 0xffffffffu);
     }
@@ -86,6 +95,8 @@ __device__ __forceinline__ int tri_index(int tid, int j)
     return j < MT - 1 ? tid + j * NT : (MT - 1) * NT + (NT - 1 - tid);
 }
 
+constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
+
 template <int MODE, int NT, int MT, int MH>
 __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
 {
@@ -93,7 +104,7 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
     __shared__ PatchHdr ph;
     __shared__ float red[NT / 32];
     __shared__ int skip;
-    __shared__ float omega;
+    __shared__ float som[kResOmega];   // Chebyshev weights of this cloth
     const IterArgs& a = p.it;
     const int tid = threadIdx.x;
     if (tid == 0) ph = a.patches[blockIdx.x];
@@ -122,8 +133,9 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
         const int e = tid + j * NT;
         if (e < nhin) rh[j] = a.hinges[ph.hinge_off + e];
     }
-    // gather lists in shared memory
+    // gather lists and Chebyshev weights in shared memory
     for (int l = tid; l <= nown; l += NT) sptr[l] = a.csr_ptr[ph.csr_off + l];
+    for (int k = tid; k < a.omega_stride && k < kResOmega; k += NT) som[k] = a.omega[ph.cloth * a.omega_stride + k];
     __syncthreads();
     const int nent = sptr[nown];
     for (int q = tid; q < nent; q += NT) sent[q] = a.csr_ent[ph.ent_off + q];
@@ -146,6 +158,9 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
         sy[l] = __ldcg(&a.Y[gg]);
         sd[l] = __ldcg(&a.buf[0][gg]);
     }
+    // this thread's first halo vertex, re-read every sweep
+    const int hl0 = nown + tid;
+    const int hg0 = hl0 < nlocal ? __ldg(&a.halo[ph.halo_off + tid]) : 0;
 
     const float gamma = ci.gamma;
     const int nsweep = p.max_iter + (p.have_final ? 1 : 0);
@@ -155,18 +170,21 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
     const int nnb = p.nbr_ptr[blockIdx.x + 1] - p.nbr_ptr[blockIdx.x];
     double* acc = a.acc + (size_t)c * a.acc_stride;
     for (int k = 0; k < nsweep; ++k) {
-        if (tid == 0) {
-            skip = cloth_done(a, c, k, first, !nbr) ? 1 : 0;
-            omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
-        }
+        // With fixed sweep counts the cap alone decides (the record stays
+        // active through the sweeps), so no thread waits on global memory
+        // for it; a tolerance needs the per-cloth decision.
+        if (!nbr && tid == 0) skip = cloth_done(a, c, k, first, true) ? 1 : 0;
         if (k > 0) {   // halo offsets d^k written by the neighbouring blocks
             if (nbr && !wait_neighbours(nb, nnb, p.pflag, mark0 + k, p.err, p.spin_budget)) return;
             const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
-            for (int l = nown + tid; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
+            if (hl0 < nlocal) sd[hl0] = __ldcg(&Dk[hg0]);
+            for (int l = hl0 + NT; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
         }
         __syncthreads();
+        const bool skip_k = nbr ? (k >= ci.max_iter && (k > ci.max_iter || !a.have_final)) : skip != 0;
+        const float omega_k = k < a.omega_stride ? (k < kResOmega ? som[k] : a.omega[c * a.omega_stride + k]) : 1.f;
         const bool res_only = k >= ci.max_iter;
-        if (!skip) {
+        if (!skip_k) {
             #pragma unroll
             for (int j = 0; j < MT; ++j) {
                 const int t = tri_index<NT, MT>(tid, j);
@@ -184,7 +202,7 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
                 const float4 d = sd[tid];
                 const float4 y = sy[tid];
                 float4 o;
-                if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega, r2);
+                if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega_k, r2);
                 else                         o = update_literal(d, y, f);
                 if (!res_only) {
                     ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;

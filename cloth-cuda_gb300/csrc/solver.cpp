@@ -215,7 +215,7 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
         bool ok = P <= rnt && build_layout(s->cloths, P, s->L, err);
         if (ok) {
             ok = s->L.max_nown <= rnt && s->L.max_ntri <= rmt * rnt && s->L.max_nhinge <= rmh * rnt &&
-                 s->L.smem_resident <= (size_t)std::min(smem_optin - 2048, 220 * 1024);
+                 s->L.smem_resident <= (size_t)std::min(smem_optin - 8192, 216 * 1024);
             if (ok) ok = s->L.npatch <= resident_max_blocks(s->mode, s->L.smem_resident);
         }
         if (ok) {
