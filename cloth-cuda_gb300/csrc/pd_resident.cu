@@ -98,7 +98,7 @@ __device__ __forceinline__ int tri_index(int tid, int j)
 constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 
 template <int MODE, int NT, int MT, int MH>
-__global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
+__global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
 {
     extern __shared__ float4 smem[];
     __shared__ PatchHdr ph;
@@ -225,40 +225,49 @@ __global__ void __launch_bounds__(NT, 1) k_resident(PersistArgs p)
     if (own) finalize_vertex(g, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
 }
 
-// MT x NT triangles and MH x NT hinges per block
-#define PDG_RES_NT 512
+// MT x NT triangles and MH x NT hinges per block.  512 threads: one block
+// (one patch) per SM; 256 threads: two half-size patches per SM, so one
+// block computes while the other waits for its neighbours.
 #define PDG_RES_MT 3
 #define PDG_RES_MH 4
 
-int resident_limits(int* nt, int* mt, int* mh)
+int resident_limits(int nt, int* mt, int* mh)
 {
-    *nt = PDG_RES_NT; *mt = PDG_RES_MT; *mh = PDG_RES_MH;
+    if (nt != 256 && nt != 512) return -1;
+    *mt = PDG_RES_MT; *mh = PDG_RES_MH;
     return 0;
 }
 
-static void* pick_resident(int mode)
+static void* pick_resident(int mode, int nt)
 {
-    return mode == kModeConsistent ? (void*)k_resident<kModeConsistent, PDG_RES_NT, PDG_RES_MT, PDG_RES_MH>
-                                   : (void*)k_resident<kModeLiteral, PDG_RES_NT, PDG_RES_MT, PDG_RES_MH>;
+    if (nt == 256)
+        return mode == kModeConsistent ? (void*)k_resident<kModeConsistent, 256, PDG_RES_MT, PDG_RES_MH>
+                                       : (void*)k_resident<kModeLiteral, 256, PDG_RES_MT, PDG_RES_MH>;
+    if (nt == 512)
+        return mode == kModeConsistent ? (void*)k_resident<kModeConsistent, 512, PDG_RES_MT, PDG_RES_MH>
+                                       : (void*)k_resident<kModeLiteral, 512, PDG_RES_MT, PDG_RES_MH>;
+    return nullptr;
 }
 
-int resident_max_blocks(int mode, size_t smem)
+int resident_max_blocks(int mode, int nt, size_t smem)
 {
-    void* f = pick_resident(mode);
+    void* f = pick_resident(mode, nt);
+    if (!f) return 0;
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess) return 0;
     int dev = 0, nsm = 0, nb = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, PDG_RES_NT, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, nt, smem) != cudaSuccess) return 0;
     return nb * nsm;
 }
 
-cudaError_t launch_resident(const PersistArgs& p, int grid, size_t smem, cudaStream_t s)
+cudaError_t launch_resident(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s)
 {
-    void* f = pick_resident(p.mode);
+    void* f = pick_resident(p.mode, nt);
+    if (!f || grid <= 0) return cudaErrorInvalidValue;
     PersistArgs copy = p;
     void* args[] = {&copy};
-    return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(PDG_RES_NT), args, smem, s);
+    return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(nt), args, smem, s);
 }
 
 }  // namespace pdg

@@ -52,10 +52,11 @@ cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t sme
 int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
 
 // Resident persistent kernel (pd_resident.cu): one patch per block, records
-// in registers.  Limits: nown <= nt, ntri <= mt*nt, nhinge <= mh*nt.
-int resident_limits(int* nt, int* mt, int* mh);
-int resident_max_blocks(int mode, size_t smem);
-cudaError_t launch_resident(const PersistArgs& p, int grid, size_t smem, cudaStream_t s);
+// in registers, nt = 512 (one block per SM) or 256 (two).  Limits:
+// nown <= nt, ntri <= mt*nt, nhinge <= mh*nt.
+int resident_limits(int nt, int* mt, int* mh);
+int resident_max_blocks(int mode, int nt, size_t smem);
+cudaError_t launch_resident(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s);
 
 // Streaming per-sweep kernel (pd_stream.cu): persistent grid, patches
 // double-buffered in shared memory by bulk copies.  Byte offsets of the

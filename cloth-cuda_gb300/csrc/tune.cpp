@@ -74,6 +74,7 @@ std::vector<Plan> candidates(bool warm)
     std::vector<Plan> c;
     if (!warm) {
         c.push_back({PDG_KERNEL_RESIDENT, 0, 0});
+        c.push_back({PDG_KERNEL_RESIDENT, 0, 256});
         c.push_back({PDG_KERNEL_PERSISTENT, 256, 256});
         c.push_back({PDG_KERNEL_PERSISTENT, 512, 512});
     }

@@ -108,7 +108,7 @@ def test_reference_literal_sensitivity_bound(pdg, oracle):
 KERNELS = {"persistent": 2, "resident": 3, "stream": 5}
 
 
-@pytest.mark.parametrize("kernel", ["persistent", "resident", "stream"])
+@pytest.mark.parametrize("kernel", ["persistent", "resident", "resident256", "stream"])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_launch_structures_agree_bitwise(pdg, oracle, kernel, mode):
     # one launch per sweep (CUDA graph), one cooperative launch per frame, the
@@ -116,8 +116,12 @@ def test_launch_structures_agree_bitwise(pdg, oracle, kernel, mode):
     # arithmetic in the same order
     m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=16, mode=mode, kernel=pdg.KERNEL_GRAPH)
     s1 = pdg.Solver(cfg, m, c)
-    cfg.kernel = KERNELS[kernel]
+    cfg.kernel = KERNELS[kernel.replace("256", "")]
+    if kernel == "resident256":   # two blocks per SM
+        cfg.block_threads = 256
     s2 = pdg.Solver(cfg, m, c)
+    if kernel == "resident256":
+        assert s2.launch_info()["block_threads"] == 256
     assert s1.launch_info()["kernel"] == pdg.KERNEL_GRAPH
     assert s2.launch_info()["kernel"] == cfg.kernel
     for _ in range(3):
