@@ -80,6 +80,26 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
         std::vector<int> perm, iperm(N);
         morton_order(m, perm);
         for (int i = 0; i < N; ++i) iperm[perm[i]] = i;
+        // A vertex is "boundary" when a triangle or hinge through it has a
+        // corner in another patch (it is then in that patch's halo).  Within
+        // each patch the boundary vertices go first, so a kernel can finish
+        // and publish them before the interior.
+        std::vector<char> bnd(N, 0);
+        {
+            auto mark = [&](const int* v, int n) {
+                const int p = iperm[v[0]] / patch_verts;
+                bool span = false;
+                for (int a = 1; a < n; ++a) span = span || iperm[v[a]] / patch_verts != p;
+                if (span)
+                    for (int a = 0; a < n; ++a) bnd[v[a]] = 1;
+            };
+            for (int t = 0; t < T; ++t) mark(&m.tris[3 * t], 3);
+            for (int e = 0; e < E; ++e) mark(&cd.quads[4 * e], 4);
+            for (int p0 = 0; p0 < N; p0 += patch_verts)
+                std::stable_partition(perm.begin() + p0, perm.begin() + std::min(N, p0 + patch_verts),
+                                      [&](int o) { return bnd[o] != 0; });
+            for (int i = 0; i < N; ++i) iperm[perm[i]] = i;
+        }
 
         std::vector<float> diag;
         jacobi_diag(m, cd, cfg.dt, diag);
@@ -149,6 +169,7 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             const int nown = p1 - p0;
             const int stamp = (int)L.patches.size();
             ltri.clear(); lhin.clear(); halo.clear();
+            int nbnd_p = 0, ntri_a = 0, nhin_a = 0;
             for (int l = 0; l < nown; ++l) {
                 const int o = perm[p0 + l];
                 for (int q = tp.vt_ptr[o]; q < tp.vt_ptr[o + 1]; ++q) {
@@ -190,6 +211,14 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                 };
                 std::stable_sort(ltri.begin(), ltri.end(), [&](int u, int w) { return lo_t(u) < lo_t(w); });
                 std::stable_sort(lhin.begin(), lhin.end(), [&](int u, int w) { return lo_h(u) < lo_h(w); });
+                // boundary vertices are local 0..nbnd-1; the records through
+                // one of them are a prefix of each list
+                nbnd_p = 0;
+                while (nbnd_p < nown && bnd[perm[p0 + nbnd_p]]) ++nbnd_p;
+                ntri_a = 0;
+                while (ntri_a < (int)ltri.size() && lo_t(ltri[ntri_a]) < nbnd_p) ++ntri_a;
+                nhin_a = 0;
+                while (nhin_a < (int)lhin.size() && lo_h(lhin[nhin_a]) < nbnd_p) ++nhin_a;
             }
             const int nlocal = nown + (int)halo.size();
             const int ntri = (int)ltri.size(), nhin = (int)lhin.size();
@@ -275,6 +304,9 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                     if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
                 }
             ph.nent = cnt[nown];
+            ph.nbnd = nbnd_p;
+            ph.ntri_a = ntri_a;
+            ph.nhin_a = nhin_a;
             L.max_nent = std::max(L.max_nent, cnt[nown]);
             L.max_nhalo = std::max(L.max_nhalo, nlocal - nown);
             L.max_nlocal = std::max(L.max_nlocal, nlocal);

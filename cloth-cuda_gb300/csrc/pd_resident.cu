@@ -97,6 +97,39 @@ __device__ __forceinline__ int tri_index(int tid, int j)
 
 constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 
+// Local step over this thread's records with list index in [t0, t1) (triangles)
+// and [e0, e1) (hinges).
+template <int MODE, int NT, int MT, int MH>
+__device__ __forceinline__ void local_records(const TriRec (&rt)[MT], const HingeRec (&rh)[MH], const float4* sy,
+                                              const float4* sd, int ntri, int nhin, int t0, int t1, int e0, int e1,
+                                              float* cx, float* cy, float* cz)
+{
+    const int tid = threadIdx.x;
+    #pragma unroll
+    for (int j = 0; j < MT; ++j) {
+        const int t = tri_index<NT, MT>(tid, j);
+        if (t >= t0 && t < t1) triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
+    }
+    #pragma unroll
+    for (int j = 0; j < MH; ++j) {
+        const int e = tid + j * NT;
+        if (e >= e0 && e < e1) hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
+    }
+}
+
+// Gather and Jacobi update of owned vertex l: o = d^(k+1), d = d^k.
+template <int MODE>
+__device__ __forceinline__ void vertex_update(const uint16_t* sent, const int* sptr, int l, const float4* sy,
+                                              const float4* sd, const float* cx, const float* cy, const float* cz,
+                                              float4 dprev, float gamma, float omega, float4& o, float4& d, float& r2)
+{
+    const float3 f = gather_slots(sent, sptr[l], sptr[l + 1], cx, cy, cz);
+    d = sd[l];
+    const float4 y = sy[l];
+    if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega, r2);
+    else                         o = update_literal(d, y, f);
+}
+
 template <int MODE, int NT, int MT, int MH>
 __global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
 {
@@ -184,39 +217,41 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
         const bool skip_k = nbr ? (k >= ci.max_iter && (k > ci.max_iter || !a.have_final)) : skip != 0;
         const float omega_k = k < a.omega_stride ? (k < kResOmega ? som[k] : a.omega[c * a.omega_stride + k]) : 1.f;
         const bool res_only = k >= ci.max_iter;
+        // Phase A: the records through boundary vertices (a prefix of each
+        // list), then the update of the boundary vertices, which the
+        // neighbouring patches read: they are published before phase B, so
+        // the exchange overlaps the interior's work.
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+        float r2 = 0.f;
         if (!skip_k) {
-            #pragma unroll
-            for (int j = 0; j < MT; ++j) {
-                const int t = tri_index<NT, MT>(tid, j);
-                if (t < ntri) triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
-            }
-            #pragma unroll
-            for (int j = 0; j < MH; ++j) {
-                const int e = tid + j * NT;
-                if (e < nhin) hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
-            }
+            local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
             __syncthreads();
-            float r2 = 0.f;
-            if (own) {
-                const float3 f = gather_slots(sent, sptr[tid], sptr[tid + 1], cx, cy, cz);
-                const float4 d = sd[tid];
-                const float4 y = sy[tid];
-                float4 o;
-                if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega_k, r2);
-                else                         o = update_literal(d, y, f);
-                if (!res_only) {
-                    ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
-                    sd[tid] = o;
-                    dprev = d;
-                }
+            if (tid < ph.nbnd) {
+                vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
+            }
+        }
+        if (nbr) publish_mark(p.pflag, mark0 + k + 1);
+        if (!skip_k) {
+            // Phase B: the remaining records, then the interior vertices
+            local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, ph.ntri_a, ntri, ph.nhin_a, nhin, cx, cy,
+                                            cz);
+            __syncthreads();
+            if (own && tid >= ph.nbnd) {
+                vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
+            }
+            // every record has read d^k: the owned offsets move on
+            if (own && !res_only) {
+                sd[tid] = o;
+                dprev = d;
             }
             // fixed sweep counts read only the residual of the start and of
             // the last sweeps; a tolerance needs every sweep's
             if (MODE == kModeConsistent && (!nbr || k == 0 || k >= ci.max_iter - 1))
                 block_residual<NT>(r2, red, acc + k);
         }
-        if (nbr) publish_mark(p.pflag, mark0 + k + 1);
-        else if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+        if (!nbr && !grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
     }
     // every per-sweep sum is complete after this barrier
     if (nbr && !grid_barrier_r(p.bar, p.err, p.spin_budget)) return;

@@ -26,7 +26,8 @@ struct PatchHdr {            // 64 B
     int ent_off;             // into csr_ent[]
     int nslot;               // 3*ntri + 4*nhinge contribution slots
     int nent;                // gather-list entries of the owned vertices
-    int pad[3];
+    int nbnd;                // owned vertices 0..nbnd-1 are in other patches' halos
+    int ntri_a, nhin_a;      // records 0..ntri_a-1 / 0..nhin_a-1 touch one of them
 };
 
 struct TriRec {              // 32 B
