@@ -262,32 +262,44 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
 
 // MT x NT triangles and MH x NT hinges per block.  512 threads: one block
 // (one patch) per SM; 256 threads: two half-size patches per SM, so one
-// block computes while the other waits for its neighbours.
-#define PDG_RES_MT 3
-#define PDG_RES_MH 4
+// block computes while the other waits for its neighbours.  The smaller
+// record set (fewer registers) is used when the patches fit it.
+struct ResVariant { int nt, mt, mh; void* f[2]; };
 
-int resident_limits(int nt, int* mt, int* mh)
+static const ResVariant* res_variants(int* n)
 {
-    if (nt != 256 && nt != 512) return -1;
-    *mt = PDG_RES_MT; *mh = PDG_RES_MH;
-    return 0;
+    static const ResVariant v[] = {
+        {512, 2, 3, {(void*)k_resident<kModeConsistent, 512, 2, 3>, (void*)k_resident<kModeLiteral, 512, 2, 3>}},
+        {512, 3, 4, {(void*)k_resident<kModeConsistent, 512, 3, 4>, (void*)k_resident<kModeLiteral, 512, 3, 4>}},
+        {256, 3, 4, {(void*)k_resident<kModeConsistent, 256, 3, 4>, (void*)k_resident<kModeLiteral, 256, 3, 4>}},
+    };
+    *n = 3;
+    return v;
 }
 
-static void* pick_resident(int mode, int nt)
+int resident_pick(int nt, int max_ntri, int max_nhinge)
 {
-    if (nt == 256)
-        return mode == kModeConsistent ? (void*)k_resident<kModeConsistent, 256, PDG_RES_MT, PDG_RES_MH>
-                                       : (void*)k_resident<kModeLiteral, 256, PDG_RES_MT, PDG_RES_MH>;
-    if (nt == 512)
-        return mode == kModeConsistent ? (void*)k_resident<kModeConsistent, 512, PDG_RES_MT, PDG_RES_MH>
-                                       : (void*)k_resident<kModeLiteral, 512, PDG_RES_MT, PDG_RES_MH>;
-    return nullptr;
+    int n = 0;
+    const ResVariant* v = res_variants(&n);
+    for (int i = 0; i < n; ++i)
+        if (v[i].nt == nt && max_ntri <= v[i].mt * nt && max_nhinge <= v[i].mh * nt) return i;
+    return -1;
 }
 
-int resident_max_blocks(int mode, int nt, size_t smem)
+static void* variant_fn(int variant, int mode)
 {
-    void* f = pick_resident(mode, nt);
+    int n = 0;
+    const ResVariant* v = res_variants(&n);
+    if (variant < 0 || variant >= n) return nullptr;
+    return v[variant].f[mode == kModeConsistent ? 0 : 1];
+}
+
+int resident_max_blocks(int mode, int variant, size_t smem)
+{
+    void* f = variant_fn(variant, mode);
     if (!f) return 0;
+    int n = 0;
+    const int nt = res_variants(&n)[variant].nt;
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess) return 0;
     int dev = 0, nsm = 0, nb = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -296,10 +308,12 @@ int resident_max_blocks(int mode, int nt, size_t smem)
     return nb * nsm;
 }
 
-cudaError_t launch_resident(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s)
+cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t smem, cudaStream_t s)
 {
-    void* f = pick_resident(p.mode, nt);
+    void* f = variant_fn(variant, p.mode);
     if (!f || grid <= 0) return cudaErrorInvalidValue;
+    int n = 0;
+    const int nt = res_variants(&n)[variant].nt;
     PersistArgs copy = p;
     void* args[] = {&copy};
     return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(nt), args, smem, s);

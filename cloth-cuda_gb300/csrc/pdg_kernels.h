@@ -53,10 +53,12 @@ int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
 
 // Resident persistent kernel (pd_resident.cu): one patch per block, records
 // in registers, nt = 512 (one block per SM) or 256 (two).  Limits:
-// nown <= nt, ntri <= mt*nt, nhinge <= mh*nt.
-int resident_limits(int nt, int* mt, int* mh);
-int resident_max_blocks(int mode, int nt, size_t smem);
-cudaError_t launch_resident(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s);
+// nown <= nt, ntri <= mt*nt, nhinge <= mh*nt for the variant's (mt, mh).
+// Kernel variant for nt threads whose record capacity holds the patches
+// (-1: none).
+int resident_pick(int nt, int max_ntri, int max_nhinge);
+int resident_max_blocks(int mode, int variant, size_t smem);
+cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t smem, cudaStream_t s);
 
 // Streaming per-sweep kernel (pd_stream.cu): persistent grid, patches
 // double-buffered in shared memory by bulk copies.  Byte offsets of the

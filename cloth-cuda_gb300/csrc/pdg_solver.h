@@ -80,6 +80,7 @@ struct pdg_solver {
     int mode = PDG_MODE_CONSISTENT;
     int have_final = 1;
     int persist_grid = 0;           // persistent / resident / streaming grid
+    int res_variant = -1;           // resident kernel instance (record capacity)
     pdg::StreamArgs sargs{};        // streaming kernel: stage layout
     size_t stream_smem = 0;
     long long launches = 0;

@@ -209,22 +209,23 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
         // SM, or (block_threads = 256) two half-size patches per SM.
         const int rnt = (c0.kernel == PDG_KERNEL_RESIDENT && c0.block_threads == 256) ? 256 : 512;
         const int per_sm = 512 / rnt;
-        int rmt = 0, rmh = 0;
-        resident_limits(rnt, &rmt, &rmh);
         int ntot = 0;
         for (const auto& c : s->cloths) ntot += c.mesh->N;
         int P = c0.patch_verts;
         if (!P) P = std::min(rnt, std::max(32, ((ntot + per_sm * nsm - 1) / (per_sm * nsm) + 31) / 32 * 32));
         bool ok = P <= rnt && build_layout(s->cloths, P, s->L, err);
+        int variant = -1;
         if (ok) {
-            ok = s->L.max_nown <= rnt && s->L.max_ntri <= rmt * rnt && s->L.max_nhinge <= rmh * rnt &&
+            variant = resident_pick(rnt, s->L.max_ntri, s->L.max_nhinge);
+            ok = variant >= 0 && s->L.max_nown <= rnt &&
                  s->L.smem_resident <= (size_t)std::min(smem_optin / per_sm - 8192, 216 * 1024);
-            if (ok) ok = s->L.npatch <= resident_max_blocks(s->mode, rnt, s->L.smem_resident);
+            if (ok) ok = s->L.npatch <= resident_max_blocks(s->mode, variant, s->L.smem_resident);
         }
         if (ok) {
             s->kernel = PDG_KERNEL_RESIDENT;
             s->patch_verts = P;
             s->nt = rnt;
+            s->res_variant = variant;
             s->persist_grid = s->L.npatch;
             // fixed sweep counts: neighbour-only synchronisation between sweeps
             s->nbr_sync = 1;
@@ -356,7 +357,7 @@ int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
             if (s->kernel == PDG_KERNEL_PERSISTENT)
                 CK(launch_persistent(p, s->nt, s->persist_grid, s->L.smem_bytes, s->stream));
             else
-                CK(launch_resident(p, s->nt, s->persist_grid, s->L.smem_resident, s->stream));
+                CK(launch_resident(p, s->res_variant, s->persist_grid, s->L.smem_resident, s->stream));
             s->launches += 1;
         } else {
             if (!s->graph) {
@@ -511,7 +512,7 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
             cudaEventRecord(e[0], st);   // the frame's events bracket the launch only
             const PersistArgs p = persist_args(s);
             cudaError_t err = s->kernel == PDG_KERNEL_RESIDENT
-                                  ? launch_resident(p, s->nt, s->persist_grid, L.smem_resident, st)
+                                  ? launch_resident(p, s->res_variant, s->persist_grid, L.smem_resident, st)
                                   : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "persistent launch: %s", cudaGetErrorString(err));
             s->launches += 1;
