@@ -57,36 +57,34 @@ __device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long
     return v;
 }
 
-// Publish "this patch finished the sweep with mark m" after all of the
-// block's global writes (the barrier orders them before thread 0's release).
-__device__ __forceinline__ void publish_mark(unsigned long long* pflag, unsigned long long m)
+// Named barriers (barrier 0 is __syncthreads).  `count` threads, a multiple
+// of 32, take part: bar.sync waits for all of them, bar.arrive only counts
+// this warp in and orders its earlier memory accesses before the waiters'
+// later ones.
+__device__ __forceinline__ void named_sync(int id, int count)
 {
-    __syncthreads();
-    if (threadIdx.x == 0) st_release_gpu(&pflag[blockIdx.x], m);
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_arrive(int id, int count)
+{
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-// Wait until every neighbouring patch published a mark >= m (first warp, one
-// lane per neighbour, acquire loads), bounded.  Returns false on timeout or a
-// prior error.
-__device__ __forceinline__ bool wait_neighbours(const int* nb, int nnb, const unsigned long long* pflag,
+// One warp waits until every neighbouring patch published a mark >= m (one
+// lane per neighbour, acquire loads), bounded.  Returns the warp-wide result:
+// false on timeout or a prior error.
+__device__ __forceinline__ bool poll_neighbours(int lane, const int* nb, int nnb, const unsigned long long* pflag,
                                                 unsigned long long m, int* err, long long budget)
 {
-    __shared__ int ok;
-    if (threadIdx.x < 32) {
-        bool good = true;
-        for (int j = threadIdx.x; j < nnb && good; j += 32) {
-            const unsigned long long* f = pflag + nb[j];
-            const long long t0 = clock64();
-            while (ld_acquire_gpu(f) < m) {
-                if (clock64() - t0 > budget || *(volatile int*)err != 0) { atomicCAS(err, 0, 3); good = false; break; }
-                __nanosleep(20);
-            }
+    bool good = true;
+    for (int j = lane; j < nnb && good; j += 32) {
+        const unsigned long long* f = pflag + nb[j];
+        const long long t0 = clock64();
+        while (ld_acquire_gpu(f) < m) {
+            if (clock64() - t0 > budget || *(volatile int*)err != 0) { atomicCAS(err, 0, 3); good = false; break; }
         }
-        const unsigned all = __ballot_sync(0xffffffffu, good);
-        if (threadIdx.x == 0) ok = (all == 0xffffffffu);
     }
-    __syncthreads();
-    return ok != 0;
+    return __ballot_sync(0xffffffffu, good) == 0xffffffffu;
 }
 
 template <int NT, int MT>
@@ -130,16 +128,52 @@ __device__ __forceinline__ void vertex_update(const uint16_t* sent, const int* s
     else                         o = update_literal(d, y, f);
 }
 
-template <int MODE, int NT, int MT, int MH>
-__global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
+// Block sum of r2 over the NT compute threads (named barrier 1), added to
+// *acc by one double atomic.
+template <int NT>
+__device__ __forceinline__ void compute_residual(float r2, float* red, double* acc)
 {
+    const int tid = threadIdx.x;
+    r2 = warp_sum(r2);
+    if ((tid & 31) == 0) red[tid >> 5] = r2;
+    named_sync(1, NT);
+    if (tid < 32) {
+        float v = tid < NT / 32 ? red[tid] : 0.f;
+        v = warp_sum(v);
+        if (tid == 0) atomicAdd(acc, (double)v);
+    }
+}
+
+// Block layout: NT compute threads (thread l < nown owns local vertex l;
+// records of the patch in registers) and one signal warp (threads NT..NT+31)
+// that publishes and polls the per-patch marks.
+//
+// Fixed sweep counts (neighbour synchronisation), one sweep:
+//   compute: [k > 0: bar 3 sync -> halo d^k load] -> bar 1 -> phase A records
+//            -> bar 1 -> update of the boundary vertices (written to global)
+//            -> bar 2 arrive -> phase B records -> bar 1 -> interior update
+//   signal:  bar 2 sync -> release mark k+1 -> [k+1 < sweeps: poll the
+//            neighbours' mark k+1 -> bar 3 arrive]
+// Barrier 1 counts the NT compute threads; barriers 2 and 3 count all
+// NT + 32 threads and alternate (bar 2 of sweep k+1 needs bar 3 of sweep
+// k+1, which needs the signal warp past bar 2 of sweep k), so no instance
+// overlaps the next.  A failed poll is passed to the compute threads through
+// `sig_ok` at bar 3 and every thread leaves.
+// With a tolerance every sweep ends in a grid barrier instead and the
+// signal warp only takes part in the block-wide barriers.
+template <int MODE, int NT, int MT, int MH>
+__global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistArgs p)
+{
+    constexpr int NTT = NT + 32;   // a multiple of 128: 4 warps per SM sub-partition
     extern __shared__ float4 smem[];
     __shared__ PatchHdr ph;
-    __shared__ float red[NT / 32];
+    __shared__ float red[NTT / 32];
     __shared__ int skip;
+    __shared__ int sig_ok;
     __shared__ float som[kResOmega];   // Chebyshev weights of this cloth
     const IterArgs& a = p.it;
     const int tid = threadIdx.x;
+    const bool comp = tid < NT;
     if (tid == 0) ph = a.patches[blockIdx.x];
     __syncthreads();
     const int nown = ph.nown, nlocal = ph.nlocal, ntri = ph.ntri, nhin = ph.nhinge;
@@ -156,22 +190,24 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
     // lowest, so warps finish the local step together.
     TriRec rt[MT];
     HingeRec rh[MH];
-    #pragma unroll
-    for (int j = 0; j < MT; ++j) {
-        const int t = tri_index<NT, MT>(tid, j);
-        if (t < ntri) rt[j] = a.tris[ph.tri_off + t];
-    }
-    #pragma unroll
-    for (int j = 0; j < MH; ++j) {
-        const int e = tid + j * NT;
-        if (e < nhin) rh[j] = a.hinges[ph.hinge_off + e];
+    if (comp) {
+        #pragma unroll
+        for (int j = 0; j < MT; ++j) {
+            const int t = tri_index<NT, MT>(tid, j);
+            if (t < ntri) rt[j] = a.tris[ph.tri_off + t];
+        }
+        #pragma unroll
+        for (int j = 0; j < MH; ++j) {
+            const int e = tid + j * NT;
+            if (e < nhin) rh[j] = a.hinges[ph.hinge_off + e];
+        }
     }
     // gather lists and Chebyshev weights in shared memory
-    for (int l = tid; l <= nown; l += NT) sptr[l] = a.csr_ptr[ph.csr_off + l];
-    for (int k = tid; k < a.omega_stride && k < kResOmega; k += NT) som[k] = a.omega[ph.cloth * a.omega_stride + k];
+    for (int l = tid; l <= nown; l += NTT) sptr[l] = a.csr_ptr[ph.csr_off + l];
+    for (int k = tid; k < a.omega_stride && k < kResOmega; k += NTT) som[k] = a.omega[ph.cloth * a.omega_stride + k];
     __syncthreads();
     const int nent = sptr[nown];
-    for (int q = tid; q < nent; q += NT) sent[q] = a.csr_ent[ph.ent_off + q];
+    for (int q = tid; q < nent; q += NTT) sent[q] = a.csr_ent[ph.ent_off + q];
 
     // predict the owned vertices; the cloth's first block resets its record
     const int c = ph.cloth;
@@ -180,78 +216,122 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
     const bool first = (int)blockIdx.x == ci.patch_begin;
     const int g = ph.vbegin + tid;
     float4 dprev = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (first) reset_rt(a.crt, a.acc, a.acc_stride, c, tid, NT);
+    if (first) reset_rt(a.crt, a.acc, a.acc_stride, c, tid, NTT);
     if (own) {
         predict_vertex(g, p.X, p.V, p.aux, p.mass, p.vcloth, a.cinfo, p.warm, p.Y, a.buf[0], a.buf[1]);
         dprev = __ldcg(&a.buf[0][g]);
     }
     if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
-    for (int l = tid; l < nlocal; l += NT) {
+    for (int l = tid; l < nlocal; l += NTT) {
         const int gg = l < nown ? ph.vbegin + l : __ldg(&a.halo[ph.halo_off + l - nown]);
         sy[l] = __ldcg(&a.Y[gg]);
         sd[l] = __ldcg(&a.buf[0][gg]);
     }
-    // this thread's first halo vertex, re-read every sweep
+    // this compute thread's first halo vertex, re-read every sweep
     const int hl0 = nown + tid;
-    const int hg0 = hl0 < nlocal ? __ldg(&a.halo[ph.halo_off + tid]) : 0;
+    const int hg0 = (comp && hl0 < nlocal) ? __ldg(&a.halo[ph.halo_off + tid]) : 0;
+    __syncthreads();
 
     const float gamma = ci.gamma;
     const int nsweep = p.max_iter + (p.have_final ? 1 : 0);
     const bool nbr = p.nbr_sync != 0;
     const unsigned long long mark0 = p.frame_seq * (unsigned long long)(nsweep + 2);
-    const int* nb = p.nbr + p.nbr_ptr[blockIdx.x];
-    const int nnb = p.nbr_ptr[blockIdx.x + 1] - p.nbr_ptr[blockIdx.x];
     double* acc = a.acc + (size_t)c * a.acc_stride;
-    for (int k = 0; k < nsweep; ++k) {
-        // With fixed sweep counts the cap alone decides (the record stays
-        // active through the sweeps), so no thread waits on global memory
-        // for it; a tolerance needs the per-cloth decision.
-        if (!nbr && tid == 0) skip = cloth_done(a, c, k, first, true) ? 1 : 0;
-        if (k > 0) {   // halo offsets d^k written by the neighbouring blocks
-            if (nbr && !wait_neighbours(nb, nnb, p.pflag, mark0 + k, p.err, p.spin_budget)) return;
-            const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
-            if (hl0 < nlocal) sd[hl0] = __ldcg(&Dk[hg0]);
-            for (int l = hl0 + NT; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
+    if (nbr && !comp) {
+        // ---- signal warp ----
+        const int lane = tid - NT;
+        const int* nb = p.nbr + p.nbr_ptr[blockIdx.x];
+        const int nnb = p.nbr_ptr[blockIdx.x + 1] - p.nbr_ptr[blockIdx.x];
+        for (int k = 0; k < nsweep; ++k) {
+            named_sync(2, NTT);   // the boundary offsets of sweep k are written
+            if (lane == 0) st_release_gpu(&p.pflag[blockIdx.x], mark0 + k + 1);
+            if (k + 1 < nsweep) {
+                const bool ok = poll_neighbours(lane, nb, nnb, p.pflag, mark0 + k + 1, p.err, p.spin_budget);
+                if (lane == 0) sig_ok = ok ? 1 : 0;
+                __syncwarp();
+                named_arrive(3, NTT);
+                if (!ok) return;
+            }
         }
-        __syncthreads();
-        const bool skip_k = nbr ? (k >= ci.max_iter && (k > ci.max_iter || !a.have_final)) : skip != 0;
-        const float omega_k = k < a.omega_stride ? (k < kResOmega ? som[k] : a.omega[c * a.omega_stride + k]) : 1.f;
-        const bool res_only = k >= ci.max_iter;
-        // Phase A: the records through boundary vertices (a prefix of each
-        // list), then the update of the boundary vertices, which the
-        // neighbouring patches read: they are published before phase B, so
-        // the exchange overlaps the interior's work.
-        float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
-        float r2 = 0.f;
-        if (!skip_k) {
-            local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
-            __syncthreads();
-            if (tid < ph.nbnd) {
+    } else if (nbr) {
+        // ---- compute threads, neighbour synchronisation ----
+        for (int k = 0; k < nsweep; ++k) {
+            if (k > 0) {   // the neighbours' d^k: wait for the signal warp, then load the halo
+                named_sync(3, NTT);
+                if (!sig_ok) return;
+                const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
+                if (hl0 < nlocal) sd[hl0] = __ldcg(&Dk[hg0]);
+                for (int l = hl0 + NT; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
+            }
+            named_sync(1, NT);
+            // the cap alone decides: the cloth's record stays active through the sweeps
+            const bool skip_k = k >= ci.max_iter && (k > ci.max_iter || !a.have_final);
+            const float omega_k =
+                k < a.omega_stride ? (k < kResOmega ? som[k] : a.omega[c * a.omega_stride + k]) : 1.f;
+            const bool res_only = k >= ci.max_iter;
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+            float r2 = 0.f;
+            // Phase A: the records through boundary vertices (a prefix of
+            // each list), then the boundary vertices, which the neighbouring
+            // patches read; the signal warp publishes them while phase B runs.
+            if (!skip_k)
+                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
+            named_sync(1, NT);
+            if (!skip_k && tid < ph.nbnd) {
                 vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
-        }
-        if (nbr) publish_mark(p.pflag, mark0 + k + 1);
-        if (!skip_k) {
+            named_arrive(2, NTT);
             // Phase B: the remaining records, then the interior vertices
-            local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, ph.ntri_a, ntri, ph.nhin_a, nhin, cx, cy,
-                                            cz);
-            __syncthreads();
-            if (own && tid >= ph.nbnd) {
+            if (!skip_k)
+                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, ph.ntri_a, ntri, ph.nhin_a, nhin, cx,
+                                                cy, cz);
+            named_sync(1, NT);
+            if (!skip_k && own && tid >= ph.nbnd) {
                 vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             // every record has read d^k: the owned offsets move on
-            if (own && !res_only) {
+            if (!skip_k && own && !res_only) {
                 sd[tid] = o;
                 dprev = d;
             }
             // fixed sweep counts read only the residual of the start and of
-            // the last sweeps; a tolerance needs every sweep's
-            if (MODE == kModeConsistent && (!nbr || k == 0 || k >= ci.max_iter - 1))
-                block_residual<NT>(r2, red, acc + k);
+            // the last sweeps
+            if (MODE == kModeConsistent && !skip_k && (k == 0 || k >= ci.max_iter - 1))
+                compute_residual<NT>(r2, red, acc + k);
         }
-        if (!nbr && !grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+    } else {
+        // ---- tolerance: every sweep ends in a grid barrier ----
+        for (int k = 0; k < nsweep; ++k) {
+            if (tid == 0) skip = cloth_done(a, c, k, first, true) ? 1 : 0;
+            if (k > 0 && comp) {
+                const float4* Dk = (k & 1) ? a.buf[1] : a.buf[0];
+                if (hl0 < nlocal) sd[hl0] = __ldcg(&Dk[hg0]);
+                for (int l = hl0 + NT; l < nlocal; l += NT) sd[l] = __ldcg(&Dk[__ldg(&a.halo[ph.halo_off + l - nown])]);
+            }
+            __syncthreads();
+            const bool skip_k = skip != 0;
+            const float omega_k =
+                k < a.omega_stride ? (k < kResOmega ? som[k] : a.omega[c * a.omega_stride + k]) : 1.f;
+            const bool res_only = k >= ci.max_iter;
+            float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+            float r2 = 0.f;
+            if (!skip_k) {
+                if (comp) local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ntri, 0, nhin, cx, cy, cz);
+                __syncthreads();
+                if (own) {
+                    vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                    if (!res_only) {
+                        ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
+                        sd[tid] = o;
+                        dprev = d;
+                    }
+                }
+                if (MODE == kModeConsistent) block_residual<NTT>(r2, red, acc + k);
+            }
+            if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+        }
     }
     // every per-sweep sum is complete after this barrier
     if (nbr && !grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
@@ -260,18 +340,18 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_resident(PersistArgs p)
     if (own) finalize_vertex(g, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
 }
 
-// MT x NT triangles and MH x NT hinges per block.  512 threads: one block
-// (one patch) per SM; 256 threads: two half-size patches per SM, so one
-// block computes while the other waits for its neighbours.  The smaller
-// record set (fewer registers) is used when the patches fit it.
+// MT x NT triangles and MH x NT hinges per block of NT compute threads plus
+// the signal warp.  480 + 32 threads: one block (one patch) per SM;
+// 224 + 32: two half-size patches per SM.  The smaller record set (fewer
+// registers) is used when the patches fit it.
 struct ResVariant { int nt, mt, mh; void* f[2]; };
 
 static const ResVariant* res_variants(int* n)
 {
     static const ResVariant v[] = {
-        {512, 2, 3, {(void*)k_resident<kModeConsistent, 512, 2, 3>, (void*)k_resident<kModeLiteral, 512, 2, 3>}},
-        {512, 3, 4, {(void*)k_resident<kModeConsistent, 512, 3, 4>, (void*)k_resident<kModeLiteral, 512, 3, 4>}},
-        {256, 3, 4, {(void*)k_resident<kModeConsistent, 256, 3, 4>, (void*)k_resident<kModeLiteral, 256, 3, 4>}},
+        {480, 2, 3, {(void*)k_resident<kModeConsistent, 480, 2, 3>, (void*)k_resident<kModeLiteral, 480, 2, 3>}},
+        {480, 3, 4, {(void*)k_resident<kModeConsistent, 480, 3, 4>, (void*)k_resident<kModeLiteral, 480, 3, 4>}},
+        {224, 3, 4, {(void*)k_resident<kModeConsistent, 224, 3, 4>, (void*)k_resident<kModeLiteral, 224, 3, 4>}},
     };
     *n = 3;
     return v;
@@ -304,7 +384,7 @@ int resident_max_blocks(int mode, int variant, size_t smem)
     int dev = 0, nsm = 0, nb = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, nt, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, nt + 32, smem) != cudaSuccess) return 0;
     return nb * nsm;
 }
 
@@ -316,7 +396,7 @@ cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t 
     const int nt = res_variants(&n)[variant].nt;
     PersistArgs copy = p;
     void* args[] = {&copy};
-    return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(nt), args, smem, s);
+    return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(nt + 32), args, smem, s);
 }
 
 }  // namespace pdg

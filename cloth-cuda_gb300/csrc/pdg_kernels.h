@@ -52,8 +52,9 @@ cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t sme
 int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
 
 // Resident persistent kernel (pd_resident.cu): one patch per block, records
-// in registers, nt = 512 (one block per SM) or 256 (two).  Limits:
-// nown <= nt, ntri <= mt*nt, nhinge <= mh*nt for the variant's (mt, mh).
+// in registers; nt compute threads (480: one block per SM, 224: two) plus a
+// signal warp.  Limits: nown <= nt, ntri <= mt*nt, nhinge <= mh*nt for the
+// variant's (mt, mh).
 // Kernel variant for nt threads whose record capacity holds the patches
 // (-1: none).
 int resident_pick(int nt, int max_ntri, int max_nhinge);

@@ -206,9 +206,10 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     std::string err;
     if ((c0.kernel == PDG_KERNEL_AUTO && !s->any_warm) || c0.kernel == PDG_KERNEL_RESIDENT) {
         // Resident kernel: every patch co-resident, one 512-thread block per
-        // SM, or (block_threads = 256) two half-size patches per SM.
-        const int rnt = (c0.kernel == PDG_KERNEL_RESIDENT && c0.block_threads == 256) ? 256 : 512;
-        const int per_sm = 512 / rnt;
+        // SM, or (block_threads = 256) two half-size patches per SM; a block
+        // is rnt compute threads and a signal warp.
+        const int rnt = (c0.kernel == PDG_KERNEL_RESIDENT && c0.block_threads == 256) ? 224 : 480;
+        const int per_sm = 512 / (rnt + 32);
         int ntot = 0;
         for (const auto& c : s->cloths) ntot += c.mesh->N;
         int P = c0.patch_verts;
@@ -224,7 +225,7 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
         if (ok) {
             s->kernel = PDG_KERNEL_RESIDENT;
             s->patch_verts = P;
-            s->nt = rnt;
+            s->nt = rnt + 32;
             s->res_variant = variant;
             s->persist_grid = s->L.npatch;
             // fixed sweep counts: neighbour-only synchronisation between sweeps
