@@ -285,8 +285,10 @@ def run_ours(args, rank, world, local_rank):
     x0, v0 = s.get_state_all()
     hx.numpy()[:] = x0; hv.numpy()[:] = v0
     xnp, vnp = hx.numpy(), hv.numpy()
+    # each step: the state goes in from pinned host buffers and the result
+    # comes back into the same buffers (the caller's frame loop)
     for _ in range(2):
-        s.set_state_all(xnp, vnp); s.step(1, stats=False); xo, vo = s.get_state_all()
+        s.set_state_all(xnp, vnp); s.step(1, stats=False); s.get_state_all(xnp, vnp)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -294,8 +296,7 @@ def run_ours(args, rank, world, local_rank):
     for i in range(args.steps):
         s.set_state_all(xnp, vnp)
         s.step(1, stats=False)
-        xo, vo = s.get_state_all()
-        xnp[:] = xo; vnp[:] = vo
+        s.get_state_all(xnp, vnp)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if world > 1:

@@ -283,11 +283,19 @@ class Solver:
                                               _p(va) if va is not None else None, 0))
 
     def get_state_all(self, x=None, v=None, on_device=False):
+        """Positions and velocities of every cloth in caller order.  With
+        on_device, x and v are device pointers; otherwise they may be
+        C-contiguous float32 (N, 3) host arrays to write into (e.g. pinned
+        buffers reused every frame), else new arrays are returned."""
         if on_device:
             _check(lib().pdg_solver_get_state_all(self.h, C.c_void_p(x) if x else None, C.c_void_p(v) if v else None, 1))
             return None
         n = int(self.offsets[-1])
-        xa = np.zeros((n, 3), np.float32); va = np.zeros((n, 3), np.float32)
+        xa = x if x is not None else np.empty((n, 3), np.float32)
+        va = v if v is not None else np.empty((n, 3), np.float32)
+        for arr in (xa, va):
+            if arr.dtype != np.float32 or not arr.flags.c_contiguous or arr.size != 3 * n:
+                raise ValueError("output arrays must be C-contiguous float32 with N*3 elements")
         _check(lib().pdg_solver_get_state_all(self.h, _p(xa), _p(va), 0))
         return xa, va
 
