@@ -25,7 +25,8 @@ __device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.
 // ---------------------------------------------------------------------------
 // Stretch projection, consistent form: Gram-Schmidt basis (b0, b1) of F's
 // columns, F2d = [b0 b1]^T F, closest rotation in SO(2) in closed form
-// R2d = rot(atan2(F2d10 - F2d01, F2d00 + F2d11)), R = [b0 b1] R2d.  This is
+// R2d = rot(atan2(F2d10 - F2d01, F2d00 + F2d11)) with (cos, sin) formed by
+// normalising (F2d00 + F2d11, F2d10 - F2d01), R = [b0 b1] R2d.  This is
 // the projection of src/stretch_reference.cpp:38-68 (JacobiSVD U V^T with the
 // determinant fix) without the SVD.
 // ---------------------------------------------------------------------------
