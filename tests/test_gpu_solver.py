@@ -353,3 +353,18 @@ def test_stream_kernel_tolerance_batch(pdg, oracle):
         outs.append((b.get_state_all(), [s_["iterations"] for s_ in st]))
     assert np.array_equal(outs[0][0][0], outs[1][0][0]) and np.array_equal(outs[0][0][1], outs[1][0][1])
     assert outs[0][1] == outs[1][1]
+
+
+def test_converged_solve_matches_direct_local_global(pdg, oracle):
+    # parity protocol: the fused consistent iteration run to convergence
+    # reaches the fixed point of the oracle's direct local/global solve
+    # (sparse LDL^T global step every iteration, consistent pin
+    # elimination, float64) within 1e-5 relative in positions
+    m, c, cfg, sc, a = scene(pdg, oracle, n=17, side=1.0, ks=20.0, kb=1e-3, rho=0.9, max_iterations=6000)
+    s = pdg.Solver(cfg, m, c)
+    st = s.step(1)[0]
+    x, v = s.get_state()
+    x0 = a["rest"].astype(np.float64).reshape(-1)
+    xd, vd = sc.step_direct(x0, np.zeros_like(x0), iters=1500, pin_elim=1, with_bend=True)
+    assert st["iterations"] == 6000
+    assert rel(x, xd) < 1e-5
