@@ -108,13 +108,14 @@ def test_reference_literal_sensitivity_bound(pdg, oracle):
 KERNELS = {"persistent": 2, "resident": 3, "stream": 5}
 
 
+@pytest.mark.parametrize("mtype", [1, 3])
 @pytest.mark.parametrize("kernel", ["persistent", "resident", "resident256", "stream"])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_launch_structures_agree_bitwise(pdg, oracle, kernel, mode):
+def test_launch_structures_agree_bitwise(pdg, oracle, kernel, mode, mtype):
     # one launch per sweep (CUDA graph), one cooperative launch per frame, the
     # resident kernel and the streaming kernel run the same per-vertex
-    # arithmetic in the same order
-    m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=16, mode=mode, kernel=pdg.KERNEL_GRAPH)
+    # arithmetic in the same order (type 3: valence-8 vertices)
+    m, c, cfg, sc, a = scene(pdg, oracle, n=33, mtype=mtype, max_iterations=16, mode=mode, kernel=pdg.KERNEL_GRAPH)
     s1 = pdg.Solver(cfg, m, c)
     cfg.kernel = KERNELS[kernel.replace("256", "")]
     if kernel == "resident256":   # two blocks per SM
