@@ -344,9 +344,7 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.nbr_ptr.push_back((int)L.nbr.size());
         }
     }
-    // y, d per local vertex, the slots and the gather lists (per-sweep kernels
-    // stage the lists like the resident kernel)
-    L.smem_bytes = L.smem_resident;
+    L.smem_bytes = 32 * (size_t)L.max_nlocal + 12 * (size_t)L.max_nslot;   // y, d per local vertex + slots
     return true;
 }
 

@@ -286,8 +286,8 @@ __device__ __forceinline__ void block_residual(float r2, float* red, double* acc
 // ||r(x^k)||^2 to acc[cloth][k].  With res_only it only evaluates the
 // residual.  Data produced by other blocks is loaded with __ldcg (L2, not L1),
 // so the same code is correct inside the persistent kernel between grid
-// barriers.  Shared memory: sy, sd (float4 per local vertex), the three slot
-// arrays, then the gather pointers and entries of the owned vertices.
+// barriers.  Shared memory: sy, sd (float4 per local vertex), then the three
+// slot arrays.
 // ---------------------------------------------------------------------------
 template <int MODE, int NT>
 __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr& ph, int k, bool res_only,
@@ -300,24 +300,13 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     const float4* __restrict__ Dk = (k & 1) ? a.buf[1] : a.buf[0];
     float4* __restrict__ Dn = (k & 1) ? a.buf[0] : a.buf[1];
     float4* sd = sy + ph.nlocal;
-    int* sptr = reinterpret_cast<int*>(cz + ph.nslot);
-    uint16_t* sent = reinterpret_cast<uint16_t*>(sptr + ph.nown + 1);
     const int tid = threadIdx.x;
-    // d^(k-1) of this thread's first owned vertex, fetched with the staging
-    float4 dp0 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (MODE == kModeConsistent && !res_only && tid < ph.nown) dp0 = __ldcg(&Dn[ph.vbegin + tid]);
 
-    // 1. stage y and d^k of owned + halo vertices, and the gather lists
+    // 1. stage y and d^k of owned + halo vertices
     for (int l = tid; l < ph.nlocal; l += NT) {
         const int g = l < ph.nown ? ph.vbegin + l : __ldg(&a.halo[ph.halo_off + l - ph.nown]);
         sy[l] = __ldcg(&a.Y[g]);
         sd[l] = __ldcg(&Dk[g]);
-    }
-    {
-        const int* __restrict__ cp = a.csr_ptr + ph.csr_off;
-        const uint16_t* __restrict__ ce = a.csr_ent + ph.ent_off;
-        for (int l = tid; l <= ph.nown; l += NT) sptr[l] = __ldg(&cp[l]);
-        for (int q = tid; q < ph.nent; q += NT) sent[q] = __ldg(&ce[q]);
     }
     __syncthreads();
     // a skip decision and weight taken by thread 0 while the block staged
@@ -340,15 +329,17 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
 
     // 3. global step per owned vertex
     const float gamma = a.cinfo[ph.cloth].gamma;
+    const int* __restrict__ cp = a.csr_ptr + ph.csr_off;
+    const uint16_t* __restrict__ ce = a.csr_ent + ph.ent_off;
     float r2 = 0.f;
     for (int l = tid; l < ph.nown; l += NT) {
-        const float3 f = gather_slots(sent, sptr[l], sptr[l + 1], cx, cy, cz);
+        const float3 f = gather_slots(ce, __ldg(&cp[l]), __ldg(&cp[l + 1]), cx, cy, cz);
         const int g = ph.vbegin + l;
         const float4 d = sd[l];
         const float4 y = sy[l];
         if (MODE == kModeConsistent) {
             float rv;
-            const float4 dp = res_only ? d : (l == tid ? dp0 : __ldcg(&Dn[g]));
+            const float4 dp = res_only ? d : __ldcg(&Dn[g]);
             const float4 o = update_consistent(d, y, f, dp, gamma, omega, rv);
             r2 += rv;
             if (!res_only) Dn[g] = o;
