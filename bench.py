@@ -127,7 +127,7 @@ class ClockSampler:
 def build_workload(pdg, scenes, wl, seed, args):
     """(meshes, constraints, configs) of a workload."""
     common = dict(kernel=args.kernel, patch_verts=args.patch_verts, block_threads=args.block_threads,
-                  compute_final_residual=1)
+                  compute_final_residual=1, smem_carveout=args.carveout)
     if wl["kind"] == "plain":
         m, c = scenes.hanging(wl["n"], wl["side"], ks=wl["ks"], kb=wl["kb"], seed=seed)
         wind = (0.0, 0.0, 0.0)
@@ -359,6 +359,7 @@ def main():
     ap.add_argument("--kernel", type=int, default=4, help="0 auto, 1 graph, 2 persistent, 3 resident, 4 autotune")
     ap.add_argument("--patch-verts", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)
+    ap.add_argument("--carveout", type=int, default=0, help="shared-memory share of L1 (percent), 0 = default")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="device-timed region only (for profiling)")
     args = ap.parse_args()

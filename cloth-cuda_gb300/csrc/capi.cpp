@@ -69,6 +69,7 @@ int pdg_config_default(pdg_config* c)
     c->patch_verts = 0;
     c->block_threads = 0;
     c->compute_final_residual = 1;
+    c->smem_carveout = 0;
     return PDG_OK;
 }
 

@@ -153,32 +153,43 @@ __global__ void k_apply_pins(float* __restrict__ pos, float* __restrict__ vel, c
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 template <int MODE, int NT>
-static cudaError_t launch_iter_t(const IterArgs& a, int npatch, size_t smem, int k, int res_only, cudaStream_t s)
+// The shared/L1 split is a property of the kernel function: it is set when
+// it differs from the last value set for this instance (carveout 0 = the
+// driver's choice).
+static cudaError_t launch_iter_t(const IterArgs& a, int npatch, size_t smem, int k, int res_only, int carveout,
+                                 cudaStream_t s)
 {
     static bool attr_set = false;   // per template instance
+    static int carve_set = 0;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(k_iter<MODE, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (e != cudaSuccess) return e;
         attr_set = true;
+    }
+    if (carveout != carve_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_iter<MODE, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             carveout > 0 ? carveout : (int)cudaSharedmemCarveoutDefault);
+        if (e != cudaSuccess) return e;
+        carve_set = carveout;
     }
     k_iter<MODE, NT><<<npatch, NT, smem, s>>>(a, k, res_only);
     return cudaGetLastError();
 }
 
 cudaError_t launch_iter(const IterArgs& a, int mode, int nt, int npatch, size_t smem, int k, int res_only,
-                        cudaStream_t s)
+                        cudaStream_t s, int carveout)
 {
     if (mode == kModeConsistent) {
         switch (nt) {
-            case 128: return launch_iter_t<kModeConsistent, 128>(a, npatch, smem, k, res_only, s);
-            case 256: return launch_iter_t<kModeConsistent, 256>(a, npatch, smem, k, res_only, s);
-            case 512: return launch_iter_t<kModeConsistent, 512>(a, npatch, smem, k, res_only, s);
+            case 128: return launch_iter_t<kModeConsistent, 128>(a, npatch, smem, k, res_only, carveout, s);
+            case 256: return launch_iter_t<kModeConsistent, 256>(a, npatch, smem, k, res_only, carveout, s);
+            case 512: return launch_iter_t<kModeConsistent, 512>(a, npatch, smem, k, res_only, carveout, s);
         }
     } else {
         switch (nt) {
-            case 128: return launch_iter_t<kModeLiteral, 128>(a, npatch, smem, k, res_only, s);
-            case 256: return launch_iter_t<kModeLiteral, 256>(a, npatch, smem, k, res_only, s);
-            case 512: return launch_iter_t<kModeLiteral, 512>(a, npatch, smem, k, res_only, s);
+            case 128: return launch_iter_t<kModeLiteral, 128>(a, npatch, smem, k, res_only, carveout, s);
+            case 256: return launch_iter_t<kModeLiteral, 256>(a, npatch, smem, k, res_only, carveout, s);
+            case 512: return launch_iter_t<kModeLiteral, 512>(a, npatch, smem, k, res_only, carveout, s);
         }
     }
     return cudaErrorInvalidValue;

@@ -8,7 +8,7 @@
 namespace pdg {
 
 cudaError_t launch_iter(const IterArgs& a, int mode, int nt, int npatch, size_t smem, int k, int res_only,
-                        cudaStream_t s);
+                        cudaStream_t s, int carveout = 0);
 cudaError_t launch_predict(const IterArgs& a, const float4* X, const float4* V, const float4* aux,
                            const float* mass, const int* vcloth, const float4* warm, int n, cudaStream_t s);
 cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float4* aux, const int* vcloth, int n,

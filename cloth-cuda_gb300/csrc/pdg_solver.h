@@ -81,6 +81,7 @@ struct pdg_solver {
     int have_final = 1;
     int persist_grid = 0;           // persistent / resident / streaming grid
     int res_variant = -1;           // resident kernel instance (record capacity)
+    int carveout = 0;               // shared/L1 split of the per-sweep kernel (percent, 0 = default)
     pdg::StreamArgs sargs{};        // streaming kernel: stage layout
     size_t stream_smem = 0;
     long long launches = 0;

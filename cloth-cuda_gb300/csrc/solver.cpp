@@ -124,7 +124,7 @@ cudaError_t launch_sweep(pdg_solver* s, const IterArgs& a, int k, int res_only, 
         s->sargs.spin_budget = s->wait_budget;
         return launch_stream(a, s->sargs, s->mode, s->nt, s->persist_grid, s->stream_smem, k, res_only, st);
     }
-    return launch_iter(a, s->mode, s->nt, s->L.npatch, s->L.smem_bytes, k, res_only, st);
+    return launch_iter(a, s->mode, s->nt, s->L.npatch, s->L.smem_bytes, k, res_only, st, s->carveout);
 }
 
 // One frame as a sequence of stream-ordered launches.
@@ -189,6 +189,8 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     if (s->nt != 128 && s->nt != 256 && s->nt != 512)
         return set_error(PDG_ERR_ARG, "block_threads must be 128, 256 or 512");
     s->patch_verts = c0.patch_verts ? c0.patch_verts : 256;
+    if (c0.smem_carveout < 0 || c0.smem_carveout > 100) return set_error(PDG_ERR_ARG, "smem_carveout must be in [0, 100]");
+    s->carveout = c0.smem_carveout;
     if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
     if (c0.kernel == PDG_KERNEL_AUTOTUNE) return autotune_create(n, cfgs, meshes, cons, stream, out);
     if (c0.kernel < PDG_KERNEL_AUTO || (c0.kernel > PDG_KERNEL_RESIDENT && c0.kernel != PDG_KERNEL_STREAM))

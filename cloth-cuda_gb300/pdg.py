@@ -37,7 +37,7 @@ class Config(C.Structure):
         ("stretch_stiffness", C.c_float), ("bend_stiffness", C.c_float), ("damping", C.c_float),
         ("wind", C.c_float * 3), ("cheb_delay", C.c_int), ("gamma", C.c_float), ("mode", C.c_int),
         ("init", C.c_int), ("kernel", C.c_int), ("patch_verts", C.c_int), ("block_threads", C.c_int),
-        ("compute_final_residual", C.c_int),
+        ("compute_final_residual", C.c_int), ("smem_carveout", C.c_int),
     ]
 
     @classmethod
