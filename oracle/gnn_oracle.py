@@ -1,7 +1,7 @@
 """Float64 restatement of the warm-start network -- TEST INFRASTRUCTURE ONLY.
 
-The network has no counterpart in the reference; this module is the checker
-for the library's hand-written CUDA forward/backward/Adam kernels (tests only).
+The network has no counterpart in the reference; the tests compare the
+library's hand-written CUDA forward/backward/Adam kernels with this module.
 
 Network (hidden H = 64), on the mesh graph (both directions of every edge):
     h0    = relu(We x + be)                          x: 10 node features

@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library under
  * cloth-cuda_gb300/) links, loads or calls this code.  Only tests/, the
  * smoke check in __graft_entry__.py and the CPU-baseline leg of bench.py use
- * it, and only as the checker or as the timed CPU baseline.
+ * it, and only to compare results with or as the timed CPU baseline.
  *
  * It restates, in plain C, the reference algorithms of Chongyao/cloth-cuda:
  *   generator          src/mesh_generator.cpp:6-91
