@@ -369,3 +369,74 @@ def test_converged_solve_matches_direct_local_global(pdg, oracle):
     xd, vd = sc.step_direct(x0, np.zeros_like(x0), iters=1500, pin_elim=1, with_bend=True)
     assert st["iterations"] == 6000
     assert rel(x, xd) < 1e-5
+
+
+def irregular_mesh(n=24, drop=0.12, seed=3):
+    """Grid with a random diagonal per cell and a random 12 % of triangles
+    removed (holes, inner boundaries, valence 1..8), unreferenced vertices
+    dropped; rest in the x-y plane with z-jitter."""
+    rng = np.random.default_rng(seed)
+    pos = np.array([[j / (n - 1), -i / (n - 1), 1e-4 * rng.standard_normal()] for i in range(n) for j in range(n)],
+                   np.float32)
+    tris = []
+    for i in range(n - 1):
+        for j in range(n - 1):
+            a, b, c, d = i * n + j, i * n + j + 1, (i + 1) * n + j, (i + 1) * n + j + 1
+            tris += [[a, c, b], [b, c, d]] if rng.random() < 0.5 else [[a, c, d], [a, d, b]]
+    tris = np.array(tris, np.int32)
+    tris = tris[rng.random(len(tris)) >= drop]
+    used = np.unique(tris)
+    remap = -np.ones(len(pos), np.int64); remap[used] = np.arange(len(used))
+    return pos[used], remap[tris].astype(np.int32)
+
+
+@pytest.mark.parametrize("kernel", ["persistent", "resident", "resident256", "stream"])
+def test_irregular_mesh(pdg, oracle, kernel):
+    # mixed valence, holes and inner boundaries: one frame against the f64
+    # oracle, and every launch structure bitwise equal to the graph path
+    pos, tris = irregular_mesh()
+    m = pdg.Mesh.create(pos, tris, density=0.1)
+    c = pdg.Constraints(m).build_stretch(1e3).build_bend(1e-2)
+    top = np.where(pos[:, 1] > -1e-6)[0]
+    c.set_pins(top[[0, -1]])
+    cfg = pdg.Config.default(max_iterations=10, rho=0.99, dt=1 / 60, gravity=-9.81, kernel=pdg.KERNEL_GRAPH)
+    g = pdg.Solver(cfg, m, c)
+    stg = g.step(2)
+    a = m.arrays(); ca = c.arrays()
+    sc = oracle.Scene(a["rest"], a["tris"], k_stretch=ca["k_stretch"], k_bend=1e-2, pins=ca["pins"], h=cfg.dt,
+                      gravity=cfg.gravity)
+    x = a["rest"].astype(np.float64).reshape(-1); v = np.zeros_like(x)
+    for _ in range(2):
+        x, v, _ = sc.step_jacobi(x, v, 10, rho=0.99)
+    xg, vg = g.get_state()
+    assert rel(xg, x) < REL_ONE_FRAME
+    cfg.kernel = KERNELS[kernel.replace("256", "")]
+    if kernel == "resident256":
+        cfg.block_threads = 256
+    s = pdg.Solver(cfg, m, c)
+    s.step(2)
+    assert all(np.array_equal(u, w) for u, w in zip(g.get_state(), s.get_state()))
+
+
+def test_batch_with_a_single_triangle_cloth(pdg, oracle):
+    # ragged batch: a 3-vertex cloth without hinges beside a regular one;
+    # each equals its own single-cloth solve
+    tri = pdg.Mesh.create(np.array([[0, 0, 0], [0.1, 0, 0], [0, -0.1, 0.001]], np.float32),
+                          np.array([[0, 1, 2]], np.int32))
+    ct = pdg.Constraints(tri).build_stretch(100.0).set_pins([0])
+    m, c, cfg, sc, a = scene(pdg, oracle, n=9)
+    cfg_t = pdg.Config.default(max_iterations=10, rho=0.99, dt=1 / 60, gravity=-9.81)
+    singles = []
+    for mm, cc, cf in [(tri, ct, cfg_t), (m, c, cfg)]:
+        s = pdg.Solver(cf, mm, cc)
+        s.step(3, stats=False)
+        singles.append(s.get_state())
+    for kern in (pdg.KERNEL_GRAPH, pdg.KERNEL_RESIDENT):
+        cfg_t.kernel = cfg.kernel = kern
+        b = pdg.Solver([cfg_t, cfg], [tri, m], [ct, c])
+        b.step(3, stats=False)
+        for i in range(2):
+            assert all(np.array_equal(u, w) for u, w in zip(b.get_state(i), singles[i]))
+    xt = singles[0][0]
+    assert np.array_equal(xt[0], np.array([0, 0, 0], np.float32))   # pinned corner stays
+    assert np.all(np.isfinite(xt))
