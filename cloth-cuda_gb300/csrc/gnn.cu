@@ -36,6 +36,7 @@ struct pdg_warmstart {
     DevBuf<bf16> xin, cat[L], pq[L], uo[L], hfin;
     DevBuf<float> out, target, freew, dout, dh, dtmp, dcat, dpq;
     DevBuf<double> loss;
+    float smooth = 0.f;   // weight of the neighbour-difference term of the loss
     pdg_solver* solver = nullptr;
     ~pdg_warmstart()
     {
@@ -142,7 +143,8 @@ int backward(pdg_warmstart* w, float inv_cnt, cudaStream_t st)
     float* g = w->g.p;
     GK(cudaMemsetAsync(g, 0, sizeof(float) * y.total, st));
     GK(cudaMemsetAsync(w->loss.p, 0, sizeof(double), st));
-    k_loss<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, w->target.p, w->freew.p, inv_cnt, w->dout.p, w->loss.p);
+    k_loss<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, w->target.p, w->freew.p, w->ptr.p, w->adj.p, w->smooth,
+                                       inv_cnt, w->dout.p, w->loss.p);
     k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dout.p, 16, NO, w->hfin.p, H, H, N, g + y.Wd, g + y.bd);
     k_gemm<float, 16, H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dout.p, 16, N, w->W.Wdt, nullptr, nullptr, 0, nullptr, 0,
                                                          nullptr, 0, w->dh.p, H);
@@ -438,6 +440,14 @@ int pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* 
     GK(cudaMemcpyAsync(&l, w->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     GK(cudaStreamSynchronize(st));
     if (loss) *loss = (float)l;
+    return PDG_OK;
+}
+
+int pdg_warmstart_set_smoothness(pdg_warmstart* w, float lambda)
+{
+    if (!w || !(lambda >= 0.f) || !std::isfinite(lambda))
+        return set_error(PDG_ERR_ARG, "pdg_warmstart_set_smoothness: lambda must be finite and >= 0");
+    w->smooth = lambda;
     return PDG_OK;
 }
 

@@ -250,23 +250,43 @@ __global__ void __launch_bounds__(256) k_msg_bwd(int N, const int* __restrict__ 
     }
 }
 
-// out[:, 0:3] vs target over free vertices: loss += sum sq / cnt; dout = 2 diff / cnt.
+// Error d_i = (out_i[0:3] - target_i) w_i over free vertices (w in {0, 1}):
+//   loss = inv_cnt [ sum_i |d_i|^2 + lam/2 sum_(i,j) w_i w_j |d_i - d_j|^2 ]
+// over the directed edges (i, j) of the symmetric adjacency; the second
+// term weighs the error's differences between neighbours (its high-frequency
+// part).  dout_i = inv_cnt [2 d_i + 2 lam sum_j w_j (d_i - d_j)] w_i, one
+// thread per vertex, no atomics.
 __global__ void k_loss(int N, const float* __restrict__ out, const float* __restrict__ target,
-                       const float* __restrict__ freew, float inv_cnt, float* __restrict__ dout,
-                       double* __restrict__ loss)
+                       const float* __restrict__ freew, const int* __restrict__ ptr, const int* __restrict__ adj,
+                       float lam, float inv_cnt, float* __restrict__ dout, double* __restrict__ loss)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float s = 0.f;
     if (i < N) {
         const float w = freew[i];
-        for (int c = 0; c < 16; ++c) {
-            float d = 0.f;
-            if (c < NO) {
-                d = (out[(size_t)i * 16 + c] - target[(size_t)i * 3 + c]) * w;
-                s += d * d;
-            }
-            dout[(size_t)i * 16 + c] = 2.f * d * inv_cnt;
+        float d[NO], gsum[NO];
+        #pragma unroll
+        for (int c = 0; c < NO; ++c) {
+            d[c] = (out[(size_t)i * 16 + c] - target[(size_t)i * 3 + c]) * w;
+            s += d[c] * d[c];
+            gsum[c] = d[c];
         }
+        if (lam != 0.f && w > 0.f) {
+            for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+                const int j = adj[q];
+                const float wj = freew[j];
+                if (wj == 0.f) continue;
+                float e2 = 0.f;
+                #pragma unroll
+                for (int c = 0; c < NO; ++c) {
+                    const float e = d[c] - (out[(size_t)j * 16 + c] - target[(size_t)j * 3 + c]) * wj;
+                    e2 += e * e;
+                    gsum[c] += lam * wj * e;
+                }
+                s += 0.5f * lam * wj * e2;
+            }
+        }
+        for (int c = 0; c < 16; ++c) dout[(size_t)i * 16 + c] = c < NO ? 2.f * gsum[c] * w * inv_cnt : 0.f;
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0 && s != 0.f) atomicAdd(loss, (double)s * inv_cnt);

@@ -391,6 +391,11 @@ class WarmStart:
         _check(lib().pdg_warmstart_attach(self.h, solver.h))
         self.solver = solver   # keep alive
 
+    def set_smoothness(self, lam):
+        """Weight of the neighbour-difference term of the loss (0: plain MSE)."""
+        _check(lib().pdg_warmstart_set_smoothness(self.h, C.c_float(lam)))
+        return self
+
     def train_frame(self, solver, lr):
         loss = C.c_float()
         _check(lib().pdg_warmstart_train_frame(self.h, solver.h, C.c_float(lr), C.byref(loss)))

@@ -1,13 +1,14 @@
 """Train and evaluate the learned warm start on data the PD solver generates.
 
     python cloth-cuda_gb300/train_warmstart.py [--trajectories 256] [--frames 64]
-        [--batch 32] [--lr 1e-3] [--eval-seeds 128] [--out params.npy] [--json result.json]
+        [--batch 32] [--lr 1e-3] [--smoothness 0] [--eval-seeds 128] [--out params.npy] [--json result.json]
 
 Training data: trajectories of cloths drawn from the batched-workload
 distribution (scenes.batch), `batch` cloths per solver; every frame of every
 trajectory is one training batch: inputs (x_n, v_n, y), target the solver's
 frame result x_{n+1} - y, computed with a deep solve (cap 400 sweeps, relative
-residual 1e-6) so the target is close to the converged positions.  MSE loss,
+residual 1e-6) so the target is close to the converged positions.  Loss: MSE
+plus --smoothness times the squared error differences over the mesh edges;
 Adam.  Evaluation on `eval_seeds` held-out cloths: for each, the same frames
 are solved from the inertial start and from the learned start (kept only
 where its residual is lower), to relative residual 1e-5 with cap 200; the
@@ -32,7 +33,7 @@ import scenes  # noqa: E402
 
 
 def train(args, log=print):
-    w = pdg.WarmStart(seed=args.seed)
+    w = pdg.WarmStart(seed=args.seed).set_smoothness(args.smoothness)
     nbatches = max(1, args.trajectories // args.batch)
     losses = []
     t0 = time.time()
@@ -50,7 +51,8 @@ def train(args, log=print):
 
 
 def score(params, args, seeds=2, frames=32, base_seed=500000):
-    """Mean training loss (lr = 0) of `params` on held-out trajectories."""
+    """Mean squared offset error (lr = 0, no smoothness term) of `params` on
+    held-out trajectories."""
     out = []
     for b in range(seeds):
         ms, cs, cfgs, _ = scenes.batch(args.batch, seed=base_seed + b, max_iterations=args.target_cap,
@@ -117,6 +119,8 @@ def main():
     ap.add_argument("--frames", type=int, default=64)
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--smoothness", type=float, default=0.0,
+                    help="weight of the neighbour-difference term of the training loss")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--target-cap", type=int, default=400)
     ap.add_argument("--target-tol", type=float, default=1e-6)

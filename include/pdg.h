@@ -271,6 +271,11 @@ int  pdg_warmstart_attach(pdg_warmstart* w, pdg_solver* s);
 /* Training on data the solver generates: one frame of `s` from its current
  * state, then one Adam step (lr > 0) on (x_n, v_n, y) -> (x_{n+1} - y). */
 int  pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* loss);
+/* Loss of training and evaluation: mean squared offset error plus lambda/2
+ * times the squared error differences over the mesh's edges (default 0).
+ * The second term weighs the high-frequency part of the error, which the
+ * residual judge of the learned start amplifies. */
+int  pdg_warmstart_set_smoothness(pdg_warmstart* w, float lambda);
 void pdg_warmstart_destroy(pdg_warmstart* w);
 
 /* ---------------- allocation-free frame ----------------------------------

@@ -76,13 +76,22 @@ def forward(p, x, e, src, dst, deg):
     return out, cache
 
 
-def loss_and_grad(p, x, e, src, dst, deg, target, free):
+def loss_and_grad(p, x, e, src, dst, deg, target, free, lam=0.0):
+    """Loss = [sum_i |d_i|^2 + lam/2 sum_(a->b) w_a w_b |d_a - d_b|^2] / cnt with
+    d = (out - target) * free over the directed edges (both directions of
+    every mesh edge), and its gradient with respect to every parameter."""
     out, c = forward(p, x, e, src, dst, deg)
     cnt = max(int(free.sum()) * NO, 1)
     diff = (out - target) * free[:, None]
-    loss = float((diff ** 2).sum() / cnt)
+    wab = (free[src] * free[dst])[:, None]
+    de = (diff[src] - diff[dst]) * wab
+    loss = float(((diff ** 2).sum() + 0.5 * lam * ((diff[src] - diff[dst]) ** 2 * wab).sum()) / cnt)
     g = {n: np.zeros(s) for n, s in shapes()}
-    dout = 2.0 * diff / cnt
+    gd = 2.0 * diff
+    if lam:
+        np.add.at(gd, src, lam * de)
+        np.add.at(gd, dst, -lam * de)
+    dout = gd * free[:, None] / cnt
     g["Wd"] = dout.T @ c["h"]
     g["bd"] = dout.sum(0)
     dh = dout @ p["Wd"]

@@ -32,10 +32,11 @@ def problem(seed=0, n=30):
     return G, p, x, e, src, dst, deg, target, free, ptr, adj
 
 
-def test_forward_backward_match_oracle(pdg):
+@pytest.mark.parametrize("lam", [0.0, 0.5])
+def test_forward_backward_match_oracle(pdg, lam):
     G, p, x, e, src, dst, deg, target, free, ptr, adj = problem(0)
     flat = G.flatten(p).astype(np.float32)
-    w = pdg.WarmStart(seed=1)
+    w = pdg.WarmStart(seed=1).set_smoothness(lam)
     assert w.count == G.count()
     w.set_params(flat)
     assert np.array_equal(w.get_params(), flat)
@@ -46,7 +47,7 @@ def test_forward_backward_match_oracle(pdg):
         if k[0] in "WABU":
             pb[k] = bf16_round(pb[k]).astype(np.float64)
     lo, go, oo = G.loss_and_grad(pb, bf16_round(x).astype(np.float64), e.astype(np.float64), src, dst, deg,
-                                 target.astype(np.float64), free.astype(np.float64))
+                                 target.astype(np.float64), free.astype(np.float64), lam)
     assert abs(loss - lo) <= 2e-2 * lo
     assert np.linalg.norm(out - oo) <= 2e-2 * np.linalg.norm(oo)
     gg = G.unflatten(grads)

@@ -38,9 +38,10 @@ def random_problem(seed=0, n=5):
     return G, p, x, e, src, dst, deg, target, free, ptr, adj
 
 
-def test_oracle_gradients_match_finite_differences():
+@pytest.mark.parametrize("lam", [0.0, 0.7])
+def test_oracle_gradients_match_finite_differences(lam):
     G, p, x, e, src, dst, deg, target, free, _, _ = random_problem(0)
-    loss, g, _ = G.loss_and_grad(p, x, e, src, dst, deg, target, free)
+    loss, g, _ = G.loss_and_grad(p, x, e, src, dst, deg, target, free, lam)
     flat = G.flatten(p)
     gflat = G.flatten(g)
     rng = np.random.default_rng(1)
@@ -49,8 +50,8 @@ def test_oracle_gradients_match_finite_differences():
     for k in idx:
         fp = flat.copy(); fp[k] += eps
         fm = flat.copy(); fm[k] -= eps
-        lp = G.loss_and_grad(G.unflatten(fp), x, e, src, dst, deg, target, free)[0]
-        lm = G.loss_and_grad(G.unflatten(fm), x, e, src, dst, deg, target, free)[0]
+        lp = G.loss_and_grad(G.unflatten(fp), x, e, src, dst, deg, target, free, lam)[0]
+        lm = G.loss_and_grad(G.unflatten(fm), x, e, src, dst, deg, target, free, lam)[0]
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - gflat[k]) <= 1e-6 + 1e-4 * abs(fd), (k, fd, gflat[k])
 
