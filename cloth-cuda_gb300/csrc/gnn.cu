@@ -72,8 +72,8 @@ int alloc_params(pdg_warmstart* w)
     const size_t sizes[] = {(size_t)H * NFP, 2u * H * H, 2u * H * H, 2u * H * H, 2u * H * H, 16u * H, (size_t)H * 16};
     size_t total = sizes[0] + L * (sizes[1] + sizes[2] + sizes[3] + sizes[4]) + sizes[5] + sizes[6];
     GK(w->wbuf.alloc(total));
-    GK(cudaMemset(w->wbuf.p, 0, sizeof(bf16) * total));
-    GK(cudaMemset(w->bdp.p, 0, sizeof(float) * 16));
+    GK(cudaMemsetAsync(w->wbuf.p, 0, sizeof(bf16) * total, w->stream));
+    GK(cudaMemsetAsync(w->bdp.p, 0, sizeof(float) * 16, w->stream));
     bf16* q = w->wbuf.p;
     w->W.We = q; q += sizes[0];
     for (int l = 0; l < L; ++l) {
@@ -84,9 +84,9 @@ int alloc_params(pdg_warmstart* w)
     }
     w->W.Wd = q; q += sizes[5];
     w->W.Wdt = q;
-    GK(cudaMemset(w->g.p, 0, sizeof(float) * n));
-    GK(cudaMemset(w->m.p, 0, sizeof(float) * n));
-    GK(cudaMemset(w->v.p, 0, sizeof(float) * n));
+    GK(cudaMemsetAsync(w->g.p, 0, sizeof(float) * n, w->stream));
+    GK(cudaMemsetAsync(w->m.p, 0, sizeof(float) * n, w->stream));
+    GK(cudaMemsetAsync(w->v.p, 0, sizeof(float) * n, w->stream));
     return PDG_OK;
 }
 
@@ -265,7 +265,7 @@ int pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out)
         fill(y.A[l], H, H, 1.f); fill(y.B[l], H, H, 1.f); fill(y.C[l], H, EF, 1.f); fill(y.U[l], H, 2 * H, 1.f);
     }
     fill(y.Wd, NO, H, 0.1f);
-    GK(cudaMemcpy(w->p.p, h.data(), sizeof(float) * y.total, cudaMemcpyHostToDevice));
+    GK(cudaMemcpyAsync(w->p.p, h.data(), sizeof(float) * y.total, cudaMemcpyHostToDevice, w->stream));
     rc = refresh_bf16(w.get(), w->stream);
     if (rc) return rc;
     GK(cudaStreamSynchronize(w->stream));
@@ -285,7 +285,8 @@ int pdg_warmstart_get_params(pdg_warmstart* w, float* host)
     if (!w || !host) return set_error(PDG_ERR_ARG, "null argument");
     GK(cudaStreamSynchronize(w->stream));
     if (w->solver) GK(cudaStreamSynchronize(w->solver->stream));
-    GK(cudaMemcpy(host, w->p.p, sizeof(float) * w->lay.total, cudaMemcpyDeviceToHost));
+    GK(cudaMemcpyAsync(host, w->p.p, sizeof(float) * w->lay.total, cudaMemcpyDeviceToHost, w->stream));
+    GK(cudaStreamSynchronize(w->stream));
     return PDG_OK;
 }
 
@@ -296,9 +297,9 @@ int pdg_warmstart_set_params(pdg_warmstart* w, const float* host)
         if (!std::isfinite(host[i])) return set_error(PDG_ERR_ARG, "non-finite parameter %d", i);
     GK(cudaStreamSynchronize(w->stream));
     if (w->solver) GK(cudaStreamSynchronize(w->solver->stream));
-    GK(cudaMemcpy(w->p.p, host, sizeof(float) * w->lay.total, cudaMemcpyHostToDevice));
-    GK(cudaMemset(w->m.p, 0, sizeof(float) * w->lay.total));
-    GK(cudaMemset(w->v.p, 0, sizeof(float) * w->lay.total));
+    GK(cudaMemcpyAsync(w->p.p, host, sizeof(float) * w->lay.total, cudaMemcpyHostToDevice, w->stream));
+    GK(cudaMemsetAsync(w->m.p, 0, sizeof(float) * w->lay.total, w->stream));
+    GK(cudaMemsetAsync(w->v.p, 0, sizeof(float) * w->lay.total, w->stream));
     w->t = 0;
     const int rc = refresh_bf16(w, w->stream);
     if (rc) return rc;

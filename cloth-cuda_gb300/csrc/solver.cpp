@@ -340,9 +340,11 @@ int pdg_solver_cloth_counts(const pdg_solver* s, int cloth, int* N, int* T)
 static int take_wait_error(pdg_solver* s)
 {
     int e = 0;
-    CK(cudaMemcpy(&e, s->bar.p + 2, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(&e, s->bar.p + 2, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     if (!e) return PDG_OK;
-    CK(cudaMemset(s->bar.p + 2, 0, sizeof(int)));
+    CK(cudaMemsetAsync(s->bar.p + 2, 0, sizeof(int), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return set_error(PDG_ERR_TIMEOUT, "bounded wait ran out (%s)",
                      e == 1 ? "grid barrier" : e == 2 ? "resident grid barrier" : "neighbour mark");
 }
