@@ -59,3 +59,35 @@ def test_two_rank_partition_and_max_timing(tmp_path):
     verts = [v for _, v in counts]
     assert abs(verts[0] - verts[1]) / sum(verts) < 0.05  # balanced by vertices
     assert tmax == max(len(mine) + r * 0.25 for r, (mine, _) in enumerate(counts))
+
+
+def _leaving_worker(rank, world, port, out_dir):
+    # rank 1 leaves between steps (after the first step's collective); rank 0
+    # must learn of it at its next collective through the process-group
+    # timeout instead of waiting forever
+    import datetime
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=3))
+    t = torch.tensor([1.0])
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)          # step 1: both ranks
+    if rank == 1:
+        return                                      # leaves without a goodbye
+    outcome = "completed"
+    try:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)      # step 2: the peer is gone
+    except Exception as e:                           # gloo raises on timeout / closed peer
+        outcome = "error: " + type(e).__name__
+    with open(os.path.join(out_dir, "outcome.txt"), "w") as f:
+        f.write(outcome)
+
+
+def test_departed_rank_is_reported_not_awaited(tmp_path):
+    world = 2
+    port = _free_port()
+    ctx = mp.start_processes(_leaving_worker, args=(world, port, str(tmp_path)), nprocs=world, join=False,
+                             start_method="spawn")
+    while not ctx.join(timeout=30):
+        pass
+    outcome = (tmp_path / "outcome.txt").read_text()
+    assert outcome.startswith("error"), outcome
