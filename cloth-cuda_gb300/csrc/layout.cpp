@@ -11,69 +11,6 @@ namespace pdg {
 
 namespace {
 
-// Shared-memory bank of every contribution slot of a patch.  Slot e is
-// stored by write group w[e] (one warp store: 32 consecutive records, one
-// corner) and, when its vertex is owned, loaded by read group r[e] (one warp
-// load of the gather: 32 consecutive owned vertices, one list position).  A
-// colour is a bank; distinct colours within every group make both the
-// stores and the gather loads free of bank conflicts.  A bipartite graph of
-// maximum degree 32 has a 32-edge-colouring (Koenig); this is the greedy
-// colouring with alternating-path recolouring, preferring the least-used
-// colour so the banks fill evenly.
-void color_slots(int nW, int nR, const std::vector<int>& w, const std::vector<int>& r, std::vector<int>& col)
-{
-    const int E = (int)w.size();
-    std::vector<int> wt((size_t)nW * 32, -1), rt((size_t)nR * 32, -1), used(32, 0);
-    col.assign(E, -1);
-    auto put = [&](int e, int c) {
-        col[e] = c;
-        wt[(size_t)w[e] * 32 + c] = e;
-        if (r[e] >= 0) rt[(size_t)r[e] * 32 + c] = e;
-        ++used[c];
-    };
-    auto take = [&](int e) {
-        wt[(size_t)w[e] * 32 + col[e]] = -1;
-        if (r[e] >= 0) rt[(size_t)r[e] * 32 + col[e]] = -1;
-        --used[col[e]];
-    };
-    std::vector<int> path;
-    for (int e = 0; e < E; ++e) {
-        const size_t we = (size_t)w[e] * 32;
-        const int re = r[e];
-        int best = -1;
-        for (int c = 0; c < 32; ++c)
-            if (wt[we + c] < 0 && (re < 0 || rt[(size_t)re * 32 + c] < 0) && (best < 0 || used[c] < used[best]))
-                best = c;
-        if (best < 0) {
-            // alpha is free at the write group, beta at the read group; swap
-            // alpha and beta along the alternating path that starts at the
-            // read group (it cannot reach the write group, which has no
-            // alpha edge), after which alpha is free at both
-            int alpha = -1, beta = -1;
-            for (int c = 0; c < 32; ++c) {
-                if (alpha < 0 && wt[we + c] < 0) alpha = c;
-                if (beta < 0 && rt[(size_t)re * 32 + c] < 0) beta = c;
-            }
-            path.clear();
-            int node = re, c = alpha;
-            bool at_read = true;
-            while (node >= 0) {
-                const int f = at_read ? rt[(size_t)node * 32 + c] : wt[(size_t)node * 32 + c];
-                if (f < 0) break;
-                path.push_back(f);
-                node = at_read ? w[f] : r[f];
-                at_read = !at_read;
-                c = c == alpha ? beta : alpha;
-            }
-            std::vector<int> old(path.size());
-            for (size_t q = 0; q < path.size(); ++q) { old[q] = col[path[q]]; take(path[q]); }
-            for (size_t q = 0; q < path.size(); ++q) put(path[q], old[q] == alpha ? beta : alpha);
-            best = alpha;
-        }
-        put(e, best);
-    }
-}
-
 uint32_t spread10(uint32_t v)
 {
     v &= 0x3ffu;
@@ -349,62 +286,23 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                     const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
                     if (l < nown) cnt[l + 1]++;
                 }
-            int maxdeg = 0;
-            for (int l = 0; l < nown; ++l) maxdeg = std::max(maxdeg, cnt[l + 1]);
             for (int l = 0; l < nown; ++l) cnt[l + 1] += cnt[l];
-            // slot e: triangle corner a of local triangle lt is e = a*ntri + lt,
-            // hinge corner a of local hinge lh is e = 3*ntri + a*nhin + lh;
-            // its write group and (owned corners) read group
-            const int ntg = (ntri + 31) / 32, nhg = (nhin + 31) / 32;
-            std::vector<int> wgrp(nslot), rgrp(nslot, -1), ent(cnt[nown]);
+            const size_t e0 = L.csr_ent.size();
+            L.csr_ent.resize(e0 + cnt[nown]);
+            for (int l = 0; l <= nown; ++l) L.csr_ptr.push_back(cnt[l]);
             std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-            for (int lt = 0; lt < ntri; ++lt)
-                for (int a = 0; a < 3; ++a) wgrp[a * ntri + lt] = (lt >> 5) * 3 + a;
-            for (int lh = 0; lh < nhin; ++lh)
-                for (int a = 0; a < 4; ++a) wgrp[3 * ntri + a * nhin + lh] = 3 * ntg + (lh >> 5) * 4 + a;
+            // slots are corner-major: triangle corner a at a*ntri + lt, hinge
+            // slot a at 3*ntri + a*nhin + lh
             for (int lt : ot)
                 for (int a = 0; a < 3; ++a) {
                     const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
-                    if (l < nown) {
-                        const int j = fill[l] - cnt[l];
-                        ent[fill[l]++] = a * ntri + lt;
-                        rgrp[a * ntri + lt] = (l >> 5) * maxdeg + j;
-                    }
+                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(a * ntri + lt);
                 }
             for (int lh : oh)
                 for (int a = 0; a < 4; ++a) {
                     const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
-                    if (l < nown) {
-                        const int j = fill[l] - cnt[l];
-                        ent[fill[l]++] = 3 * ntri + a * nhin + lh;
-                        rgrp[3 * ntri + a * nhin + lh] = (l >> 5) * maxdeg + j;
-                    }
+                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
                 }
-            std::vector<int> bank;
-            color_slots(3 * ntg + 4 * nhg, ((nown + 31) / 32) * std::max(1, maxdeg), wgrp, rgrp, bank);
-            // address = row * 32 + bank, rows filled per bank in slot order
-            std::vector<int> rows(32, 0), addr(nslot);
-            for (int e = 0; e < nslot; ++e) addr[e] = rows[bank[e]]++ * 32 + bank[e];
-            const int nslot_pad = 32 * *std::max_element(rows.begin(), rows.end());
-            if (nslot_pad > 65535) {
-                err = "patch too large for 16-bit slot addresses; lower patch_verts";
-                return false;
-            }
-            ph.nslot = nslot_pad;
-            for (int lt = 0; lt < ntri; ++lt) {
-                TriRec& r = L.tris[ph.tri_off + lt];
-                r.l2 |= (uint32_t)addr[lt] << 16;
-                r.s12 = (uint32_t)addr[ntri + lt] | ((uint32_t)addr[2 * ntri + lt] << 16);
-            }
-            for (int lh = 0; lh < nhin; ++lh) {
-                const uint32_t s0 = addr[3 * ntri + lh], s1 = addr[3 * ntri + nhin + lh];
-                const uint32_t s2 = addr[3 * ntri + 2 * nhin + lh], s3 = addr[3 * ntri + 3 * nhin + lh];
-                L.hslot.push_back(make_uint2(s0 | (s1 << 16), s2 | (s3 << 16)));
-            }
-            const size_t e0 = L.csr_ent.size();
-            L.csr_ent.resize(e0 + cnt[nown]);
-            for (int l = 0; l <= nown; ++l) L.csr_ptr.push_back(cnt[l]);
-            for (int q = 0; q < cnt[nown]; ++q) L.csr_ent[e0 + q] = (uint16_t)addr[ent[q]];
             ph.nent = cnt[nown];
             ph.nbnd = nbnd_p;
             ph.ntri_a = ntri_a;
@@ -412,11 +310,11 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.max_nent = std::max(L.max_nent, cnt[nown]);
             L.max_nhalo = std::max(L.max_nhalo, nlocal - nown);
             L.max_nlocal = std::max(L.max_nlocal, nlocal);
-            L.max_nslot = std::max(L.max_nslot, ph.nslot);
+            L.max_nslot = std::max(L.max_nslot, nslot);
             L.max_nown = std::max(L.max_nown, nown);
             L.max_ntri = std::max(L.max_ntri, ntri);
             L.max_nhinge = std::max(L.max_nhinge, nhin);
-            const size_t res = 32 * (size_t)nlocal + 12 * (size_t)ph.nslot + 4 * (size_t)(nown + 1) + 2 * (size_t)cnt[nown];
+            const size_t res = 32 * (size_t)nlocal + 12 * (size_t)nslot + 4 * (size_t)(nown + 1) + 2 * (size_t)cnt[nown];
             L.smem_resident = std::max(L.smem_resident, (res + 15) / 16 * 16);
             L.patches.push_back(ph);
         }

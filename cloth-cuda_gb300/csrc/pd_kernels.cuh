@@ -127,10 +127,8 @@ __device__ __forceinline__ float3 edge(const float4* sy, const float4* sd, int i
 }
 
 // Triangle phase for one local triangle: writes the contributions of its
-// three corners to their slots.  Slot addresses are bank-coloured by the
-// layout: the 32 slots one warp stores (32 consecutive records, one corner)
-// sit in 32 different banks, and so do the 32 slots one warp of the gather
-// loads (32 consecutive owned vertices, one list position).
+// three corners.  Slots are corner-major (corner c of local triangle lt at
+// c*ntri + lt), so a warp's stores are unit-stride and free of bank conflicts.
 // Corner contributions of one triangle from its two edge vectors:
 // c_v = h^2 wA sum_col coef_{v,col} (R - F)_col (consistent) or with R alone
 // (literal), coef from Dm_inv G = (g00, g10, g01, g11).
@@ -159,25 +157,23 @@ __device__ __forceinline__ void tri_force(float3 d1, float3 d2, float4 G, float 
     c2 = make_float3(ffma(g10, q0.x, fmul(g11, q1.x)), ffma(g10, q0.y, fmul(g11, q1.y)), ffma(g10, q0.z, fmul(g11, q1.z)));
 }
 
-// s12: the record's slots of corners 1 and 2 (passed separately so a kernel
-// that keeps records in registers can fetch this word when it stores)
 template <int MODE>
-__device__ __forceinline__ void triangle_contrib(const TriRec& r, uint32_t s12, const float4* sy, const float4* sd,
-                                                 float* cx, float* cy, float* cz)
+__device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
+                                                 int ntri, float* cx, float* cy, float* cz)
 {
-    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2 & 0xffffu;
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2;
     float3 c0, c1, c2;
     tri_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), r.G, r.h2wA, c0, c1, c2);
-    const int b0 = r.l2 >> 16, b1 = s12 & 0xffffu, b2 = s12 >> 16;
-    cx[b0] = c0.x; cy[b0] = c0.y; cz[b0] = c0.z;
+    const int b1 = ntri + lt, b2 = 2 * ntri + lt;
+    cx[lt] = c0.x; cy[lt] = c0.y; cz[lt] = c0.z;
     cx[b1] = c1.x; cy[b1] = c1.y; cz[b1] = c1.z;
     cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z;
 }
 
 // Hinge phase: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
 // n_rest <= 1e-10, src/pd_solver.cu:304-335); slot s gets h^2 k w_s (p - e)
-// (consistent) or h^2 k w_s p (literal), at the slot address the layout
-// gives corner s (hs: corners 0 | 1 << 16, 2 | 3 << 16).
+// (consistent) or h^2 k w_s p (literal).  Slot s of local hinge e sits at
+// hbase + s*nhin + e.
 // Bending "force" q of one hinge (slot s receives w_s q): e = sum w_i x_i
 // formed as sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0 from edge vectors.
 template <int MODE>
@@ -199,8 +195,8 @@ __device__ __forceinline__ float3 hinge_force(float3 e1, float3 e2, float3 e3, f
 }
 
 template <int MODE>
-__device__ __forceinline__ void hinge_contrib(const HingeRec& r, uint2 hs, const float4* sy, const float4* sd,
-                                              float* cx, float* cy, float* cz)
+__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int e_,
+                                              int hbase, int nhin, float* cx, float* cy, float* cz)
 {
     const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
     const float4 y0 = sy[i0], d0 = sd[i0];
@@ -208,7 +204,7 @@ __device__ __forceinline__ void hinge_contrib(const HingeRec& r, uint2 hs, const
     const float4 w = r.w;
     const float3 q = hinge_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), edge(sy, sd, i0, i3), x0, w,
                                        r.h2k, r.nrest);
-    const int s0 = hs.x & 0xffffu, s1 = hs.x >> 16, s2 = hs.y & 0xffffu, s3 = hs.y >> 16;
+    const int s0 = hbase + e_, s1 = s0 + nhin, s2 = s1 + nhin, s3 = s2 + nhin;
     cx[s0] = fmul(w.x, q.x); cy[s0] = fmul(w.x, q.y); cz[s0] = fmul(w.x, q.z);
     cx[s1] = fmul(w.y, q.x); cy[s1] = fmul(w.y, q.y); cz[s1] = fmul(w.y, q.z);
     cx[s2] = fmul(w.z, q.x); cy[s2] = fmul(w.z, q.y); cz[s2] = fmul(w.z, q.z);
@@ -322,13 +318,12 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     const int ntri = ph.ntri, nhin = ph.nhinge;
     for (int t = tid; t < ntri; t += NT) {
         const TriRec r = tr[t];
-        triangle_contrib<MODE>(r, r.s12, sy, sd, cx, cy, cz);
+        triangle_contrib<MODE>(r, sy, sd, t, ntri, cx, cy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;
-    const uint2* __restrict__ hsl = a.hslot + ph.hinge_off;
     for (int e = tid; e < nhin; e += NT) {
         const HingeRec r = hr[e];
-        hinge_contrib<MODE>(r, __ldg(&hsl[e]), sy, sd, cx, cy, cz);
+        hinge_contrib<MODE>(r, sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
     }
     __syncthreads();
 

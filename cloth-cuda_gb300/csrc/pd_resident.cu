@@ -97,25 +97,21 @@ constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 
 // Local step over this thread's records with list index in [t0, t1) (triangles)
 // and [e0, e1) (hinges).
-// Slot addresses are static for the frame; the hinges' and the last word of
-// each triangle record are read through L1 when the record stores rather
-// than held in registers.
 template <int MODE, int NT, int MT, int MH>
-__device__ __forceinline__ void local_records(const TriRec (&rt)[MT], const HingeRec (&rh)[MH],
-                                              const TriRec* __restrict__ tg, const uint2* __restrict__ hs,
-                                              const float4* sy, const float4* sd, int t0, int t1, int e0, int e1,
+__device__ __forceinline__ void local_records(const TriRec (&rt)[MT], const HingeRec (&rh)[MH], const float4* sy,
+                                              const float4* sd, int ntri, int nhin, int t0, int t1, int e0, int e1,
                                               float* cx, float* cy, float* cz)
 {
     const int tid = threadIdx.x;
     #pragma unroll
     for (int j = 0; j < MT; ++j) {
         const int t = tri_index<NT, MT>(tid, j);
-        if (t >= t0 && t < t1) triangle_contrib<MODE>(rt[j], __ldg(&tg[t].s12), sy, sd, cx, cy, cz);
+        if (t >= t0 && t < t1) triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
     }
     #pragma unroll
     for (int j = 0; j < MH; ++j) {
         const int e = tid + j * NT;
-        if (e >= e0 && e < e1) hinge_contrib<MODE>(rh[j], __ldg(&hs[e]), sy, sd, cx, cy, cz);
+        if (e >= e0 && e < e1) hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
     }
 }
 
@@ -194,8 +190,6 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     // lowest, so warps finish the local step together.
     TriRec rt[MT];
     HingeRec rh[MH];
-    const uint2* hs = a.hslot + ph.hinge_off;
-    const TriRec* tg = a.tris + ph.tri_off;
     if (comp) {
         #pragma unroll
         for (int j = 0; j < MT; ++j) {
@@ -281,7 +275,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // each list), then the boundary vertices, which the neighbouring
             // patches read; the signal warp publishes them while phase B runs.
             if (!skip_k)
-                local_records<MODE, NT, MT, MH>(rt, rh, tg, hs, sy, sd, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
+                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
             named_sync(1, NT);
             if (!skip_k && tid < ph.nbnd) {
                 vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
@@ -290,7 +284,8 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             named_arrive(2, NTT);
             // Phase B: the remaining records, then the interior vertices
             if (!skip_k)
-                local_records<MODE, NT, MT, MH>(rt, rh, tg, hs, sy, sd, ph.ntri_a, ntri, ph.nhin_a, nhin, cx, cy, cz);
+                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, ph.ntri_a, ntri, ph.nhin_a, nhin, cx,
+                                                cy, cz);
             named_sync(1, NT);
             if (!skip_k && own && tid >= ph.nbnd) {
                 vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
@@ -323,7 +318,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
             float r2 = 0.f;
             if (!skip_k) {
-                if (comp) local_records<MODE, NT, MT, MH>(rt, rh, tg, hs, sy, sd, 0, ntri, 0, nhin, cx, cy, cz);
+                if (comp) local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ntri, 0, nhin, cx, cy, cz);
                 __syncthreads();
                 if (own) {
                     vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);

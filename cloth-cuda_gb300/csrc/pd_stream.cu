@@ -192,9 +192,8 @@ __global__ void __launch_bounds__(NT) k_stream(IterArgs a, StreamArgs sa, int k,
             const int ntri = h.ntri, nhin = h.nhinge;
             const TriRec* tr = reinterpret_cast<const TriRec*>(st + sa.o_tri);
             const HingeRec* hr = reinterpret_cast<const HingeRec*>(st + sa.o_hin);
-            const uint2* hsl = a.hslot + h.hinge_off;
-            for (int t = tid; t < ntri; t += NT) triangle_contrib<MODE>(tr[t], tr[t].s12, sy, sd, cx, cy, cz);
-            for (int e = tid; e < nhin; e += NT) hinge_contrib<MODE>(hr[e], __ldg(&hsl[e]), sy, sd, cx, cy, cz);
+            for (int t = tid; t < ntri; t += NT) triangle_contrib<MODE>(tr[t], sy, sd, t, ntri, cx, cy, cz);
+            for (int e = tid; e < nhin; e += NT) hinge_contrib<MODE>(hr[e], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
             __syncthreads();
             const bool ro = res_only != 0 || k >= a.cinfo[h.cloth].max_iter;
             const float gamma = a.cinfo[h.cloth].gamma;

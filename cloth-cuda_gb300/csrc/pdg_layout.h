@@ -24,7 +24,7 @@ struct PatchHdr {            // 64 B
     int hinge_off, nhinge;   // into hinge_rec[]
     int csr_off;             // into csr_ptr[] (nown + 1 entries, relative to ent_off)
     int ent_off;             // into csr_ent[]
-    int nslot;               // contribution slot array length (bank-coloured, a multiple of 32)
+    int nslot;               // 3*ntri + 4*nhinge contribution slots
     int nent;                // gather-list entries of the owned vertices
     int nbnd;                // owned vertices 0..nbnd-1 are in other patches' halos
     int ntri_a, nhin_a;      // records 0..ntri_a-1 / 0..nhin_a-1 touch one of them
@@ -34,8 +34,8 @@ struct TriRec {              // 32 B
     float4   G;              // Dm_inv col-major (g00, g10, g01, g11)
     float    h2wA;           // h^2 * k_stretch * rest area
     uint32_t l01;            // local indices of corners 0 | 1 << 16
-    uint32_t l2;             // local index of corner 2 | slot of corner 0 << 16
-    uint32_t s12;            // slots of corners 1 | 2 << 16
+    uint32_t l2;             // local index of corner 2
+    float    pad;
 };
 
 struct HingeRec {            // 32 B
@@ -76,7 +76,6 @@ struct IterArgs {
     const int*       halo;
     const TriRec*    tris;
     const HingeRec*  hinges;
-    const uint2*     hslot;       // per hinge: slots of corners 0 | 1 << 16, 2 | 3 << 16
     const int*       csr_ptr;
     const uint16_t*  csr_ent;
     const ClothInfo* cinfo;

@@ -37,7 +37,6 @@ struct HostLayout {
     std::vector<int> halo;
     std::vector<TriRec> tris;
     std::vector<HingeRec> hinges;
-    std::vector<uint2> hslot;       // per hinge: its four slot addresses
     std::vector<int> csr_ptr;
     std::vector<uint16_t> csr_ent;
     std::vector<int> nbr_ptr, nbr;  // patches owning each patch's halo vertices
@@ -101,7 +100,6 @@ struct pdg_solver {
     pdg::DevBuf<pdg::PatchHdr> patches;
     pdg::DevBuf<pdg::TriRec> tris;
     pdg::DevBuf<pdg::HingeRec> hinges;
-    pdg::DevBuf<uint2> hslot;
     pdg::DevBuf<pdg::ClothInfo> cinfo;
     pdg::DevBuf<pdg::ClothRT> crt;
     pdg::DevBuf<unsigned> bar;
