@@ -291,18 +291,49 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.csr_ent.resize(e0 + cnt[nown]);
             for (int l = 0; l <= nown; ++l) L.csr_ptr.push_back(cnt[l]);
             std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-            // slots are corner-major: triangle corner a at a*ntri + lt, hinge
-            // slot a at 3*ntri + a*nhin + lh
+            // Two slot addressings hold the same contributions.  Corner-major
+            // (resident and streaming kernels, summed through the gather
+            // lists): triangle corner a at a*ntri + lt, hinge corner a at
+            // 3*ntri + a*nhin + lh.  Vertex-major (per-patch sweep kernels):
+            // contribution j of owned vertex l at j*npad + l, so a warp's
+            // gather loads are unit-stride and need no list entries; halo
+            // corners get 0xffff and store nothing.
+            int maxdeg = 0;
+            for (int l = 0; l < nown; ++l) maxdeg = std::max(maxdeg, cnt[l + 1] - cnt[l]);
+            const int npad = nown | 1;
+            const long vm_nslot = (long)std::max(1, maxdeg) * npad;
+            if (vm_nslot > 65535) {
+                err = "patch too large for 16-bit slot addresses; lower patch_verts";
+                return false;
+            }
+            std::vector<uint32_t> vm(nslot, 0xffffu);
             for (int lt : ot)
                 for (int a = 0; a < 3; ++a) {
                     const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
-                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(a * ntri + lt);
+                    if (l < nown) {
+                        vm[a * ntri + lt] = (uint32_t)((fill[l] - cnt[l]) * npad + l);
+                        L.csr_ent[e0 + fill[l]++] = (uint16_t)(a * ntri + lt);
+                    }
                 }
             for (int lh : oh)
                 for (int a = 0; a < 4; ++a) {
                     const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
-                    if (l < nown) L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
+                    if (l < nown) {
+                        vm[3 * ntri + a * nhin + lh] = (uint32_t)((fill[l] - cnt[l]) * npad + l);
+                        L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
+                    }
                 }
+            for (int lt = 0; lt < ntri; ++lt) {
+                TriRec& r = L.tris[ph.tri_off + lt];
+                r.l2 |= vm[lt] << 16;
+                r.vm12 = vm[ntri + lt] | (vm[2 * ntri + lt] << 16);
+            }
+            for (int lh = 0; lh < nhin; ++lh)
+                L.hvm.push_back(make_uint2(vm[3 * ntri + lh] | (vm[3 * ntri + nhin + lh] << 16),
+                                           vm[3 * ntri + 2 * nhin + lh] | (vm[3 * ntri + 3 * nhin + lh] << 16)));
+            ph.vm_npad = npad;
+            ph.vm_nslot = (int)vm_nslot;
+            L.max_vm_slot = std::max(L.max_vm_slot, 32 * (size_t)nlocal + 12 * (size_t)vm_nslot);
             ph.nent = cnt[nown];
             ph.nbnd = nbnd_p;
             ph.ntri_a = ntri_a;
@@ -344,7 +375,8 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.nbr_ptr.push_back((int)L.nbr.size());
         }
     }
-    L.smem_bytes = 32 * (size_t)L.max_nlocal + 12 * (size_t)L.max_nslot;   // y, d per local vertex + slots
+    // per-patch sweep kernels: y, d per local vertex and the vertex-major slots
+    L.smem_bytes = (L.max_vm_slot + 15) / 16 * 16;
     return true;
 }
 

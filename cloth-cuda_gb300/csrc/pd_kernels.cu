@@ -37,8 +37,8 @@ __global__ void __launch_bounds__(NT) k_iter(IterArgs a, int k, int res_only)
     }
     float4* sx = smem;
     float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
-    float* cy = cx + ph.nslot;
-    float* cz = cy + ph.nslot;
+    float* cy = cx + ph.vm_nslot;
+    float* cz = cy + ph.vm_nslot;
     process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, 1.f, sx, cx, cy, cz, red,
                             &skip, &omega);
 }
@@ -57,8 +57,8 @@ __global__ void __launch_bounds__(NT) k_res_eval(IterArgs a, const float4* D, in
     b.acc = a.acc + slot;
     float4* sx = smem;
     float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
-    float* cy = cx + ph.nslot;
-    float* cz = cy + ph.nslot;
+    float* cy = cx + ph.vm_nslot;
+    float* cz = cy + ph.vm_nslot;
     process_patch<kModeConsistent, NT>(b, ph, 0, true, 1.f, sx, cx, cy, cz, red);
 }
 

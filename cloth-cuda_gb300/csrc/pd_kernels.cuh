@@ -161,13 +161,28 @@ template <int MODE>
 __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
                                                  int ntri, float* cx, float* cy, float* cz)
 {
-    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2;
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2 & 0xffffu;
     float3 c0, c1, c2;
     tri_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), r.G, r.h2wA, c0, c1, c2);
     const int b1 = ntri + lt, b2 = 2 * ntri + lt;
     cx[lt] = c0.x; cy[lt] = c0.y; cz[lt] = c0.z;
     cx[b1] = c1.x; cy[b1] = c1.y; cz[b1] = c1.z;
     cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z;
+}
+
+// Vertex-major variants for the per-patch sweep kernels: the record carries
+// the slot address of each corner (0xffff for a halo corner: no store).
+template <int MODE>
+__device__ __forceinline__ void triangle_contrib_vm(const TriRec& r, const float4* sy, const float4* sd, float* cx,
+                                                    float* cy, float* cz)
+{
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2 & 0xffffu;
+    float3 c0, c1, c2;
+    tri_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), r.G, r.h2wA, c0, c1, c2);
+    const uint32_t b0 = r.l2 >> 16, b1 = r.vm12 & 0xffffu, b2 = r.vm12 >> 16;
+    if (b0 != 0xffffu) { cx[b0] = c0.x; cy[b0] = c0.y; cz[b0] = c0.z; }
+    if (b1 != 0xffffu) { cx[b1] = c1.x; cy[b1] = c1.y; cz[b1] = c1.z; }
+    if (b2 != 0xffffu) { cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z; }
 }
 
 // Hinge phase: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
@@ -209,6 +224,23 @@ __device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* s
     cx[s1] = fmul(w.y, q.x); cy[s1] = fmul(w.y, q.y); cz[s1] = fmul(w.y, q.z);
     cx[s2] = fmul(w.z, q.x); cy[s2] = fmul(w.z, q.y); cz[s2] = fmul(w.z, q.z);
     cx[s3] = fmul(w.w, q.x); cy[s3] = fmul(w.w, q.y); cz[s3] = fmul(w.w, q.z);
+}
+
+template <int MODE>
+__device__ __forceinline__ void hinge_contrib_vm(const HingeRec& r, uint2 hs, const float4* sy, const float4* sd,
+                                                 float* cx, float* cy, float* cz)
+{
+    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
+    const float4 y0 = sy[i0], d0 = sd[i0];
+    const float3 x0 = make_float3(fadd(y0.x, d0.x), fadd(y0.y, d0.y), fadd(y0.z, d0.z));
+    const float4 w = r.w;
+    const float3 q = hinge_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), edge(sy, sd, i0, i3), x0, w,
+                                       r.h2k, r.nrest);
+    const uint32_t s0 = hs.x & 0xffffu, s1 = hs.x >> 16, s2 = hs.y & 0xffffu, s3 = hs.y >> 16;
+    if (s0 != 0xffffu) { cx[s0] = fmul(w.x, q.x); cy[s0] = fmul(w.x, q.y); cz[s0] = fmul(w.x, q.z); }
+    if (s1 != 0xffffu) { cx[s1] = fmul(w.y, q.x); cy[s1] = fmul(w.y, q.y); cz[s1] = fmul(w.y, q.z); }
+    if (s2 != 0xffffu) { cx[s2] = fmul(w.z, q.x); cy[s2] = fmul(w.z, q.y); cz[s2] = fmul(w.z, q.z); }
+    if (s3 != 0xffffu) { cx[s3] = fmul(w.w, q.x); cy[s3] = fmul(w.w, q.y); cz[s3] = fmul(w.w, q.z); }
 }
 
 // Sum of the contribution slots of one owned vertex, in gather-list order.
@@ -287,7 +319,7 @@ __device__ __forceinline__ void block_residual(float r2, float* red, double* acc
 // residual.  Data produced by other blocks is loaded with __ldcg (L2, not L1),
 // so the same code is correct inside the persistent kernel between grid
 // barriers.  Shared memory: sy, sd (float4 per local vertex), then the three
-// slot arrays.
+// slot arrays in vertex-major order (ph.vm_nslot each).
 // ---------------------------------------------------------------------------
 template <int MODE, int NT>
 __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr& ph, int k, bool res_only,
@@ -318,22 +350,29 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     const int ntri = ph.ntri, nhin = ph.nhinge;
     for (int t = tid; t < ntri; t += NT) {
         const TriRec r = tr[t];
-        triangle_contrib<MODE>(r, sy, sd, t, ntri, cx, cy, cz);
+        triangle_contrib_vm<MODE>(r, sy, sd, cx, cy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;
+    const uint2* __restrict__ hv = a.hvm + ph.hinge_off;
     for (int e = tid; e < nhin; e += NT) {
         const HingeRec r = hr[e];
-        hinge_contrib<MODE>(r, sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
+        hinge_contrib_vm<MODE>(r, __ldg(&hv[e]), sy, sd, cx, cy, cz);
     }
     __syncthreads();
 
     // 3. global step per owned vertex
     const float gamma = a.cinfo[ph.cloth].gamma;
     const int* __restrict__ cp = a.csr_ptr + ph.csr_off;
-    const uint16_t* __restrict__ ce = a.csr_ent + ph.ent_off;
+    const int npad = ph.vm_npad;
     float r2 = 0.f;
     for (int l = tid; l < ph.nown; l += NT) {
-        const float3 f = gather_slots(ce, __ldg(&cp[l]), __ldg(&cp[l + 1]), cx, cy, cz);
+        // contributions j = 0..deg-1 of vertex l, in gather-list order
+        const int deg = __ldg(&cp[l + 1]) - __ldg(&cp[l]);
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int j = 0, s = l; j < deg; ++j, s += npad) {
+            fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
+        }
+        const float3 f = make_float3(fx, fy, fz);
         const int g = ph.vbegin + l;
         const float4 d = sd[l];
         const float4 y = sy[l];

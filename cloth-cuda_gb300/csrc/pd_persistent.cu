@@ -71,8 +71,8 @@ __global__ void __launch_bounds__(NT) k_persistent(PersistArgs p)
             if (!skip) {
                 float4* sx = smem;
                 float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
-                float* cy = cx + ph.nslot;
-                float* cz = cy + ph.nslot;
+                float* cy = cx + ph.vm_nslot;
+                float* cz = cy + ph.vm_nslot;
                 process_patch<MODE, NT>(a, ph, k, res_only || k >= a.cinfo[ph.cloth].max_iter, omega,
                                         sx, cx, cy, cz, red);
             }

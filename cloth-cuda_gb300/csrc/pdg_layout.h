@@ -14,7 +14,7 @@
 
 namespace pdg {
 
-struct PatchHdr {            // 64 B
+struct PatchHdr {            // 80 B
     int cloth;               // cloth index
     int vbegin;              // first owned vertex (global, reordered)
     int nown;                // owned vertices
@@ -28,14 +28,17 @@ struct PatchHdr {            // 64 B
     int nent;                // gather-list entries of the owned vertices
     int nbnd;                // owned vertices 0..nbnd-1 are in other patches' halos
     int ntri_a, nhin_a;      // records 0..ntri_a-1 / 0..nhin_a-1 touch one of them
+    int vm_npad;             // vertex-major slots: contribution j of owned vertex l at j*vm_npad + l
+    int vm_nslot;            // vertex-major slot array length
+    int pad[2];
 };
 
 struct TriRec {              // 32 B
     float4   G;              // Dm_inv col-major (g00, g10, g01, g11)
     float    h2wA;           // h^2 * k_stretch * rest area
     uint32_t l01;            // local indices of corners 0 | 1 << 16
-    uint32_t l2;             // local index of corner 2
-    float    pad;
+    uint32_t l2;             // local index of corner 2 | vertex-major slot of corner 0 << 16
+    uint32_t vm12;           // vertex-major slots of corners 1 | 2 << 16 (0xffff: halo corner)
 };
 
 struct HingeRec {            // 32 B
@@ -76,6 +79,7 @@ struct IterArgs {
     const int*       halo;
     const TriRec*    tris;
     const HingeRec*  hinges;
+    const uint2*     hvm;         // per hinge: vertex-major slots of corners 0 | 1 << 16, 2 | 3 << 16
     const int*       csr_ptr;
     const uint16_t*  csr_ent;
     const ClothInfo* cinfo;

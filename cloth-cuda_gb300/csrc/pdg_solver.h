@@ -24,7 +24,8 @@ struct ClothSetup {
 struct HostLayout {
     int ntot = 0, ncloth = 0, npatch = 0, cap = 0, omega_stride = 1;
     int max_nlocal = 0, max_nslot = 0, max_nown = 0, max_ntri = 0, max_nhinge = 0, max_nent = 0, max_nhalo = 0;
-    size_t smem_bytes = 0;          // per-sweep kernels
+    size_t smem_bytes = 0;          // per-patch sweep kernels (vertex-major slots)
+    size_t max_vm_slot = 0;         // largest 32*nlocal + 12*vm_nslot of a patch
     size_t smem_resident = 0;       // resident kernel: + gather lists
     std::vector<int> perm_global;   // reordered vertex -> index in the batch's caller order
     std::vector<int> perm_local;    // reordered vertex -> index within its cloth
@@ -37,6 +38,7 @@ struct HostLayout {
     std::vector<int> halo;
     std::vector<TriRec> tris;
     std::vector<HingeRec> hinges;
+    std::vector<uint2> hvm;         // per hinge: its vertex-major slot addresses
     std::vector<int> csr_ptr;
     std::vector<uint16_t> csr_ent;
     std::vector<int> nbr_ptr, nbr;  // patches owning each patch's halo vertices
@@ -100,6 +102,7 @@ struct pdg_solver {
     pdg::DevBuf<pdg::PatchHdr> patches;
     pdg::DevBuf<pdg::TriRec> tris;
     pdg::DevBuf<pdg::HingeRec> hinges;
+    pdg::DevBuf<uint2> hvm;
     pdg::DevBuf<pdg::ClothInfo> cinfo;
     pdg::DevBuf<pdg::ClothRT> crt;
     pdg::DevBuf<unsigned> bar;

@@ -59,6 +59,7 @@ int upload_all(pdg_solver* s)
     CK(s->patches.upload(L.patches, st));
     CK(s->tris.upload(L.tris, st));
     CK(s->hinges.upload(L.hinges, st));
+    CK(s->hvm.upload(L.hvm, st));
     CK(s->cinfo.upload(L.cinfo, st));
     CK(s->nbr_ptr.upload(L.nbr_ptr, st));
     CK(s->nbr.upload(L.nbr, st));
@@ -92,7 +93,7 @@ int upload_all(pdg_solver* s)
 IterArgs iter_args(pdg_solver* s)
 {
     IterArgs a;
-    a.patches = s->patches.p; a.halo = s->halo.p; a.tris = s->tris.p; a.hinges = s->hinges.p;
+    a.patches = s->patches.p; a.halo = s->halo.p; a.tris = s->tris.p; a.hinges = s->hinges.p; a.hvm = s->hvm.p;
     a.csr_ptr = s->csr_ptr.p; a.csr_ent = s->csr_ent.p; a.cinfo = s->cinfo.p; a.crt = s->crt.p;
     a.omega = s->omega.p; a.omega_stride = s->L.omega_stride;
     a.Y = s->Y.p; a.buf[0] = s->A.p; a.buf[1] = s->B.p; a.ncloth = s->L.ncloth;
