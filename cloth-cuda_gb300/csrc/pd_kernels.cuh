@@ -170,18 +170,16 @@ __device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* 
     cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z;
 }
 
-// Vertex-major variants: the record carries the slot address of each corner
-// (0xffff for a halo corner: no store).  vm12, the record's last word, is
-// passed separately so a kernel holding records in registers can fetch it
-// when it stores.
+// Vertex-major variants for the per-patch sweep kernels: the record carries
+// the slot address of each corner (0xffff for a halo corner: no store).
 template <int MODE>
-__device__ __forceinline__ void triangle_contrib_vm(const TriRec& r, uint32_t vm12, const float4* sy,
-                                                    const float4* sd, float* cx, float* cy, float* cz)
+__device__ __forceinline__ void triangle_contrib_vm(const TriRec& r, const float4* sy, const float4* sd, float* cx,
+                                                    float* cy, float* cz)
 {
     const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2 & 0xffffu;
     float3 c0, c1, c2;
     tri_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), r.G, r.h2wA, c0, c1, c2);
-    const uint32_t b0 = r.l2 >> 16, b1 = vm12 & 0xffffu, b2 = vm12 >> 16;
+    const uint32_t b0 = r.l2 >> 16, b1 = r.vm12 & 0xffffu, b2 = r.vm12 >> 16;
     if (b0 != 0xffffu) { cx[b0] = c0.x; cy[b0] = c0.y; cz[b0] = c0.z; }
     if (b1 != 0xffffu) { cx[b1] = c1.x; cy[b1] = c1.y; cz[b1] = c1.z; }
     if (b2 != 0xffffu) { cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z; }
@@ -352,7 +350,7 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     const int ntri = ph.ntri, nhin = ph.nhinge;
     for (int t = tid; t < ntri; t += NT) {
         const TriRec r = tr[t];
-        triangle_contrib_vm<MODE>(r, r.vm12, sy, sd, cx, cy, cz);
+        triangle_contrib_vm<MODE>(r, sy, sd, cx, cy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;
     const uint2* __restrict__ hv = a.hvm + ph.hinge_off;

@@ -97,40 +97,31 @@ constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 
 // Local step over this thread's records with list index in [t0, t1) (triangles)
 // and [e0, e1) (hinges).
-// Records write to vertex-major slots.  The slot addresses are static for
-// the frame: the hinges' and the last word of each triangle record are read
-// through L1 when the record stores rather than held in registers.
 template <int MODE, int NT, int MT, int MH>
-__device__ __forceinline__ void local_records(const TriRec (&rt)[MT], const HingeRec (&rh)[MH],
-                                              const TriRec* __restrict__ tg, const uint2* __restrict__ hv,
-                                              const float4* sy, const float4* sd, int t0, int t1, int e0, int e1,
+__device__ __forceinline__ void local_records(const TriRec (&rt)[MT], const HingeRec (&rh)[MH], const float4* sy,
+                                              const float4* sd, int ntri, int nhin, int t0, int t1, int e0, int e1,
                                               float* cx, float* cy, float* cz)
 {
     const int tid = threadIdx.x;
     #pragma unroll
     for (int j = 0; j < MT; ++j) {
         const int t = tri_index<NT, MT>(tid, j);
-        if (t >= t0 && t < t1) triangle_contrib_vm<MODE>(rt[j], __ldg(&tg[t].vm12), sy, sd, cx, cy, cz);
+        if (t >= t0 && t < t1) triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
     }
     #pragma unroll
     for (int j = 0; j < MH; ++j) {
         const int e = tid + j * NT;
-        if (e >= e0 && e < e1) hinge_contrib_vm<MODE>(rh[j], __ldg(&hv[e]), sy, sd, cx, cy, cz);
+        if (e >= e0 && e < e1) hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
     }
 }
 
-// Gather (vertex-major slots: contribution j of vertex l at j*npad + l) and
-// Jacobi update of owned vertex l: o = d^(k+1), d = d^k.
+// Gather and Jacobi update of owned vertex l: o = d^(k+1), d = d^k.
 template <int MODE>
-__device__ __forceinline__ void vertex_update(int deg, int npad, int l, const float4* sy, const float4* sd,
-                                              const float* cx, const float* cy, const float* cz, float4 dprev,
-                                              float gamma, float omega, float4& o, float4& d, float& r2)
+__device__ __forceinline__ void vertex_update(const uint16_t* sent, const int* sptr, int l, const float4* sy,
+                                              const float4* sd, const float* cx, const float* cy, const float* cz,
+                                              float4 dprev, float gamma, float omega, float4& o, float4& d, float& r2)
 {
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int j = 0, s = l; j < deg; ++j, s += npad) {
-        fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
-    }
-    const float3 f = make_float3(fx, fy, fz);
+    const float3 f = gather_slots(sent, sptr[l], sptr[l + 1], cx, cy, cz);
     d = sd[l];
     const float4 y = sy[l];
     if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega, r2);
@@ -189,8 +180,10 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     float4* sy = smem;
     float4* sd = sy + nlocal;
     float* cx = reinterpret_cast<float*>(sd + nlocal);
-    float* cy = cx + ph.vm_nslot;
-    float* cz = cy + ph.vm_nslot;
+    float* cy = cx + ph.nslot;
+    float* cz = cy + ph.nslot;
+    int* sptr = reinterpret_cast<int*>(cz + ph.nslot);
+    uint16_t* sent = reinterpret_cast<uint16_t*>(sptr + nown + 1);
 
     // records in registers for the whole frame.  The partial last round of
     // triangles goes to the highest threads and that of hinges to the
@@ -209,13 +202,12 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             if (e < nhin) rh[j] = a.hinges[ph.hinge_off + e];
         }
     }
-    // Chebyshev weights in shared memory; each owned vertex's contribution
-    // count in a register
+    // gather lists and Chebyshev weights in shared memory
+    for (int l = tid; l <= nown; l += NTT) sptr[l] = a.csr_ptr[ph.csr_off + l];
     for (int k = tid; k < a.omega_stride && k < kResOmega; k += NTT) som[k] = a.omega[ph.cloth * a.omega_stride + k];
-    const int deg = tid < nown ? a.csr_ptr[ph.csr_off + tid + 1] - a.csr_ptr[ph.csr_off + tid] : 0;
-    const int npad = ph.vm_npad;
-    const uint2* hv = a.hvm + ph.hinge_off;
-    const TriRec* tg = a.tris + ph.tri_off;
+    __syncthreads();
+    const int nent = sptr[nown];
+    for (int q = tid; q < nent; q += NTT) sent[q] = a.csr_ent[ph.ent_off + q];
 
     // predict the owned vertices; the cloth's first block resets its record
     const int c = ph.cloth;
@@ -283,19 +275,20 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // each list), then the boundary vertices, which the neighbouring
             // patches read; the signal warp publishes them while phase B runs.
             if (!skip_k)
-                local_records<MODE, NT, MT, MH>(rt, rh, tg, hv, sy, sd, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
+                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
             named_sync(1, NT);
             if (!skip_k && tid < ph.nbnd) {
-                vertex_update<MODE>(deg, npad, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             named_arrive(2, NTT);
             // Phase B: the remaining records, then the interior vertices
             if (!skip_k)
-                local_records<MODE, NT, MT, MH>(rt, rh, tg, hv, sy, sd, ph.ntri_a, ntri, ph.nhin_a, nhin, cx, cy, cz);
+                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, ph.ntri_a, ntri, ph.nhin_a, nhin, cx,
+                                                cy, cz);
             named_sync(1, NT);
             if (!skip_k && own && tid >= ph.nbnd) {
-                vertex_update<MODE>(deg, npad, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             // every record has read d^k: the owned offsets move on
@@ -325,10 +318,10 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
             float r2 = 0.f;
             if (!skip_k) {
-                if (comp) local_records<MODE, NT, MT, MH>(rt, rh, tg, hv, sy, sd, 0, ntri, 0, nhin, cx, cy, cz);
+                if (comp) local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ntri, 0, nhin, cx, cy, cz);
                 __syncthreads();
                 if (own) {
-                    vertex_update<MODE>(deg, npad, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                    vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                     if (!res_only) {
                         ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
                         sd[tid] = o;
