@@ -333,15 +333,6 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     float4* __restrict__ Dn = (k & 1) ? a.buf[0] : a.buf[1];
     float4* sd = sy + ph.nlocal;
     const int tid = threadIdx.x;
-    const int* __restrict__ cp = a.csr_ptr + ph.csr_off;
-    // the contribution count and d^(k-1) of this thread's first owned vertex,
-    // fetched with the staging instead of when the gather needs them
-    int deg0 = 0;
-    float4 dp0 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (tid < ph.nown) {
-        deg0 = __ldg(&cp[tid + 1]) - __ldg(&cp[tid]);
-        if (MODE == kModeConsistent && !res_only) dp0 = __ldcg(&Dn[ph.vbegin + tid]);
-    }
 
     // 1. stage y and d^k of owned + halo vertices
     for (int l = tid; l < ph.nlocal; l += NT) {
@@ -371,11 +362,12 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
 
     // 3. global step per owned vertex
     const float gamma = a.cinfo[ph.cloth].gamma;
+    const int* __restrict__ cp = a.csr_ptr + ph.csr_off;
     const int npad = ph.vm_npad;
     float r2 = 0.f;
     for (int l = tid; l < ph.nown; l += NT) {
         // contributions j = 0..deg-1 of vertex l, in gather-list order
-        const int deg = l == tid ? deg0 : __ldg(&cp[l + 1]) - __ldg(&cp[l]);
+        const int deg = __ldg(&cp[l + 1]) - __ldg(&cp[l]);
         float fx = 0.f, fy = 0.f, fz = 0.f;
         for (int j = 0, s = l; j < deg; ++j, s += npad) {
             fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
@@ -386,7 +378,7 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
         const float4 y = sy[l];
         if (MODE == kModeConsistent) {
             float rv;
-            const float4 dp = res_only ? d : (l == tid ? dp0 : __ldcg(&Dn[g]));
+            const float4 dp = res_only ? d : __ldcg(&Dn[g]);
             const float4 o = update_consistent(d, y, f, dp, gamma, omega, rv);
             r2 += rv;
             if (!res_only) Dn[g] = o;
