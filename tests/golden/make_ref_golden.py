@@ -1,6 +1,9 @@
 """Record golden vectors of the reference's own CUDA step (run on a GPU machine).
 
-    python tests/golden/make_ref_golden.py
+    python tests/golden/make_ref_golden.py [out_dir] [--missing]
+
+With --missing only the cases whose fixture is not in tests/golden yet are
+recorded.
 
 For each case the reference kernels of src/pd_solver.cu (compiled for sm_103a
 into oracle/_ref/pd_solver_ref.cubin, launched by oracle/ref_harness.c in the
@@ -33,6 +36,9 @@ CASES = {
     # 10x10 type-3 grid, cell 0.1, stretch 100, bend 1, corners pinned, dt 0.01
     "grid10t3_s1": (("grid", 10, 0.1, 3), dict(ks=100.0, kb=1.0, h=0.01, g=-9.8, damping=0.0), 1, 0.0),
     "grid10t3_pert_s1": (("grid", 10, 0.1, 3), dict(ks=100.0, kb=1.0, h=0.01, g=-9.8, damping=0.2), 1, 0.005),
+    # the 33x33 hanging cloth of the small benchmark workload (1,089 vertices)
+    "hang33_rest_s1": (("hang", 33, 1.0), dict(ks=1e3, kb=1e-2, h=1 / 60, g=-9.81, damping=0.0), 1, 0.0),
+    "hang33_pert_s1": (("hang", 33, 1.0), dict(ks=1e3, kb=1e-2, h=1 / 60, g=-9.81, damping=0.0), 1, 0.01),
 }
 
 
@@ -61,11 +67,13 @@ def start_state(sc, pos, pert, seed=1):
     return x, v
 
 
-def main(out_dir=HERE):
+def main(out_dir=HERE, missing_only=False):
     if not ref_kernels.available():
         raise SystemExit("reference kernels unavailable (oracle/_ref/pd_solver_ref.cubin or the harness missing)")
     os.makedirs(out_dir, exist_ok=True)
     for name, (mesh, p, sweeps, pert) in CASES.items():
+        if missing_only and os.path.exists(os.path.join(HERE, "ref_%s.npz" % name)):
+            continue
         sc, pos = make_scene(mesh, p)
         x0, v0 = start_state(sc, pos, pert)
         x1, v1 = ref_kernels.ref_step(sc, x0, v0, sweeps)
@@ -76,4 +84,5 @@ def main(out_dir=HERE):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else HERE)
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(args[0] if args else HERE, missing_only="--missing" in sys.argv)
