@@ -71,7 +71,8 @@ __global__ void k_select_cloth(IterArgs a, int slot_y, int slot_w)
     const double r2y = a.acc[(size_t)c * a.acc_stride + slot_y];
     const double r2w = a.acc[(size_t)c * a.acc_stride + slot_w];
     ClothRT& rt = a.crt[c];
-    rt.warm = (a.cinfo[c].init == 2 && isfinite(r2w) && r2w < r2y) ? 1 : 0;
+    const int init = a.cinfo[c].init;
+    rt.warm = ((init == 2 && r2w < r2y) || init == 3) && isfinite(r2w) ? 1 : 0;
     rt.res_y2 = r2y;
 }
 

@@ -406,7 +406,7 @@ __device__ __forceinline__ bool cloth_done(const IterArgs& a, int c, int k, bool
         // normaliser: the residual of the inertial start, measured by the
         // warm-start selection when a learned start was evaluated, else the
         // residual of the start iterate itself
-        const bool own_start = !(ci.init == 2 && a.warm_active);
+        const bool own_start = !(ci.init >= 2 && a.warm_active);
         const double ry2 = (k == 1 && own_start) ? acc0 : __ldcg(&rt->res_y2);
         if (k == 1 && designated) {
             rt->res0_2 = acc0;
@@ -464,7 +464,7 @@ __device__ __forceinline__ void predict_vertex(int i, const float4* X, const flo
     float4 s;
     if (au.w < 0.f)                    s = make_float4(fsub(au.x, y.x), fsub(au.y, y.y), fsub(au.z, y.z), au.w);
     else if (ci.init == 1)             s = make_float4(fsub(x.x, y.x), fsub(x.y, y.y), fsub(x.z, y.z), au.w);
-    else if (ci.init == 2 && warm) {   const float4 w = __ldcg(&warm[i]); s = make_float4(w.x, w.y, w.z, au.w); }
+    else if (ci.init >= 2 && warm) {   const float4 w = __ldcg(&warm[i]); s = make_float4(w.x, w.y, w.z, au.w); }
     else                               s = make_float4(0.f, 0.f, 0.f, au.w);
     A[i] = s;
     B[i] = s;
@@ -480,7 +480,7 @@ __device__ __forceinline__ void frame_stats_cloth(const IterArgs& a, int c)
     const double* acc = a.acc + (size_t)c * a.acc_stride;
     if (ci.mode == kModeConsistent) {
         rt->res0_2 = __ldcg(&acc[0]);
-        if (!(ci.init == 2 && a.warm_active)) rt->res_y2 = rt->res0_2;
+        if (!(ci.init >= 2 && a.warm_active)) rt->res_y2 = rt->res0_2;
     }
     if (__ldcg(&rt->active)) {
         rt->used = ci.max_iter;

@@ -111,7 +111,7 @@ struct pdg_solver {
     std::vector<pdg::ClothRT> h_rt;
     bool warm_valid = false;
     pdg_warmstart* ws = nullptr;   // attached learned warm start (not owned)
-    bool any_warm = false;         // some cloth asks for PDG_INIT_WARMSTART
+    bool any_warm = false;         // some cloth asks for a learned start
     std::vector<pdg_tune_entry> tune;   // autotuner candidate table
 
     ~pdg_solver();

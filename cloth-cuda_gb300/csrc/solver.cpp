@@ -37,7 +37,7 @@ int check_cfg(const pdg_config& c, int i)
     if (c.cheb_delay < 0) return set_error(PDG_ERR_ARG, "cloth %d: cheb_delay must be >= 0", i);
     if (c.mode != PDG_MODE_CONSISTENT && c.mode != PDG_MODE_REFERENCE_LITERAL)
         return set_error(PDG_ERR_ARG, "cloth %d: unknown mode", i);
-    if (c.init < 0 || c.init > 2) return set_error(PDG_ERR_ARG, "cloth %d: unknown init", i);
+    if (c.init < 0 || c.init > 3) return set_error(PDG_ERR_ARG, "cloth %d: unknown init", i);
     if (!std::isfinite(c.gravity) || !std::isfinite(c.wind[0]) || !std::isfinite(c.wind[1]) || !std::isfinite(c.wind[2]))
         return set_error(PDG_ERR_ARG, "cloth %d: non-finite acceleration", i);
     return PDG_OK;
@@ -197,7 +197,8 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     if (c0.kernel < PDG_KERNEL_AUTO || (c0.kernel > PDG_KERNEL_RESIDENT && c0.kernel != PDG_KERNEL_STREAM))
         return set_error(PDG_ERR_ARG, "unknown kernel");
     s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_GRAPH : c0.kernel;
-    for (const auto& c : s->cloths) s->any_warm = s->any_warm || c.cfg.init == PDG_INIT_WARMSTART;
+    for (const auto& c : s->cloths)
+        s->any_warm = s->any_warm || c.cfg.init == PDG_INIT_WARMSTART || c.cfg.init == PDG_INIT_WARMSTART_KEEP;
     if (s->any_warm && (c0.kernel == PDG_KERNEL_PERSISTENT || c0.kernel == PDG_KERNEL_RESIDENT))
         return set_error(PDG_ERR_ARG, "the learned warm start runs with the per-sweep (graph) kernels only");
 

@@ -60,7 +60,7 @@ std::string problem_key(int n, const pdg_config* cfgs, const pdg_mesh* const* me
         nt += meshes[i]->data->T;
         cap = std::max(cap, cfgs[i].max_iterations);
         tol |= cfgs[i].tolerance > 0.f;
-        warm |= cfgs[i].init == PDG_INIT_WARMSTART;
+        warm |= cfgs[i].init == PDG_INIT_WARMSTART || cfgs[i].init == PDG_INIT_WARMSTART_KEEP;
         final_res |= cfgs[i].compute_final_residual;
     }
     char buf[512];
@@ -124,7 +124,8 @@ int autotune_create(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes
         }
     }
     bool warm = false;
-    for (int i = 0; i < n; ++i) warm = warm || cfgs[i].init == PDG_INIT_WARMSTART;
+    for (int i = 0; i < n; ++i)
+        warm = warm || cfgs[i].init == PDG_INIT_WARMSTART || cfgs[i].init == PDG_INIT_WARMSTART_KEEP;
 
     std::vector<pdg_tune_entry> table;
     int best = -1;

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(HERE, "libpdg.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_STATE, ERR_TIMEOUT, ERR_NUMERIC, ERR_IO = 0, -1, -2, -3, -4, -5, -6, -7
 MODE_CONSISTENT, MODE_REFERENCE_LITERAL = 0, 1
-INIT_INERTIAL, INIT_PREVIOUS, INIT_WARMSTART = 0, 1, 2
+INIT_INERTIAL, INIT_PREVIOUS, INIT_WARMSTART, INIT_WARMSTART_KEEP = 0, 1, 2, 3
 KERNEL_AUTO, KERNEL_GRAPH, KERNEL_PERSISTENT, KERNEL_RESIDENT, KERNEL_AUTOTUNE, KERNEL_STREAM = 0, 1, 2, 3, 4, 5
 
 

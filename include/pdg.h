@@ -42,6 +42,8 @@ extern "C" {
 #define PDG_INIT_PREVIOUS 1   /* x_n (what src/pd_solver.cu:528 does)      */
 #define PDG_INIT_WARMSTART 2  /* the learned prediction, kept only if its
                                  residual is below the inertial start's     */
+#define PDG_INIT_WARMSTART_KEEP 3  /* the learned prediction, always kept (no
+                                 residual judge; for evaluating the network) */
 
 /* Launch structure of the iteration loop. */
 #define PDG_KERNEL_AUTO       0  /* resident when it fits, else graph (no timing) */
@@ -249,7 +251,8 @@ void pdg_autotune_clear_cache(void);
  * the converged position from the inertial prediction.  Attached to a solver
  * whose cloths use cfg.init = PDG_INIT_WARMSTART, every frame evaluates the
  * prediction and the inertial start and keeps, per cloth, the one with the
- * lower residual (plain PD remains the fallback).  Parameter layout: see
+ * lower residual (plain PD remains the fallback); PDG_INIT_WARMSTART_KEEP
+ * always keeps the prediction.  Parameter layout: see
  * pdg_warmstart_get_params (We[64][10] be[64] {A[64][64] B[64][64] C[64][4]
  * c[64] U[64][128] u[64]} x 2 Wd[3][64] bd[3], fp32). */
 int  pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out);
@@ -266,7 +269,7 @@ int  pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr,
 /* One Adam step (beta 0.9/0.999) with the gradients of the last eval/train. */
 int  pdg_warmstart_adam_step(pdg_warmstart* w, float lr);
 /* Bind to a solver (per-sweep kernels); its frames then use the prediction
- * for cloths with cfg.init == PDG_INIT_WARMSTART. */
+ * for cloths with cfg.init == PDG_INIT_WARMSTART or _KEEP. */
 int  pdg_warmstart_attach(pdg_warmstart* w, pdg_solver* s);
 /* Training on data the solver generates: one frame of `s` from its current
  * state, then one Adam step (lr > 0) on (x_n, v_n, y) -> (x_{n+1} - y). */
