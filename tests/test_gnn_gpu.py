@@ -115,3 +115,18 @@ def test_training_on_solver_data_beats_inertial_start_and_never_hurts(pdg):
     assert all(r <= 1.0 + 1e-6 for r in ratio)   # never worse than the inertial start
     for s_ in st:   # kept exactly when its residual is lower
         assert (s_["warm_start_used"] == 1) == (s_["res_initial"] < s_["res_inertial"] * (1 - 1e-7))
+
+
+def test_keep_mode_always_uses_the_learned_start(pdg):
+    # PDG_INIT_WARMSTART_KEEP skips the residual judge: every cloth starts
+    # from the prediction, and its start residual is reported as such
+    import scenes
+    ms, cs, cfgs, _ = scenes.batch(4, seed=11, max_iterations=20, tolerance=0.0, n_range=(17, 25),
+                                   kernel=pdg.KERNEL_GRAPH, init=pdg.INIT_WARMSTART_KEEP)
+    s = pdg.Solver(cfgs, ms, cs)
+    w = pdg.WarmStart(seed=0)
+    w.attach(s)
+    for _ in range(2):
+        st = s.step(1)
+    assert all(x["warm_start_used"] == 1 for x in st)
+    assert all(np.isfinite(x["res_initial"]) and x["status"] == 0 for x in st)
