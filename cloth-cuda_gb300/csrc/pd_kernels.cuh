@@ -248,10 +248,7 @@ template <class IDX>
 __device__ __forceinline__ float3 gather_slots(const IDX* ent, int b, int e, const float* cx, const float* cy,
                                                const float* cz)
 {
-    // unrolled so several entries' loads are in flight; the sums keep the
-    // list order
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    #pragma unroll 4
     for (int q = b; q < e; ++q) {
         const int s = ent[q];
         fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
