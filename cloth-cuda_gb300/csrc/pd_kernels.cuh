@@ -243,7 +243,7 @@ __device__ __forceinline__ void hinge_contrib_vm(const HingeRec& r, uint2 hs, co
     if (s3 != 0xffffu) { cx[s3] = fmul(w.w, q.x); cy[s3] = fmul(w.w, q.y); cz[s3] = fmul(w.w, q.z); }
 }
 
-// Sum of the contribution slots of one owned vertex, in gather-list order.
+// Sum of the contribution slots of list entries [b, e), in list order.
 template <class IDX>
 __device__ __forceinline__ float3 gather_slots(const IDX* ent, int b, int e, const float* cx, const float* cy,
                                                const float* cz)
@@ -251,6 +251,33 @@ __device__ __forceinline__ float3 gather_slots(const IDX* ent, int b, int e, con
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for (int q = b; q < e; ++q) {
         const int s = ent[q];
+        fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
+    }
+    return make_float3(fx, fy, fz);
+}
+
+// The force on an owned vertex is defined as (sum of the first half of its
+// list) + (sum of the second half), the first half holding ceil(deg/2)
+// entries, each half in list order.  Every kernel forms exactly this, so
+// one that gives the two halves to two threads produces the same bits.
+__device__ __forceinline__ int gather_half(int deg) { return (deg + 1) >> 1; }
+__device__ __forceinline__ float3 fadd3(float3 a, float3 b)
+{
+    return make_float3(fadd(a.x, b.x), fadd(a.y, b.y), fadd(a.z, b.z));
+}
+template <class IDX>
+__device__ __forceinline__ float3 gather_force(const IDX* ent, int b, int e, const float* cx, const float* cy,
+                                               const float* cz)
+{
+    const int h = b + gather_half(e - b);
+    return fadd3(gather_slots(ent, b, h, cx, cy, cz), gather_slots(ent, h, e, cx, cy, cz));
+}
+// vertex-major slots: contribution j of vertex l at j*npad + l
+__device__ __forceinline__ float3 gather_vm(int l, int j0, int j1, int npad, const float* cx, const float* cy,
+                                            const float* cz)
+{
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int j = j0, s = j0 * npad + l; j < j1; ++j, s += npad) {
         fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
     }
     return make_float3(fx, fy, fz);
@@ -366,13 +393,10 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     const int npad = ph.vm_npad;
     float r2 = 0.f;
     for (int l = tid; l < ph.nown; l += NT) {
-        // contributions j = 0..deg-1 of vertex l, in gather-list order
+        // contributions j = 0..deg-1 of vertex l: first half + second half
         const int deg = __ldg(&cp[l + 1]) - __ldg(&cp[l]);
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        for (int j = 0, s = l; j < deg; ++j, s += npad) {
-            fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
-        }
-        const float3 f = make_float3(fx, fy, fz);
+        const int h = gather_half(deg);
+        const float3 f = fadd3(gather_vm(l, 0, h, npad, cx, cy, cz), gather_vm(l, h, deg, npad, cx, cy, cz));
         const int g = ph.vbegin + l;
         const float4 d = sd[l];
         const float4 y = sy[l];

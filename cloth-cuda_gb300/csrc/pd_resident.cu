@@ -115,17 +115,25 @@ __device__ __forceinline__ void local_records(const TriRec (&rt)[MT], const Hing
     }
 }
 
-// Gather and Jacobi update of owned vertex l: o = d^(k+1), d = d^k.
+// Jacobi update of owned vertex l with force f: o = d^(k+1), d = d^k.
+template <int MODE>
+__device__ __forceinline__ void vertex_update_f(float3 f, int l, const float4* sy, const float4* sd, float4 dprev,
+                                                float gamma, float omega, float4& o, float4& d, float& r2)
+{
+    d = sd[l];
+    const float4 y = sy[l];
+    if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega, r2);
+    else                         o = update_literal(d, y, f);
+}
+
+// Gather by one thread and update.
 template <int MODE>
 __device__ __forceinline__ void vertex_update(const uint16_t* sent, const int* sptr, int l, const float4* sy,
                                               const float4* sd, const float* cx, const float* cy, const float* cz,
                                               float4 dprev, float gamma, float omega, float4& o, float4& d, float& r2)
 {
-    const float3 f = gather_slots(sent, sptr[l], sptr[l + 1], cx, cy, cz);
-    d = sd[l];
-    const float4 y = sy[l];
-    if (MODE == kModeConsistent) o = update_consistent(d, y, f, dprev, gamma, omega, r2);
-    else                         o = update_literal(d, y, f);
+    vertex_update_f<MODE>(gather_force(sent, sptr[l], sptr[l + 1], cx, cy, cz), l, sy, sd, dprev, gamma, omega, o,
+                          d, r2);
 }
 
 // Block sum of r2 over the NT compute threads (named barrier 1), added to
@@ -170,6 +178,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     __shared__ float red[NTT / 32];
     __shared__ int skip;
     __shared__ int sig_ok;
+    __shared__ float3 part[NT / 2];   // second halves of the boundary vertices' sums
     __shared__ float som[kResOmega];   // Chebyshev weights of this cloth
     const IterArgs& a = p.it;
     const int tid = threadIdx.x;
@@ -255,6 +264,10 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
         }
     } else if (nbr) {
         // ---- compute threads, neighbour synchronisation ----
+        // helpers for the boundary sums: the warps right after the boundary
+        // warps, when the block has that many
+        const int hb = 32 * ((ph.nbnd + 31) / 32);
+        const bool split_a = ph.nbnd > 0 && 2 * hb <= NT;
         for (int k = 0; k < nsweep; ++k) {
             if (k > 0) {   // the neighbours' d^k: wait for the signal warp, then load the halo
                 named_sync(3, NTT);
@@ -270,6 +283,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 k < a.omega_stride ? (k < kResOmega ? som[k] : a.omega[c * a.omega_stride + k]) : 1.f;
             const bool res_only = k >= ci.max_iter;
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
+            float3 p1 = make_float3(0.f, 0.f, 0.f);
             float r2 = 0.f;
             // Phase A: the records through boundary vertices (a prefix of
             // each list), then the boundary vertices, which the neighbouring
@@ -277,8 +291,24 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             if (!skip_k)
                 local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
             named_sync(1, NT);
+            // The boundary vertices' sums are on the neighbours' critical path:
+            // when the block has room, thread l sums the first half of vertex
+            // l's list and helper thread hb + l the second half (barrier 4:
+            // the owners' warps wait, the helpers' warps only arrive).
+            if (!skip_k && split_a) {
+                if (tid < ph.nbnd) {
+                    const int b = sptr[tid], e = sptr[tid + 1];
+                    p1 = gather_slots(sent, b, b + gather_half(e - b), cx, cy, cz);
+                } else if (tid >= hb && tid < hb + ph.nbnd) {
+                    const int l = tid - hb, b = sptr[l], e = sptr[l + 1];
+                    part[l] = gather_slots(sent, b + gather_half(e - b), e, cx, cy, cz);
+                }
+                if (tid < hb) named_sync(4, 2 * hb);
+                else if (tid < 2 * hb) named_arrive(4, 2 * hb);
+            }
             if (!skip_k && tid < ph.nbnd) {
-                vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                if (split_a) vertex_update_f<MODE>(fadd3(p1, part[tid]), tid, sy, sd, dprev, gamma, omega_k, o, d, r2);
+                else         vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             named_arrive(2, NTT);

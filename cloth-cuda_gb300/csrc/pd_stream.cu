@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(NT) k_stream(IterArgs a, StreamArgs sa, int k,
             const float4* sdp = reinterpret_cast<const float4*>(st + sa.o_dp);
             float r2 = 0.f;
             for (int l = tid; l < nown; l += NT) {
-                const float3 f = gather_slots(ce, cp[l], cp[l + 1], cx, cy, cz);
+                const float3 f = gather_force(ce, cp[l], cp[l + 1], cx, cy, cz);
                 const int g = h.vbegin + l;
                 const float4 d = sd[l];
                 const float4 y = sy[l];
