@@ -19,7 +19,8 @@ update) of the named workload, all synthetic and generated from seeds:
 
 Prints one JSON line.  `value` is device-timed vertex-steps/s with the state
 resident in HBM (CUDA events on the solver's stream, L2 flushed before every
-step); `e2e` is the same metric through the C ABI with pinned host buffers,
+step); `e2e` is the same metric through the C ABI (pdg_solver_step_host, one call per
+frame) with pinned host buffers,
 host<->device copies of x and v inside the timed region.  Under torchrun each
 rank advances its own replica (weak scaling, no collective on the data path).
 """
@@ -286,17 +287,16 @@ def run_ours(args, rank, world, local_rank):
     hx.numpy()[:] = x0; hv.numpy()[:] = v0
     xnp, vnp = hx.numpy(), hv.numpy()
     # each step: the state goes in from pinned host buffers and the result
-    # comes back into the same buffers (the caller's frame loop)
+    # comes back into the same buffers (the caller's frame loop), through
+    # the one-call upload / step / download entry point
     for _ in range(2):
-        s.set_state_all(xnp, vnp); s.step(1, stats=False); s.get_state_all(xnp, vnp)
+        s.step_host(xnp, vnp, xnp, vnp)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(args.steps):
-        s.set_state_all(xnp, vnp)
-        s.step(1, stats=False)
-        s.get_state_all(xnp, vnp)
+        s.step_host(xnp, vnp, xnp, vnp)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if world > 1:

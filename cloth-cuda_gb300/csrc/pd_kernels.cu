@@ -118,23 +118,28 @@ __global__ void k_finalize(float4* __restrict__ X, float4* __restrict__ V, const
 }
 
 // AoS xyz (caller order, cloth by cloth) <-> float4 reordered.
-__global__ void k_scatter_state(const float* __restrict__ src, float4* __restrict__ dst,
+// Caller-order AoS xyz -> solver-order float4 (w = 0), for one or two
+// arrays per launch (x and v of a state copy).
+__global__ void k_scatter_state(const float* __restrict__ src0, float4* __restrict__ dst0,
+                                const float* __restrict__ src1, float4* __restrict__ dst1,
                                 const int* __restrict__ perm_global, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int o = perm_global[i];
-    dst[i] = make_float4(src[3 * o], src[3 * o + 1], src[3 * o + 2], 0.f);
+    if (src0) dst0[i] = make_float4(src0[3 * o], src0[3 * o + 1], src0[3 * o + 2], 0.f);
+    if (src1) dst1[i] = make_float4(src1[3 * o], src1[3 * o + 1], src1[3 * o + 2], 0.f);
 }
 
-__global__ void k_gather_state(const float4* __restrict__ src, float* __restrict__ dst,
+__global__ void k_gather_state(const float4* __restrict__ src0, float* __restrict__ dst0,
+                               const float4* __restrict__ src1, float* __restrict__ dst1,
                                const int* __restrict__ perm_global, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int o = perm_global[i];
-    const float4 v = src[i];
-    dst[3 * o] = v.x; dst[3 * o + 1] = v.y; dst[3 * o + 2] = v.z;
+    if (dst0) { const float4 v = src0[i]; dst0[3 * o] = v.x; dst0[3 * o + 1] = v.y; dst0[3 * o + 2] = v.z; }
+    if (dst1) { const float4 v = src1[i]; dst1[3 * o] = v.x; dst1[3 * o + 1] = v.y; dst1[3 * o + 2] = v.z; }
 }
 
 // apply_constraints_kernel (src/pd_solver.cu:414-428) on AoS device arrays.
@@ -237,17 +242,19 @@ cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t sme
     return cudaGetLastError();
 }
 
-cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s)
+cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s,
+                                 const float* src1, float4* dst1)
 {
-    if (n == 0) return cudaSuccess;
-    k_scatter_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, perm, n);
+    if (n == 0 || (!src && !src1)) return cudaSuccess;
+    k_scatter_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, src1, dst1, perm, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s)
+cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s,
+                                const float4* src1, float* dst1)
 {
-    if (n == 0) return cudaSuccess;
-    k_gather_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, perm, n);
+    if (n == 0 || (!dst && !dst1)) return cudaSuccess;
+    k_gather_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, src1, dst1, perm, n);
     return cudaGetLastError();
 }
 

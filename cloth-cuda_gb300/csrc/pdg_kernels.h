@@ -17,8 +17,11 @@ cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float
 // then the per-cloth choice between them (slots acc_stride-2 / -1).
 cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t smem, const float4* warm,
                                const int* vcloth, int n, cudaStream_t s);
-cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s);
-cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s);
+// Caller order <-> solver order for one array, or two in one launch (src1/dst1).
+cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s,
+                                 const float* src1 = nullptr, float4* dst1 = nullptr);
+cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s,
+                                const float4* src1 = nullptr, float* dst1 = nullptr);
 cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P,
                               cudaStream_t s);
 

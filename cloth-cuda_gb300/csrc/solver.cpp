@@ -408,36 +408,50 @@ int pdg_solver_reset(pdg_solver* s)
     return PDG_OK;
 }
 
+// State copies between caller order (AoS xyz) and the solver's float4
+// arrays; host pointers go through the device staging buffers.  Both arrays
+// move in one scatter or gather launch.  `sync` = 0 leaves the copies
+// enqueued on the solver's stream.
+static int put_state(pdg_solver* s, int vb, int n, const float* x, const float* v, int on_device, bool whole)
+{
+    if (!x && !v) return PDG_OK;
+    const int* perm = whole ? s->perm_global.p : s->perm_local.p + vb;
+    if (!on_device) {
+        if (x) CK(cudaMemcpyAsync(s->stage_x.p, x, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        if (v) CK(cudaMemcpyAsync(s->stage_v.p, v, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+        x = x ? s->stage_x.p : nullptr;
+        v = v ? s->stage_v.p : nullptr;
+    }
+    CK(launch_scatter_state(x, s->X.p + vb, perm, n, s->stream, v, s->V.p + vb));
+    return PDG_OK;
+}
+
+static int take_state(pdg_solver* s, int vb, int n, float* x, float* v, int on_device, bool whole)
+{
+    if (!x && !v) return PDG_OK;
+    const int* perm = whole ? s->perm_global.p : s->perm_local.p + vb;
+    float* dx = (x && !on_device) ? s->stage_x.p : x;
+    float* dv = (v && !on_device) ? s->stage_v.p : v;
+    CK(launch_gather_state(s->X.p + vb, dx, perm, n, s->stream, s->V.p + vb, dv));
+    if (!on_device) {
+        if (x) CK(cudaMemcpyAsync(x, dx, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+        if (v) CK(cudaMemcpyAsync(v, dv, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    return PDG_OK;
+}
+
 static int set_state_range(pdg_solver* s, int vb, int n, const float* x, const float* v, int on_device, bool whole)
 {
-    const int* perm = whole ? s->perm_global.p : s->perm_local.p + vb;
-    for (int which = 0; which < 2; ++which) {
-        const float* src = which == 0 ? x : v;
-        if (!src) continue;
-        float4* dst = (which == 0 ? s->X.p : s->V.p) + vb;
-        if (!on_device) {
-            float* stage = (which == 0 ? s->stage_x.p : s->stage_v.p);
-            CK(cudaMemcpyAsync(stage, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, s->stream));
-            src = stage;
-        }
-        CK(launch_scatter_state(src, dst, perm, n, s->stream));
-    }
+    const int rc = put_state(s, vb, n, x, v, on_device, whole);
+    if (rc) return rc;
     if (!on_device) CK(cudaStreamSynchronize(s->stream));
     return PDG_OK;
 }
 
 static int get_state_range(pdg_solver* s, int vb, int n, float* x, float* v, int on_device, bool whole)
 {
-    const int* perm = whole ? s->perm_global.p : s->perm_local.p + vb;
-    for (int which = 0; which < 2; ++which) {
-        float* dstp = which == 0 ? x : v;
-        if (!dstp) continue;
-        const float4* src = (which == 0 ? s->X.p : s->V.p) + vb;
-        float* dst = on_device ? dstp : (which == 0 ? s->stage_x.p : s->stage_v.p);
-        CK(launch_gather_state(src, dst, perm, n, s->stream));
-        if (!on_device)
-            CK(cudaMemcpyAsync(dstp, dst, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
-    }
+    const int rc = take_state(s, vb, n, x, v, on_device, whole);
+    if (rc) return rc;
     if (!on_device) CK(cudaStreamSynchronize(s->stream));
     return PDG_OK;
 }
@@ -466,6 +480,22 @@ int pdg_solver_get_state_all(pdg_solver* s, float* x, float* v, int on_device)
 {
     if (!s) return set_error(PDG_ERR_ARG, "null solver");
     return get_state_range(s, 0, s->L.ntot, x, v, on_device, true);
+}
+
+int pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const float* v_in, float* x_out,
+                         float* v_out, pdg_frame_stats* stats)
+{
+    if (!s || nframes < 0) return set_error(PDG_ERR_ARG, "pdg_solver_step_host: bad arguments");
+    int rc = put_state(s, 0, s->L.ntot, x_in, v_in, 0, true);
+    if (rc) return rc;
+    // the frames, then the download: all stream-ordered behind the upload
+    rc = pdg_solver_step(s, nframes, nullptr);
+    if (rc) return rc;
+    rc = take_state(s, 0, s->L.ntot, x_out, v_out, 0, true);
+    if (rc) return rc;
+    if (stats) return pdg_solver_step(s, 0, stats);   // reads the last frame's records (synchronises)
+    CK(cudaStreamSynchronize(s->stream));
+    return PDG_OK;
 }
 
 int pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets)

@@ -299,6 +299,21 @@ class Solver:
         _check(lib().pdg_solver_get_state_all(self.h, _p(xa), _p(va), 0))
         return xa, va
 
+    def step_host(self, x_in=None, v_in=None, x_out=None, v_out=None, nframes=1, stats=False):
+        """Upload / step / download in one call with one synchronisation
+        (pdg_solver_step_host).  Inputs and outputs are C-contiguous float32
+        (N, 3) host arrays of the whole batch in caller order (pinned ones
+        copy fastest); any may be None.  Input and output may be the same
+        arrays."""
+        n = int(self.offsets[-1])
+        for arr in (x_in, v_in, x_out, v_out):
+            if arr is not None and (arr.dtype != np.float32 or not arr.flags.c_contiguous or arr.size != 3 * n):
+                raise ValueError("state arrays must be C-contiguous float32 with N*3 elements")
+        st = (FrameStats * self.n)() if stats else None
+        q = lambda a: _p(a) if a is not None else None
+        _check(lib().pdg_solver_step_host(self.h, nframes, q(x_in), q(v_in), q(x_out), q(v_out), st))
+        return [s.as_dict() for s in st] if stats else None
+
     def set_pin_targets(self, targets, cloth=0):
         t = _f32(targets).reshape(-1, 3)
         _check(lib().pdg_solver_set_pin_targets(self.h, cloth, _p(t)))

@@ -196,6 +196,17 @@ int  pdg_solver_get_state(pdg_solver* s, int cloth, float* x, float* v,
 /* Whole batch at once: x, v hold sum(N) vertices, cloths back to back. */
 int  pdg_solver_set_state_all(pdg_solver* s, const float* x, const float* v, int on_device);
 int  pdg_solver_get_state_all(pdg_solver* s, float* x, float* v, int on_device);
+/* A frame loop's upload / step / download in one call, host buffers, whole
+ * batch in caller order (as the _all calls).  x_in / v_in (either may be
+ * NULL: keep the solver's state) are copied in, nframes frames run, the
+ * result is copied into x_out / v_out (either may be NULL), and the call
+ * returns once the copies are complete, after one synchronisation.  The
+ * same as set_state_all + step + get_state_all, without their separate
+ * synchronisations.  Replaces the step + cudaMemcpy of mesh.d_pos / d_vel
+ * in the reference's frame loop (src/tools/sim_cloth.cpp:237-251 with
+ * lines 44-45 and 82-83).  stats as for pdg_solver_step. */
+int  pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const float* v_in,
+                          float* x_out, float* v_out, pdg_frame_stats* stats);
 /* Move the pins of one cloth (Constraints::target_positions). */
 int  pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets);
 /* Inertial prediction y of the last frame and the residual r(x) of a given

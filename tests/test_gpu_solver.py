@@ -220,6 +220,35 @@ def test_state_roundtrip_and_free_fall(pdg, oracle):
     assert np.allclose(x3, expect, rtol=0, atol=1e-6)
 
 
+@pytest.mark.parametrize("kernel", [1, 3])
+def test_step_host_equals_set_step_get(pdg, oracle, kernel):
+    # pdg_solver_step_host is set_state_all + step + get_state_all in one call
+    ms, cs, cfgs = [], [], []
+    for i, n in enumerate((9, 17)):
+        m, c, cfg, sc, a = scene(pdg, oracle, n=n, seed=i, kernel=kernel)
+        ms.append(m); cs.append(c); cfgs.append(cfg)
+    s1 = pdg.Solver(cfgs, ms, cs)
+    s2 = pdg.Solver(cfgs, ms, cs)
+    n = int(s1.offsets[-1])
+    rng = np.random.default_rng(3)
+    rest = np.concatenate([np.asarray(m.arrays()["rest"]).reshape(-1, 3) for m in ms])
+    x = (rest + rng.normal(0, 1e-3, (n, 3))).astype(np.float32)
+    v = rng.normal(0, 1e-2, (n, 3)).astype(np.float32)
+    for f in range(3):
+        s1.set_state_all(x, v); s1.step(1, stats=False); xa, va = s1.get_state_all()
+        xb, vb = np.empty_like(x), np.empty_like(v)
+        st = s2.step_host(x, v, xb, vb, stats=True)
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+        assert [t["iterations"] for t in st] == [10, 10]
+        x, v = xb, vb
+    # in place, and with the state kept on the device (no inputs)
+    xc, vc = x.copy(), v.copy()
+    s1.set_state_all(x, v); s1.step(2, stats=False); xa, va = s1.get_state_all()
+    s2.step_host(xc, vc, xc, vc)
+    s2.step_host(None, None, xc, None)
+    assert np.array_equal(xa, xc)
+
+
 def test_apply_pins_device(pdg):
     torch = pytest.importorskip("torch")
     pos = torch.arange(30, dtype=torch.float32, device="cuda")
