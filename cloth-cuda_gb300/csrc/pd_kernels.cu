@@ -142,6 +142,29 @@ __global__ void k_gather_state(const float4* __restrict__ src0, float* __restric
     if (dst1) { const float4 v = src1[i]; dst1[3 * o] = v.x; dst1[3 * o + 1] = v.y; dst1[3 * o + 2] = v.z; }
 }
 
+// The same copies walked in caller order through the inverse permutation,
+// so the caller-side buffers (page-locked host memory accessed in place)
+// are read and written contiguously.
+__global__ void k_put_state(const float* __restrict__ x, const float* __restrict__ v, float4* __restrict__ X,
+                            float4* __restrict__ V, const int* __restrict__ inv, int n)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int i = inv[o];
+    if (x) X[i] = make_float4(x[3 * o], x[3 * o + 1], x[3 * o + 2], 0.f);
+    if (v) V[i] = make_float4(v[3 * o], v[3 * o + 1], v[3 * o + 2], 0.f);
+}
+
+__global__ void k_take_state(const float4* __restrict__ X, const float4* __restrict__ V, float* __restrict__ x,
+                             float* __restrict__ v, const int* __restrict__ inv, int n)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const int i = inv[o];
+    if (x) { const float4 a = X[i]; x[3 * o] = a.x; x[3 * o + 1] = a.y; x[3 * o + 2] = a.z; }
+    if (v) { const float4 a = V[i]; v[3 * o] = a.x; v[3 * o + 1] = a.y; v[3 * o + 2] = a.z; }
+}
+
 // apply_constraints_kernel (src/pd_solver.cu:414-428) on AoS device arrays.
 __global__ void k_apply_pins(float* __restrict__ pos, float* __restrict__ vel, const int* __restrict__ idx,
                              const float* __restrict__ target, int P)
@@ -255,6 +278,22 @@ cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, 
 {
     if (n == 0 || (!dst && !dst1)) return cudaSuccess;
     k_gather_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, src1, dst1, perm, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_put_state(const float* x, const float* v, float4* X, float4* V, const int* inv, int n,
+                             cudaStream_t s)
+{
+    if (n == 0 || (!x && !v)) return cudaSuccess;
+    k_put_state<<<nblk(n, 256), 256, 0, s>>>(x, v, X, V, inv, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_take_state(const float4* X, const float4* V, float* x, float* v, const int* inv, int n,
+                              cudaStream_t s)
+{
+    if (n == 0 || (!x && !v)) return cudaSuccess;
+    k_take_state<<<nblk(n, 256), 256, 0, s>>>(X, V, x, v, inv, n);
     return cudaGetLastError();
 }
 

@@ -22,6 +22,12 @@ cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm,
                                  const float* src1 = nullptr, float4* dst1 = nullptr);
 cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s,
                                 const float4* src1 = nullptr, float* dst1 = nullptr);
+// Whole-batch copies in caller order (inv: caller index -> reordered vertex);
+// x / v may be device pointers or mapped page-locked host memory.
+cudaError_t launch_put_state(const float* x, const float* v, float4* X, float4* V, const int* inv, int n,
+                             cudaStream_t s);
+cudaError_t launch_take_state(const float4* X, const float4* V, float* x, float* v, const int* inv, int n,
+                              cudaStream_t s);
 cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P,
                               cudaStream_t s);
 

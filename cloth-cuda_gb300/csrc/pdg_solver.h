@@ -93,6 +93,7 @@ struct pdg_solver {
     pdg::DevBuf<float4> X, V, Y, A, B, aux, warm;
     pdg::DevBuf<float> mass, omega, stage_x, stage_v;
     pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, nbr_ptr, nbr;
+    pdg::DevBuf<int> inv_global;   // caller-order index in the batch -> reordered vertex
     pdg::DevBuf<double> acc;
     pdg::DevBuf<unsigned long long> pflag;
     unsigned long long frame_seq = 0;

@@ -53,6 +53,12 @@ int upload_all(pdg_solver* s)
     CK(s->vcloth.upload(L.vcloth, st));
     CK(s->perm_global.upload(L.perm_global, st));
     CK(s->perm_local.upload(L.perm_local, st));
+    {
+        std::vector<int> inv(L.ntot);
+        for (int g = 0; g < L.ntot; ++g) inv[L.perm_global[g]] = g;
+        CK(s->inv_global.upload(inv, st));
+        CK(cudaStreamSynchronize(st));   // `inv` is a host temporary
+    }
     CK(s->halo.upload(L.halo, st));
     CK(s->csr_ptr.upload(L.csr_ptr, st));
     CK(s->csr_ent.upload(L.csr_ent, st));
@@ -482,17 +488,53 @@ int pdg_solver_get_state_all(pdg_solver* s, float* x, float* v, int on_device)
     return get_state_range(s, 0, s->L.ntot, x, v, on_device, true);
 }
 
+// Device address of a host buffer that kernels may read and write in place
+// (page-locked and mapped into the device's address space), else nullptr.
+static void* mapped_host(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const float* v_in, float* x_out,
                          float* v_out, pdg_frame_stats* stats)
 {
     if (!s || nframes < 0) return set_error(PDG_ERR_ARG, "pdg_solver_step_host: bad arguments");
-    int rc = put_state(s, 0, s->L.ntot, x_in, v_in, 0, true);
-    if (rc) return rc;
+    // Page-locked caller buffers are read and written in place by the copy
+    // kernels (in caller order, so host memory is walked contiguously);
+    // pageable ones go through the device staging buffers.
+    const int n = s->L.ntot;
+    const size_t bytes = sizeof(float) * 3 * (size_t)n;
+    if (x_in || v_in) {
+        const float* dx = static_cast<const float*>(mapped_host(x_in));
+        const float* dv = static_cast<const float*>(mapped_host(v_in));
+        if (x_in && !dx) {
+            CK(cudaMemcpyAsync(s->stage_x.p, x_in, bytes, cudaMemcpyHostToDevice, s->stream));
+            dx = s->stage_x.p;
+        }
+        if (v_in && !dv) {
+            CK(cudaMemcpyAsync(s->stage_v.p, v_in, bytes, cudaMemcpyHostToDevice, s->stream));
+            dv = s->stage_v.p;
+        }
+        CK(launch_put_state(dx, dv, s->X.p, s->V.p, s->inv_global.p, n, s->stream));
+    }
     // the frames, then the download: all stream-ordered behind the upload
-    rc = pdg_solver_step(s, nframes, nullptr);
+    int rc = pdg_solver_step(s, nframes, nullptr);
     if (rc) return rc;
-    rc = take_state(s, 0, s->L.ntot, x_out, v_out, 0, true);
-    if (rc) return rc;
+    if (x_out || v_out) {
+        float* mx = static_cast<float*>(mapped_host(x_out));
+        float* mv = static_cast<float*>(mapped_host(v_out));
+        float* dx = x_out ? (mx ? mx : s->stage_x.p) : nullptr;
+        float* dv = v_out ? (mv ? mv : s->stage_v.p) : nullptr;
+        CK(launch_take_state(s->X.p, s->V.p, dx, dv, s->inv_global.p, n, s->stream));
+        if (x_out && !mx) CK(cudaMemcpyAsync(x_out, dx, bytes, cudaMemcpyDeviceToHost, s->stream));
+        if (v_out && !mv) CK(cudaMemcpyAsync(v_out, dv, bytes, cudaMemcpyDeviceToHost, s->stream));
+    }
     if (stats) return pdg_solver_step(s, 0, stats);   // reads the last frame's records (synchronises)
     CK(cudaStreamSynchronize(s->stream));
     return PDG_OK;

@@ -247,6 +247,18 @@ def test_step_host_equals_set_step_get(pdg, oracle, kernel):
     s2.step_host(xc, vc, xc, vc)
     s2.step_host(None, None, xc, None)
     assert np.array_equal(xa, xc)
+    # page-locked buffers are read and written in place by the copy kernels
+    torch = pytest.importorskip("torch")
+    px = torch.empty((n, 3), dtype=torch.float32).pin_memory().numpy()
+    pv = torch.empty((n, 3), dtype=torch.float32).pin_memory().numpy()
+    px[:] = x; pv[:] = v
+    s1.set_state_all(x, v); s1.step(1, stats=False); xa, va = s1.get_state_all()
+    s2.step_host(px, pv, px, pv)
+    assert np.array_equal(xa, px) and np.array_equal(va, pv)
+    qx = torch.empty((n, 3), dtype=torch.float32).pin_memory().numpy()
+    s1.step(1, stats=False); xa, _ = s1.get_state_all()
+    s2.step_host(None, None, qx, None)   # pinned output, no input
+    assert np.array_equal(xa, qx)
 
 
 def test_apply_pins_device(pdg):
