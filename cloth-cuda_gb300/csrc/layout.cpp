@@ -4,6 +4,7 @@
 #include "pdg_solver.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 
@@ -49,6 +50,216 @@ void morton_order(const MeshData& m, std::vector<int>& perm)
     for (int i = 0; i < m.N; ++i) perm[i] = (int)(key[i] & 0xffffffffu);
 }
 
+// Dm_inv of a triangle whose corners are rotated by r places, (p0, p1, p2)
+// -> (p_r, p_r+1, p_r+2).  Rows of G weight the two edge vectors (F = Ds G,
+// row 0 with x1 - x0, row 1 with x2 - x0); one rotation maps the edges to
+// (e2 - e1, -e1), so the rows become (row1, -(row0 + row1)).
+float4 rotate_G(const float* G, int r)
+{
+    float a0 = G[0], a1 = G[2], b0 = G[1], b1 = G[3];   // row 0 = (g00, g01), row 1 = (g10, g11)
+    for (int q = 0; q < r; ++q) {
+        const float n0 = -(a0 + b0), n1 = -(a1 + b1);
+        a0 = b0; a1 = b1;
+        b0 = n0; b1 = n1;
+    }
+    return make_float4(a0, b0, a1, b1);
+}
+
+// A cell of one cloth in cloth vertex ids, with its record payload; the
+// local indices and slots are filled in per patch.
+struct CellBuild {
+    int v[6];        // c0, c1, c2, c3, x1, x2 (-1: absent)
+    CellRec rec;
+};
+
+// The cells of one cloth, independent of the patch cut, so every patch size
+// and launch structure sums the same contributions in the same order.
+//  1. Triangles are paired across shared edges, longest edge first (the
+//     diagonals of a grid's quads), greedily; a pair must be consistently
+//     oriented and have distinct apexes.
+//  2. One cell per pair, numbered by its lower triangle, and one per
+//     unpaired triangle.  The hinge of a pair's shared edge is its h0.
+//  3. Every other hinge lies on an edge between two cells and goes to one of
+//     them as h1 / h2 (at most two per cell): greedily to the less loaded
+//     one, else along an augmenting path of moves.  What is left over stays
+//     a lone hinge.
+void build_cells(const MeshData& m, const Topology& tp, const ConstraintData& cd, float h2,
+                 std::vector<CellBuild>& cells, std::vector<int>& lone)
+{
+    const int T = m.T, E = (int)cd.bend_k.size();
+    const int nedge = (int)(tp.edges.size() / 4);
+    auto tv = [&](int t, int k) { return m.tris[3 * t + (k % 3)]; };
+    // corner k of triangle t such that (p_k, p_k+1) = (a, b), else -1
+    auto side = [&](int t, int a, int b) {
+        for (int k = 0; k < 3; ++k)
+            if (tv(t, k) == a && tv(t, k + 1) == b) return k;
+        return -1;
+    };
+    auto apex = [&](int t, int a, int b) {
+        for (int k = 0; k < 3; ++k)
+            if (tv(t, k) != a && tv(t, k) != b) return tv(t, k);
+        return -1;
+    };
+    // topology edge of the vertex pair (a, b), -1 if none (edges are sorted)
+    auto find_edge = [&](int a, int b) {
+        if (a > b) std::swap(a, b);
+        int lo = 0, hi = nedge;
+        while (lo < hi) {
+            const int mid = (lo + hi) / 2;
+            const int u = tp.edges[4 * mid], w = tp.edges[4 * mid + 1];
+            if (u < a || (u == a && w < b)) lo = mid + 1; else hi = mid;
+        }
+        return (lo < nedge && tp.edges[4 * lo] == a && tp.edges[4 * lo + 1] == b) ? lo : -1;
+    };
+
+    // 1. pairing
+    std::vector<int> cand;
+    for (int e = 0; e < nedge; ++e) {
+        const int v0 = tp.edges[4 * e], v1 = tp.edges[4 * e + 1], ta = tp.edges[4 * e + 2], tb = tp.edges[4 * e + 3];
+        if (tb < 0 || ta == tb) continue;
+        const bool fwd = side(ta, v0, v1) >= 0;
+        if (!(fwd ? side(tb, v1, v0) >= 0 : (side(ta, v1, v0) >= 0 && side(tb, v0, v1) >= 0))) continue;
+        if (apex(ta, v0, v1) == apex(tb, v0, v1)) continue;
+        cand.push_back(e);
+    }
+    std::stable_sort(cand.begin(), cand.end(), [&](int p, int q) { return tp.rest_len[p] > tp.rest_len[q]; });
+    std::vector<int> partner(T, -1), pedge(T, -1);
+    for (int e : cand) {
+        const int ta = tp.edges[4 * e + 2], tb = tp.edges[4 * e + 3];
+        if (partner[ta] >= 0 || partner[tb] >= 0) continue;
+        partner[ta] = tb; partner[tb] = ta;
+        pedge[ta] = pedge[tb] = e;
+    }
+
+    // 2. cells
+    cells.clear();
+    std::vector<int> cell_of(T, -1);
+    auto stretch = [&](int t) { return h2 * ((t < (int)cd.k_stretch.size() ? cd.k_stretch[t] : 0.f) * m.area[t]); };
+    for (int t = 0; t < T; ++t) {
+        if (partner[t] >= 0 && partner[t] < t) continue;
+        CellBuild c{};
+        for (int& x : c.v) x = -1;
+        const int u = partner[t];
+        int r0 = 0;
+        if (u >= 0) {
+            const int a = tp.edges[4 * pedge[t]], b = tp.edges[4 * pedge[t] + 1];
+            r0 = side(t, a, b);
+            if (r0 < 0) r0 = side(t, b, a);
+        }
+        c.v[0] = tv(t, r0); c.v[1] = tv(t, r0 + 1); c.v[2] = tv(t, r0 + 2);
+        c.rec.G0 = rotate_G(&m.Dm_inv[4 * t], r0);
+        c.rec.h2wA0 = stretch(t);
+        if (u >= 0) {
+            const int r1 = side(u, c.v[1], c.v[0]);
+            c.v[3] = tv(u, r1 + 2);
+            c.rec.G1 = rotate_G(&m.Dm_inv[4 * u], r1);
+            c.rec.h2wA1 = stretch(u);
+            cell_of[u] = (int)cells.size();
+        }
+        cell_of[t] = (int)cells.size();
+        cells.push_back(c);
+    }
+    const int C = (int)cells.size();
+
+    // weights of hinge e over c0..c3 and its corner outside the cell (-1: none)
+    auto cell_weights = [&](const CellBuild& c, int e, float4& W, float& wx) {
+        float w[4] = {0.f, 0.f, 0.f, 0.f};
+        int x = -1;
+        wx = 0.f;
+        for (int j = 0; j < 4; ++j) {
+            const int v = cd.quads[4 * e + j];
+            int k = 0;
+            while (k < 4 && c.v[k] != v) ++k;
+            if (k < 4) w[k] = cd.w[4 * e + j];
+            else { x = v; wx = cd.w[4 * e + j]; }
+        }
+        W = make_float4(w[0], w[1], w[2], w[3]);
+        return x;
+    };
+
+    // 3. hinges: h0 of a pair, else an outer hinge of one of its two cells
+    std::vector<int> h0(C, -1);
+    std::vector<std::array<int, 2>> ca(E, {-1, -1});   // candidate cells
+    lone.clear();
+    for (int e = 0; e < E; ++e) {
+        const int* q = &cd.quads[4 * e];
+        const int te = find_edge(q[0], q[1]);
+        int c0 = -1, c1 = -1;
+        if (te >= 0 && tp.edges[4 * te + 3] >= 0) {
+            const int ta = tp.edges[4 * te + 2], tb = tp.edges[4 * te + 3];
+            const int pa = apex(ta, q[0], q[1]), pb = apex(tb, q[0], q[1]);
+            if ((pa == q[2] && pb == q[3]) || (pa == q[3] && pb == q[2])) { c0 = cell_of[ta]; c1 = cell_of[tb]; }
+        }
+        if (c0 < 0) { lone.push_back(e); continue; }
+        if (c0 == c1) {
+            if (h0[c0] < 0) h0[c0] = e; else lone.push_back(e);
+            continue;
+        }
+        ca[e] = {c0, c1};
+    }
+    std::vector<std::array<int, 2>> held(C, {-1, -1});
+    auto nheld = [&](int c) { return (held[c][0] >= 0) + (held[c][1] >= 0); };
+    auto put = [&](int c, int e) { held[c][held[c][0] >= 0 ? 1 : 0] = e; };
+    auto take = [&](int c, int e) { held[c][held[c][0] == e ? 0 : 1] = -1; };
+    std::vector<int> from_c(C, -1), from_h(C, -1), seen(C, -1), queue;
+    for (int e = 0; e < E; ++e) {
+        if (ca[e][0] < 0) continue;
+        const int a = ca[e][0], b = ca[e][1];
+        const int best = nheld(b) < nheld(a) ? b : a;
+        if (nheld(best) < 2) { put(best, e); continue; }
+        // augmenting path: move held hinges to their other cell until one
+        // has room (breadth first, bounded)
+        queue.clear();
+        for (int c : {a, b}) { seen[c] = e; from_c[c] = -1; from_h[c] = e; queue.push_back(c); }
+        int found = -1;
+        for (size_t qi = 0; qi < queue.size() && found < 0 && queue.size() < 512; ++qi) {
+            const int c = queue[qi];
+            for (int s2 = 0; s2 < 2 && found < 0; ++s2) {
+                const int f = held[c][s2];
+                if (f < 0) continue;
+                const int o = ca[f][0] == c ? ca[f][1] : ca[f][0];
+                if (seen[o] == e) continue;
+                seen[o] = e; from_c[o] = c; from_h[o] = f;
+                if (nheld(o) < 2) found = o; else queue.push_back(o);
+            }
+        }
+        if (found < 0) { lone.push_back(e); continue; }
+        for (int c = found; c >= 0;) {   // c gains from_h[c], which leaves from_c[c]
+            const int f = from_h[c], p = from_c[c];
+            if (p >= 0) take(p, f);
+            put(c, f);
+            c = p;
+        }
+    }
+    std::sort(lone.begin(), lone.end());
+
+    // 4. hinge payloads, outer hinges in hinge order
+    for (int c = 0; c < C; ++c) {
+        CellBuild& cb = cells[c];
+        CellRec& r = cb.rec;
+        if (h0[c] >= 0) {
+            float wx;
+            cell_weights(cb, h0[c], r.W0, wx);
+            r.h2k0 = h2 * cd.bend_k[h0[c]];
+            r.nrest0 = cd.n_rest[h0[c]];
+        }
+        std::array<int, 2> hs = held[c];
+        if (hs[0] < 0 || (hs[1] >= 0 && hs[1] < hs[0])) std::swap(hs[0], hs[1]);
+        for (int j = 0; j < 2; ++j) {
+            const int e = hs[j];
+            if (e < 0) continue;
+            float4 W;
+            float wx;
+            const int x = cell_weights(cb, e, W, wx);
+            (j == 0 ? r.W1 : r.W2) = W;
+            (j == 0 ? r.wx1 : r.wx2) = wx;
+            (j == 0 ? r.h2k1 : r.h2k2) = h2 * cd.bend_k[e];
+            (j == 0 ? r.nrest1 : r.nrest2) = cd.n_rest[e];
+            cb.v[4 + j] = x;
+        }
+    }
+}
+
 }  // namespace
 
 bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout& L, std::string& err)
@@ -76,25 +287,36 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
         const Topology& tp = *cl[ci].topo;
         const ConstraintData& cd = cl[ci].cons;
         const pdg_config& cfg = cl[ci].cfg;
-        const int N = m.N, T = m.T, E = (int)cd.bend_k.size();
+        const int N = m.N;
         std::vector<int> perm, iperm(N);
         morton_order(m, perm);
         for (int i = 0; i < N; ++i) iperm[perm[i]] = i;
-        // A vertex is "boundary" when a triangle or hinge through it has a
+        const float h2 = cfg.dt * cfg.dt;
+        std::vector<CellBuild> cells;
+        std::vector<int> lone;
+        build_cells(m, tp, cd, h2, cells, lone);
+        const int C = (int)cells.size(), H = (int)lone.size();
+        // A vertex is "boundary" when a cell or lone hinge through it has a
         // corner in another patch (it is then in that patch's halo).  Within
         // each patch the boundary vertices go first, so a kernel can finish
         // and publish them before the interior.
         std::vector<char> bnd(N, 0);
         {
             auto mark = [&](const int* v, int n) {
-                const int p = iperm[v[0]] / patch_verts;
+                int p = -1;
                 bool span = false;
-                for (int a = 1; a < n; ++a) span = span || iperm[v[a]] / patch_verts != p;
+                for (int a = 0; a < n; ++a) {
+                    if (v[a] < 0) continue;
+                    const int q = iperm[v[a]] / patch_verts;
+                    span = span || (p >= 0 && q != p);
+                    p = q;
+                }
                 if (span)
-                    for (int a = 0; a < n; ++a) bnd[v[a]] = 1;
+                    for (int a = 0; a < n; ++a)
+                        if (v[a] >= 0) bnd[v[a]] = 1;
             };
-            for (int t = 0; t < T; ++t) mark(&m.tris[3 * t], 3);
-            for (int e = 0; e < E; ++e) mark(&cd.quads[4 * e], 4);
+            for (int c = 0; c < C; ++c) mark(cells[c].v, 6);
+            for (int e : lone) mark(&cd.quads[4 * e], 4);
             for (int p0 = 0; p0 < N; p0 += patch_verts)
                 std::stable_partition(perm.begin() + p0, perm.begin() + std::min(N, p0 + patch_verts),
                                       [&](int o) { return bnd[o] != 0; });
@@ -150,79 +372,90 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             }
         }
 
-        // vertex -> hinge lists
-        std::vector<int> vh_ptr(N + 1, 0), vh(4 * (size_t)E);
-        for (int e = 0; e < E; ++e)
-            for (int a = 0; a < 4; ++a) vh_ptr[cd.quads[4 * e + a] + 1]++;
-        for (int i = 0; i < N; ++i) vh_ptr[i + 1] += vh_ptr[i];
+        // vertex -> cell and vertex -> lone hinge lists
+        std::vector<int> vc_ptr(N + 1, 0), vc, vh_ptr(N + 1, 0), vh;
         {
-            std::vector<int> f(vh_ptr.begin(), vh_ptr.end() - 1);
-            for (int e = 0; e < E; ++e)
-                for (int a = 0; a < 4; ++a) vh[f[cd.quads[4 * e + a]]++] = e;
+            for (int c = 0; c < C; ++c)
+                for (int k = 0; k < 6; ++k)
+                    if (cells[c].v[k] >= 0) vc_ptr[cells[c].v[k] + 1]++;
+            for (int q = 0; q < H; ++q)
+                for (int a = 0; a < 4; ++a) vh_ptr[cd.quads[4 * lone[q] + a] + 1]++;
+            for (int i = 0; i < N; ++i) { vc_ptr[i + 1] += vc_ptr[i]; vh_ptr[i + 1] += vh_ptr[i]; }
+            vc.resize(vc_ptr[N]);
+            vh.resize(vh_ptr[N]);
+            std::vector<int> f(vc_ptr.begin(), vc_ptr.end() - 1), g(vh_ptr.begin(), vh_ptr.end() - 1);
+            for (int c = 0; c < C; ++c)
+                for (int k = 0; k < 6; ++k)
+                    if (cells[c].v[k] >= 0) vc[f[cells[c].v[k]]++] = c;
+            for (int q = 0; q < H; ++q)
+                for (int a = 0; a < 4; ++a) vh[g[cd.quads[4 * lone[q] + a]]++] = q;
         }
 
-        std::vector<int> tmark(T, -1), hmark(E, -1), vmark(N, -1), vloc(N, 0);
-        std::vector<int> ltri, lhin, halo, cnt;
-        const float h2 = cfg.dt * cfg.dt;
+        std::vector<int> cmark(C, -1), hmark(H, -1), vmark(N, -1), vloc(N, 0);
+        std::vector<int> lcell, lhin, halo, cnt;
         for (int p0 = 0; p0 < N; p0 += patch_verts) {
             const int p1 = std::min(N, p0 + patch_verts);
             const int nown = p1 - p0;
             const int stamp = (int)L.patches.size();
-            ltri.clear(); lhin.clear(); halo.clear();
-            int nbnd_p = 0, ntri_a = 0, nhin_a = 0;
+            lcell.clear(); lhin.clear(); halo.clear();
+            int nbnd_p = 0, ncell_a = 0, nhin_a = 0;
             for (int l = 0; l < nown; ++l) {
                 const int o = perm[p0 + l];
-                for (int q = tp.vt_ptr[o]; q < tp.vt_ptr[o + 1]; ++q) {
-                    const int t = tp.vt[q];
-                    if (tmark[t] != stamp) { tmark[t] = stamp; ltri.push_back(t); }
+                for (int q = vc_ptr[o]; q < vc_ptr[o + 1]; ++q) {
+                    const int c = vc[q];
+                    if (cmark[c] != stamp) { cmark[c] = stamp; lcell.push_back(c); }
                 }
                 for (int q = vh_ptr[o]; q < vh_ptr[o + 1]; ++q) {
                     const int e = vh[q];
                     if (hmark[e] != stamp) { hmark[e] = stamp; lhin.push_back(e); }
                 }
             }
-            std::sort(ltri.begin(), ltri.end());
+            std::sort(lcell.begin(), lcell.end());
             std::sort(lhin.begin(), lhin.end());
             auto touch = [&](int o) {
+                if (o < 0) return;
                 const int n = iperm[o];
                 if (n >= p0 && n < p1) return;
                 if (vmark[n] != stamp) { vmark[n] = stamp; halo.push_back(n); }
             };
-            for (int t : ltri)
-                for (int a = 0; a < 3; ++a) touch(m.tris[3 * t + a]);
-            for (int e : lhin)
-                for (int a = 0; a < 4; ++a) touch(cd.quads[4 * e + a]);
+            for (int c : lcell)
+                for (int k = 0; k < 6; ++k) touch(cells[c].v[k]);
+            for (int q : lhin)
+                for (int a = 0; a < 4; ++a) touch(cd.quads[4 * lone[q] + a]);
             std::sort(halo.begin(), halo.end());
             for (int l = 0; l < nown; ++l) vloc[p0 + l] = l;
             for (size_t q = 0; q < halo.size(); ++q) vloc[halo[q]] = nown + (int)q;
+            auto loc = [&](int o) { return (uint32_t)vloc[iperm[o]]; };
             // record placement follows the Morton order of the lowest local
             // corner, so the lanes of a warp touch neighbouring vertices and
             // neighbouring slots (fewer shared-memory bank conflicts); the
             // summation order is fixed separately below
             {
-                auto lo_t = [&](int t) {
-                    return std::min(vloc[iperm[m.tris[3 * t]]],
-                                    std::min(vloc[iperm[m.tris[3 * t + 1]]], vloc[iperm[m.tris[3 * t + 2]]]));
-                };
-                auto lo_h = [&](int e) {
-                    int lo = vloc[iperm[cd.quads[4 * e]]];
-                    for (int a = 1; a < 4; ++a) lo = std::min(lo, vloc[iperm[cd.quads[4 * e + a]]]);
+                auto lo_c = [&](int c) {
+                    int lo = 1 << 30;
+                    for (int k = 0; k < 6; ++k)
+                        if (cells[c].v[k] >= 0) lo = std::min(lo, (int)loc(cells[c].v[k]));
                     return lo;
                 };
-                std::stable_sort(ltri.begin(), ltri.end(), [&](int u, int w) { return lo_t(u) < lo_t(w); });
+                auto lo_h = [&](int q) {
+                    int lo = (int)loc(cd.quads[4 * lone[q]]);
+                    for (int a = 1; a < 4; ++a) lo = std::min(lo, (int)loc(cd.quads[4 * lone[q] + a]));
+                    return lo;
+                };
+                std::stable_sort(lcell.begin(), lcell.end(), [&](int u, int w) { return lo_c(u) < lo_c(w); });
                 std::stable_sort(lhin.begin(), lhin.end(), [&](int u, int w) { return lo_h(u) < lo_h(w); });
                 // boundary vertices are local 0..nbnd-1; the records through
                 // one of them are a prefix of each list
                 nbnd_p = 0;
                 while (nbnd_p < nown && bnd[perm[p0 + nbnd_p]]) ++nbnd_p;
-                ntri_a = 0;
-                while (ntri_a < (int)ltri.size() && lo_t(ltri[ntri_a]) < nbnd_p) ++ntri_a;
+                ncell_a = 0;
+                while (ncell_a < (int)lcell.size() && lo_c(lcell[ncell_a]) < nbnd_p) ++ncell_a;
                 nhin_a = 0;
                 while (nhin_a < (int)lhin.size() && lo_h(lhin[nhin_a]) < nbnd_p) ++nhin_a;
             }
             const int nlocal = nown + (int)halo.size();
-            const int ntri = (int)ltri.size(), nhin = (int)lhin.size();
-            const int nslot = 3 * ntri + 4 * nhin;
+            const int ncell = (int)lcell.size(), nhin = (int)lhin.size();
+            const int nslot = 6 * ncell + 4 * nhin;
             if (nlocal > 65535 || nslot > 65535) {
                 err = "patch too large for 16-bit local indices; lower patch_verts";
                 return false;
@@ -238,26 +471,26 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             ph.nown = nown;
             ph.nlocal = nlocal;
             ph.halo_off = (int)L.halo.size();
-            ph.tri_off = (int)L.tris.size();
-            ph.ntri = ntri;
+            ph.cell_off = (int)L.cells.size();
+            ph.ncell = ncell;
             ph.hinge_off = (int)L.hinges.size();
             ph.nhinge = nhin;
             ph.csr_off = (int)L.csr_ptr.size();
             ph.ent_off = (int)L.csr_ent.size();
             ph.nslot = nslot;
             for (int n : halo) L.halo.push_back(vbase + n);
-            auto loc = [&](int o) { return (uint32_t)vloc[iperm[o]]; };
-            for (int t : ltri) {
-                TriRec r{};
-                const float* G = &m.Dm_inv[4 * t];
-                r.G = make_float4(G[0], G[1], G[2], G[3]);
-                const float k = t < (int)cd.k_stretch.size() ? cd.k_stretch[t] : 0.f;
-                r.h2wA = h2 * (k * m.area[t]);
-                r.l01 = loc(m.tris[3 * t]) | (loc(m.tris[3 * t + 1]) << 16);
-                r.l2 = loc(m.tris[3 * t + 2]);
-                L.tris.push_back(r);
+            for (int c : lcell) {
+                const CellBuild& cb = cells[c];
+                CellRec r = cb.rec;
+                const uint32_t l0 = loc(cb.v[0]);
+                auto lv = [&](int k) { return cb.v[k] >= 0 ? loc(cb.v[k]) : l0; };
+                r.c01 = l0 | (lv(1) << 16);
+                r.c23 = lv(2) | (lv(3) << 16);
+                r.x12 = lv(4) | (lv(5) << 16);
+                L.cells.push_back(r);
             }
-            for (int e : lhin) {
+            for (int q : lhin) {
+                const int e = lone[q];
                 HingeRec r{};
                 r.w = make_float4(cd.w[4 * e], cd.w[4 * e + 1], cd.w[4 * e + 2], cd.w[4 * e + 3]);
                 r.h2k = h2 * cd.bend_k[e];
@@ -266,24 +499,24 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                 r.l23 = loc(cd.quads[4 * e + 2]) | (loc(cd.quads[4 * e + 3]) << 16);
                 L.hinges.push_back(r);
             }
-            // gather lists: owned vertex l sums the slots of its corners in
-            // global triangle order, then global hinge order -- independent
-            // of where the records sit in the patch, so every patch size and
-            // launch structure adds in the same order
-            std::vector<int> ot(ntri), oh(nhin);
-            for (int q = 0; q < ntri; ++q) ot[q] = q;
+            // gather lists: owned vertex l sums its outputs in global cell
+            // order (outputs o0..o5 within a cell), then global lone-hinge
+            // order -- independent of where the records sit in the patch, so
+            // every patch size and launch structure adds in the same order
+            std::vector<int> oc(ncell), oh(nhin);
+            for (int q = 0; q < ncell; ++q) oc[q] = q;
             for (int q = 0; q < nhin; ++q) oh[q] = q;
-            std::sort(ot.begin(), ot.end(), [&](int u, int w) { return ltri[u] < ltri[w]; });
+            std::sort(oc.begin(), oc.end(), [&](int u, int w) { return lcell[u] < lcell[w]; });
             std::sort(oh.begin(), oh.end(), [&](int u, int w) { return lhin[u] < lhin[w]; });
             cnt.assign(nown + 1, 0);
-            for (int lt = 0; lt < ntri; ++lt)
-                for (int a = 0; a < 3; ++a) {
-                    const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
-                    if (l < nown) cnt[l + 1]++;
+            for (int lc = 0; lc < ncell; ++lc)
+                for (int k = 0; k < 6; ++k) {
+                    const int v = cells[lcell[lc]].v[k];
+                    if (v >= 0 && (int)loc(v) < nown) cnt[loc(v) + 1]++;
                 }
             for (int lh = 0; lh < nhin; ++lh)
                 for (int a = 0; a < 4; ++a) {
-                    const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
+                    const int l = (int)loc(cd.quads[4 * lone[lhin[lh]] + a]);
                     if (l < nown) cnt[l + 1]++;
                 }
             for (int l = 0; l < nown; ++l) cnt[l + 1] += cnt[l];
@@ -293,11 +526,11 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             std::vector<int> fill(cnt.begin(), cnt.end() - 1);
             // Two slot addressings hold the same contributions.  Corner-major
             // (resident and streaming kernels, summed through the gather
-            // lists): triangle corner a at a*ntri + lt, hinge corner a at
-            // 3*ntri + a*nhin + lh.  Vertex-major (per-patch sweep kernels):
+            // lists): output k of cell lc at k*ncell + lc, hinge corner a at
+            // 6*ncell + a*nhin + lh.  Vertex-major (per-patch sweep kernels):
             // contribution j of owned vertex l at j*npad + l, so a warp's
             // gather loads are unit-stride and need no list entries; halo
-            // corners get 0xffff and store nothing.
+            // corners and absent outputs get 0xffff and store nothing.
             int maxdeg = 0;
             for (int l = 0; l < nown; ++l) maxdeg = std::max(maxdeg, cnt[l + 1] - cnt[l]);
             const int npad = nown | 1;
@@ -307,43 +540,46 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
                 return false;
             }
             std::vector<uint32_t> vm(nslot, 0xffffu);
-            for (int lt : ot)
-                for (int a = 0; a < 3; ++a) {
-                    const int l = (int)loc(m.tris[3 * ltri[lt] + a]);
+            for (int lc : oc)
+                for (int k = 0; k < 6; ++k) {
+                    const int v = cells[lcell[lc]].v[k];
+                    if (v < 0) continue;
+                    const int l = (int)loc(v);
                     if (l < nown) {
-                        vm[a * ntri + lt] = (uint32_t)((fill[l] - cnt[l]) * npad + l);
-                        L.csr_ent[e0 + fill[l]++] = (uint16_t)(a * ntri + lt);
+                        vm[k * ncell + lc] = (uint32_t)((fill[l] - cnt[l]) * npad + l);
+                        L.csr_ent[e0 + fill[l]++] = (uint16_t)(k * ncell + lc);
                     }
                 }
             for (int lh : oh)
                 for (int a = 0; a < 4; ++a) {
-                    const int l = (int)loc(cd.quads[4 * lhin[lh] + a]);
+                    const int l = (int)loc(cd.quads[4 * lone[lhin[lh]] + a]);
                     if (l < nown) {
-                        vm[3 * ntri + a * nhin + lh] = (uint32_t)((fill[l] - cnt[l]) * npad + l);
-                        L.csr_ent[e0 + fill[l]++] = (uint16_t)(3 * ntri + a * nhin + lh);
+                        vm[6 * ncell + a * nhin + lh] = (uint32_t)((fill[l] - cnt[l]) * npad + l);
+                        L.csr_ent[e0 + fill[l]++] = (uint16_t)(6 * ncell + a * nhin + lh);
                     }
                 }
-            for (int lt = 0; lt < ntri; ++lt) {
-                TriRec& r = L.tris[ph.tri_off + lt];
-                r.l2 |= vm[lt] << 16;
-                r.vm12 = vm[ntri + lt] | (vm[2 * ntri + lt] << 16);
+            for (int lc = 0; lc < ncell; ++lc) {
+                CellRec& r = L.cells[ph.cell_off + lc];
+                r.vm01 = vm[lc] | (vm[ncell + lc] << 16);
+                r.vm23 = vm[2 * ncell + lc] | (vm[3 * ncell + lc] << 16);
+                r.vm45 = vm[4 * ncell + lc] | (vm[5 * ncell + lc] << 16);
             }
             for (int lh = 0; lh < nhin; ++lh)
-                L.hvm.push_back(make_uint2(vm[3 * ntri + lh] | (vm[3 * ntri + nhin + lh] << 16),
-                                           vm[3 * ntri + 2 * nhin + lh] | (vm[3 * ntri + 3 * nhin + lh] << 16)));
+                L.hvm.push_back(make_uint2(vm[6 * ncell + lh] | (vm[6 * ncell + nhin + lh] << 16),
+                                           vm[6 * ncell + 2 * nhin + lh] | (vm[6 * ncell + 3 * nhin + lh] << 16)));
             ph.vm_npad = npad;
             ph.vm_nslot = (int)vm_nslot;
             L.max_vm_slot = std::max(L.max_vm_slot, 32 * (size_t)nlocal + 12 * (size_t)vm_nslot);
             ph.nent = cnt[nown];
             ph.nbnd = nbnd_p;
-            ph.ntri_a = ntri_a;
+            ph.ncell_a = ncell_a;
             ph.nhin_a = nhin_a;
             L.max_nent = std::max(L.max_nent, cnt[nown]);
             L.max_nhalo = std::max(L.max_nhalo, nlocal - nown);
             L.max_nlocal = std::max(L.max_nlocal, nlocal);
             L.max_nslot = std::max(L.max_nslot, nslot);
             L.max_nown = std::max(L.max_nown, nown);
-            L.max_ntri = std::max(L.max_ntri, ntri);
+            L.max_ncell = std::max(L.max_ncell, ncell);
             L.max_nhinge = std::max(L.max_nhinge, nhin);
             const size_t res = 32 * (size_t)nlocal + 12 * (size_t)nslot + 4 * (size_t)(nown + 1) + 2 * (size_t)cnt[nown];
             L.smem_resident = std::max(L.smem_resident, (res + 15) / 16 * 16);

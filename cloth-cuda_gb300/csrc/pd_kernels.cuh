@@ -21,6 +21,10 @@ __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b)
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return ffma(a.x, b.x, ffma(a.y, b.y, fmul(a.z, b.z))); }
 __device__ __forceinline__ float3 scale3(float3 a, float s) { return make_float3(fmul(a.x, s), fmul(a.y, s), fmul(a.z, s)); }
 __device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 fadd3(float3 a, float3 b)
+{
+    return make_float3(fadd(a.x, b.x), fadd(a.y, b.y), fadd(a.z, b.z));
+}
 
 // ---------------------------------------------------------------------------
 // Stretch projection, consistent form: Gram-Schmidt basis (b0, b1) of F's
@@ -126,9 +130,6 @@ __device__ __forceinline__ float3 edge(const float4* sy, const float4* sd, int i
                        fadd(fsub(yj.z, yi.z), fsub(dj.z, di.z)));
 }
 
-// Triangle phase for one local triangle: writes the contributions of its
-// three corners.  Slots are corner-major (corner c of local triangle lt at
-// c*ntri + lt), so a warp's stores are unit-stride and free of bank conflicts.
 // Corner contributions of one triangle from its two edge vectors:
 // c_v = h^2 wA sum_col coef_{v,col} (R - F)_col (consistent) or with R alone
 // (literal), coef from Dm_inv G = (g00, g10, g01, g11).
@@ -157,48 +158,12 @@ __device__ __forceinline__ void tri_force(float3 d1, float3 d2, float4 G, float 
     c2 = make_float3(ffma(g10, q0.x, fmul(g11, q1.x)), ffma(g10, q0.y, fmul(g11, q1.y)), ffma(g10, q0.z, fmul(g11, q1.z)));
 }
 
+// Hinge: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
+// n_rest <= 1e-10, src/pd_solver.cu:304-335); corner i receives w_i q with
+// q = h^2 k (p - e) (consistent) or h^2 k p (literal).
 template <int MODE>
-__device__ __forceinline__ void triangle_contrib(const TriRec& r, const float4* sy, const float4* sd, int lt,
-                                                 int ntri, float* cx, float* cy, float* cz)
+__device__ __forceinline__ float3 hinge_q(float3 e, float h2k, float nrest)
 {
-    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2 & 0xffffu;
-    float3 c0, c1, c2;
-    tri_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), r.G, r.h2wA, c0, c1, c2);
-    const int b1 = ntri + lt, b2 = 2 * ntri + lt;
-    cx[lt] = c0.x; cy[lt] = c0.y; cz[lt] = c0.z;
-    cx[b1] = c1.x; cy[b1] = c1.y; cz[b1] = c1.z;
-    cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z;
-}
-
-// Vertex-major variants for the per-patch sweep kernels: the record carries
-// the slot address of each corner (0xffff for a halo corner: no store).
-template <int MODE>
-__device__ __forceinline__ void triangle_contrib_vm(const TriRec& r, const float4* sy, const float4* sd, float* cx,
-                                                    float* cy, float* cz)
-{
-    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l2 & 0xffffu;
-    float3 c0, c1, c2;
-    tri_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), r.G, r.h2wA, c0, c1, c2);
-    const uint32_t b0 = r.l2 >> 16, b1 = r.vm12 & 0xffffu, b2 = r.vm12 >> 16;
-    if (b0 != 0xffffu) { cx[b0] = c0.x; cy[b0] = c0.y; cz[b0] = c0.z; }
-    if (b1 != 0xffffu) { cx[b1] = c1.x; cy[b1] = c1.y; cz[b1] = c1.z; }
-    if (b2 != 0xffffu) { cx[b2] = c2.x; cy[b2] = c2.y; cz[b2] = c2.z; }
-}
-
-// Hinge phase: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
-// n_rest <= 1e-10, src/pd_solver.cu:304-335); slot s gets h^2 k w_s (p - e)
-// (consistent) or h^2 k w_s p (literal).  Slot s of local hinge e sits at
-// hbase + s*nhin + e.
-// Bending "force" q of one hinge (slot s receives w_s q): e = sum w_i x_i
-// formed as sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0 from edge vectors.
-template <int MODE>
-__device__ __forceinline__ float3 hinge_force(float3 e1, float3 e2, float3 e3, float3 x0, float4 w, float h2k,
-                                              float nrest)
-{
-    const float ws = fadd(fadd(w.x, w.y), fadd(w.z, w.w));
-    const float3 e = make_float3(ffma(w.y, e1.x, ffma(w.z, e2.x, ffma(w.w, e3.x, fmul(ws, x0.x)))),
-                                 ffma(w.y, e1.y, ffma(w.z, e2.y, ffma(w.w, e3.y, fmul(ws, x0.y)))),
-                                 ffma(w.y, e1.z, ffma(w.z, e2.z, ffma(w.w, e3.z, fmul(ws, x0.z)))));
     float3 p = make_float3(0.f, 0.f, 0.f);
     if (nrest > 1e-10f) {
         const float len = __fsqrt_rn(dot3(e, e));
@@ -209,6 +174,107 @@ __device__ __forceinline__ float3 hinge_force(float3 e1, float3 e2, float3 e3, f
     return scale3(p, h2k);
 }
 
+// e = sum w_i x_i formed as sum_{i>0} w_i (x_i - x_0) + (sum w_i) x_0 from
+// edge vectors.
+template <int MODE>
+__device__ __forceinline__ float3 hinge_force(float3 e1, float3 e2, float3 e3, float3 x0, float4 w, float h2k,
+                                              float nrest)
+{
+    const float ws = fadd(fadd(w.x, w.y), fadd(w.z, w.w));
+    const float3 e = make_float3(ffma(w.y, e1.x, ffma(w.z, e2.x, ffma(w.w, e3.x, fmul(ws, x0.x)))),
+                                 ffma(w.y, e1.y, ffma(w.z, e2.y, ffma(w.w, e3.y, fmul(ws, x0.y)))),
+                                 ffma(w.y, e1.z, ffma(w.z, e2.z, ffma(w.w, e3.z, fmul(ws, x0.z)))));
+    return hinge_q<MODE>(e, h2k, nrest);
+}
+
+// The same with a fifth term: the outer corner x of a cell's outer-edge
+// hinge, at edge vector ex from x_0 with weight wx.
+template <int MODE>
+__device__ __forceinline__ float3 hinge_force_x(float3 e1, float3 e2, float3 e3, float3 ex, float3 x0, float4 w,
+                                                float wx, float h2k, float nrest)
+{
+    const float ws = fadd(fadd(fadd(w.x, w.y), fadd(w.z, w.w)), wx);
+    const float3 e =
+        make_float3(ffma(wx, ex.x, ffma(w.y, e1.x, ffma(w.z, e2.x, ffma(w.w, e3.x, fmul(ws, x0.x))))),
+                    ffma(wx, ex.y, ffma(w.y, e1.y, ffma(w.z, e2.y, ffma(w.w, e3.y, fmul(ws, x0.y))))),
+                    ffma(wx, ex.z, ffma(w.y, e1.z, ffma(w.z, e2.z, ffma(w.w, e3.z, fmul(ws, x0.z))))));
+    return hinge_q<MODE>(e, h2k, nrest);
+}
+
+__device__ __forceinline__ float3 edge4(float4 yi, float4 di, float4 yj, float4 dj)
+{
+    return make_float3(fadd(fsub(yj.x, yi.x), fsub(dj.x, di.x)), fadd(fsub(yj.y, yi.y), fsub(dj.y, di.y)),
+                       fadd(fsub(yj.z, yi.z), fsub(dj.z, di.z)));
+}
+
+// The six outputs of one cell: o_k for c_k is t0's + t1's contribution, then
+// h0's, h1's and h2's (w_k q added by fused multiply-add); o4 / o5 are the
+// outer corners' shares of h1 / h2.  Every launch structure calls this, so
+// the per-cell sums are bitwise the same everywhere.
+template <int MODE>
+__device__ __forceinline__ void cell_force(const CellRec& r, const float4* sy, const float4* sd, float3 (&o)[6])
+{
+    const int i0 = r.c01 & 0xffffu, i1 = r.c01 >> 16, i2 = r.c23 & 0xffffu, i3 = r.c23 >> 16;
+    const int j1 = r.x12 & 0xffffu, j2 = r.x12 >> 16;
+    const float4 y0 = sy[i0], d0 = sd[i0], y1 = sy[i1], d1 = sd[i1];
+    const float4 y2 = sy[i2], d2 = sd[i2], y3 = sy[i3], d3 = sd[i3];
+    const float4 yx1 = sy[j1], dx1 = sd[j1], yx2 = sy[j2], dx2 = sd[j2];
+    const float3 e01 = edge4(y0, d0, y1, d1), e02 = edge4(y0, d0, y2, d2), e03 = edge4(y0, d0, y3, d3);
+    const float3 e13 = edge4(y1, d1, y3, d3);
+    const float3 ex1 = edge4(y0, d0, yx1, dx1), ex2 = edge4(y0, d0, yx2, dx2);
+    const float3 x0 = make_float3(fadd(y0.x, d0.x), fadd(y0.y, d0.y), fadd(y0.z, d0.z));
+    float3 a0, a1, a2, b0, b1, b3;
+    tri_force<MODE>(e01, e02, r.G0, r.h2wA0, a0, a1, a2);
+    tri_force<MODE>(make_float3(-e01.x, -e01.y, -e01.z), e13, r.G1, r.h2wA1, b1, b0, b3);
+    const float3 q0 = hinge_force<MODE>(e01, e02, e03, x0, r.W0, r.h2k0, r.nrest0);
+    const float3 q1 = hinge_force_x<MODE>(e01, e02, e03, ex1, x0, r.W1, r.wx1, r.h2k1, r.nrest1);
+    const float3 q2 = hinge_force_x<MODE>(e01, e02, e03, ex2, x0, r.W2, r.wx2, r.h2k2, r.nrest2);
+    auto acc = [&](float3 t, float w0, float w1, float w2) {
+        return make_float3(ffma(w2, q2.x, ffma(w1, q1.x, ffma(w0, q0.x, t.x))),
+                           ffma(w2, q2.y, ffma(w1, q1.y, ffma(w0, q0.y, t.y))),
+                           ffma(w2, q2.z, ffma(w1, q1.z, ffma(w0, q0.z, t.z))));
+    };
+    o[0] = acc(fadd3(a0, b0), r.W0.x, r.W1.x, r.W2.x);
+    o[1] = acc(fadd3(a1, b1), r.W0.y, r.W1.y, r.W2.y);
+    o[2] = acc(a2, r.W0.z, r.W1.z, r.W2.z);
+    o[3] = acc(b3, r.W0.w, r.W1.w, r.W2.w);
+    o[4] = scale3(q1, r.wx1);
+    o[5] = scale3(q2, r.wx2);
+}
+
+// Corner-major slots (resident and streaming kernels): output k of local
+// cell lc at k*ncell + lc, so a warp's stores are unit-stride and free of
+// bank conflicts.
+template <int MODE>
+__device__ __forceinline__ void cell_contrib(const CellRec& r, const float4* sy, const float4* sd, int lc, int ncell,
+                                             float* cx, float* cy, float* cz)
+{
+    float3 o[6];
+    cell_force<MODE>(r, sy, sd, o);
+    #pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const int s = k * ncell + lc;
+        cx[s] = o[k].x; cy[s] = o[k].y; cz[s] = o[k].z;
+    }
+}
+
+// Vertex-major slots (per-patch sweep kernels): the record carries each
+// output's slot address (0xffff for a halo corner or an absent output).
+template <int MODE>
+__device__ __forceinline__ void cell_contrib_vm(const CellRec& r, const float4* sy, const float4* sd, float* cx,
+                                                float* cy, float* cz)
+{
+    float3 o[6];
+    cell_force<MODE>(r, sy, sd, o);
+    const uint32_t vm[6] = {r.vm01 & 0xffffu, r.vm01 >> 16, r.vm23 & 0xffffu, r.vm23 >> 16,
+                            r.vm45 & 0xffffu, r.vm45 >> 16};
+    #pragma unroll
+    for (int k = 0; k < 6; ++k)
+        if (vm[k] != 0xffffu) { cx[vm[k]] = o[k].x; cy[vm[k]] = o[k].y; cz[vm[k]] = o[k].z; }
+}
+
+// Lone hinge: slot s of local hinge e_ sits at hbase + s*nhin + e_ (hbase =
+// 6*ncell).
 template <int MODE>
 __device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int e_,
                                               int hbase, int nhin, float* cx, float* cy, float* cz)
@@ -261,10 +327,6 @@ __device__ __forceinline__ float3 gather_slots(const IDX* ent, int b, int e, con
 // entries, each half in list order.  Every kernel forms exactly this, so
 // one that gives the two halves to two threads produces the same bits.
 __device__ __forceinline__ int gather_half(int deg) { return (deg + 1) >> 1; }
-__device__ __forceinline__ float3 fadd3(float3 a, float3 b)
-{
-    return make_float3(fadd(a.x, b.x), fadd(a.y, b.y), fadd(a.z, b.z));
-}
 template <class IDX>
 __device__ __forceinline__ float3 gather_force(const IDX* ent, int b, int e, const float* cx, const float* cy,
                                                const float* cz)
@@ -372,12 +434,12 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     if (skip_s && *(const volatile int*)skip_s) return;
     if (omega_s) omega = *(const volatile float*)omega_s;
 
-    // 2. local step: triangles then hinges, contributions to shared slots
-    const TriRec* __restrict__ tr = a.tris + ph.tri_off;
-    const int ntri = ph.ntri, nhin = ph.nhinge;
-    for (int t = tid; t < ntri; t += NT) {
-        const TriRec r = tr[t];
-        triangle_contrib_vm<MODE>(r, sy, sd, cx, cy, cz);
+    // 2. local step: cells then lone hinges, contributions to shared slots
+    const CellRec* __restrict__ cr = a.cells + ph.cell_off;
+    const int ncell = ph.ncell, nhin = ph.nhinge;
+    for (int c = tid; c < ncell; c += NT) {
+        const CellRec r = cr[c];
+        cell_contrib_vm<MODE>(r, sy, sd, cx, cy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;
     const uint2* __restrict__ hv = a.hvm + ph.hinge_off;

@@ -11,8 +11,8 @@
 // residual.  Every wait is bounded by a clock64 budget; on expiry the block
 // records an error code and leaves, and so do all others at their next wait.
 //
-// Used when every patch fits one block (nown <= NT, ntri <= MT*NT,
-// nhinge <= MH*NT) and all patches are co-resident.
+// Used when every patch fits one block (nown <= NT) and all patches are
+// co-resident.
 #include "pd_kernels.cuh"
 #include "pdg_kernels.h"
 
@@ -87,32 +87,19 @@ __device__ __forceinline__ bool poll_neighbours(int lane, const int* nb, int nnb
     return __ballot_sync(0xffffffffu, good) == 0xffffffffu;
 }
 
-template <int NT, int MT>
-__device__ __forceinline__ int tri_index(int tid, int j)
-{
-    return j < MT - 1 ? tid + j * NT : (MT - 1) * NT + (NT - 1 - tid);
-}
-
 constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 
-// Local step over this thread's records with list index in [t0, t1) (triangles)
-// and [e0, e1) (hinges).
-template <int MODE, int NT, int MT, int MH>
-__device__ __forceinline__ void local_records(const TriRec (&rt)[MT], const HingeRec (&rh)[MH], const float4* sy,
-                                              const float4* sd, int ntri, int nhin, int t0, int t1, int e0, int e1,
-                                              float* cx, float* cy, float* cz)
+// Local step over the records with list index in [t0, t1) (cells) and
+// [e0, e1) (lone hinges), read through the read-only data path: a patch's
+// records stay in L1 for the whole frame.
+template <int MODE, int NT>
+__device__ __forceinline__ void local_records(const CellRec* __restrict__ rc, const HingeRec* __restrict__ rh,
+                                              const float4* sy, const float4* sd, int ncell, int nhin, int t0, int t1,
+                                              int e0, int e1, float* cx, float* cy, float* cz)
 {
     const int tid = threadIdx.x;
-    #pragma unroll
-    for (int j = 0; j < MT; ++j) {
-        const int t = tri_index<NT, MT>(tid, j);
-        if (t >= t0 && t < t1) triangle_contrib<MODE>(rt[j], sy, sd, t, ntri, cx, cy, cz);
-    }
-    #pragma unroll
-    for (int j = 0; j < MH; ++j) {
-        const int e = tid + j * NT;
-        if (e >= e0 && e < e1) hinge_contrib<MODE>(rh[j], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
-    }
+    for (int t = t0 + tid; t < t1; t += NT) cell_contrib<MODE>(rc[t], sy, sd, t, ncell, cx, cy, cz);
+    for (int e = e0 + tid; e < e1; e += NT) hinge_contrib<MODE>(rh[e], sy, sd, e, 6 * ncell, nhin, cx, cy, cz);
 }
 
 // Jacobi update of owned vertex l with force f: o = d^(k+1), d = d^k.
@@ -169,7 +156,7 @@ __device__ __forceinline__ void compute_residual(float r2, float* red, double* a
 // `sig_ok` at bar 3 and every thread leaves.
 // With a tolerance every sweep ends in a grid barrier instead and the
 // signal warp only takes part in the block-wide barriers.
-template <int MODE, int NT, int MT, int MH>
+template <int MODE, int NT>
 __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistArgs p)
 {
     constexpr int NTT = NT + 32;   // a multiple of 128: 4 warps per SM sub-partition
@@ -185,7 +172,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     const bool comp = tid < NT;
     if (tid == 0) ph = a.patches[blockIdx.x];
     __syncthreads();
-    const int nown = ph.nown, nlocal = ph.nlocal, ntri = ph.ntri, nhin = ph.nhinge;
+    const int nown = ph.nown, nlocal = ph.nlocal, ncell = ph.ncell, nhin = ph.nhinge;
     float4* sy = smem;
     float4* sd = sy + nlocal;
     float* cx = reinterpret_cast<float*>(sd + nlocal);
@@ -194,23 +181,8 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     int* sptr = reinterpret_cast<int*>(cz + ph.nslot);
     uint16_t* sent = reinterpret_cast<uint16_t*>(sptr + nown + 1);
 
-    // records in registers for the whole frame.  The partial last round of
-    // triangles goes to the highest threads and that of hinges to the
-    // lowest, so warps finish the local step together.
-    TriRec rt[MT];
-    HingeRec rh[MH];
-    if (comp) {
-        #pragma unroll
-        for (int j = 0; j < MT; ++j) {
-            const int t = tri_index<NT, MT>(tid, j);
-            if (t < ntri) rt[j] = a.tris[ph.tri_off + t];
-        }
-        #pragma unroll
-        for (int j = 0; j < MH; ++j) {
-            const int e = tid + j * NT;
-            if (e < nhin) rh[j] = a.hinges[ph.hinge_off + e];
-        }
-    }
+    const CellRec* __restrict__ rc = a.cells + ph.cell_off;
+    const HingeRec* __restrict__ rh = a.hinges + ph.hinge_off;
     // gather lists and Chebyshev weights in shared memory
     for (int l = tid; l <= nown; l += NTT) sptr[l] = a.csr_ptr[ph.csr_off + l];
     for (int k = tid; k < a.omega_stride && k < kResOmega; k += NTT) som[k] = a.omega[ph.cloth * a.omega_stride + k];
@@ -289,7 +261,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // each list), then the boundary vertices, which the neighbouring
             // patches read; the signal warp publishes them while phase B runs.
             if (!skip_k)
-                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ph.ntri_a, 0, ph.nhin_a, cx, cy, cz);
+                local_records<MODE, NT>(rc, rh, sy, sd, ncell, nhin, 0, ph.ncell_a, 0, ph.nhin_a, cx, cy, cz);
             named_sync(1, NT);
             // The boundary vertices' sums are on the neighbours' critical path:
             // when the block has room, thread l sums the first half of vertex
@@ -314,7 +286,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             named_arrive(2, NTT);
             // Phase B: the remaining records, then the interior vertices
             if (!skip_k)
-                local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, ph.ntri_a, ntri, ph.nhin_a, nhin, cx,
+                local_records<MODE, NT>(rc, rh, sy, sd, ncell, nhin, ph.ncell_a, ncell, ph.nhin_a, nhin, cx,
                                                 cy, cz);
             named_sync(1, NT);
             if (!skip_k && own && tid >= ph.nbnd) {
@@ -348,7 +320,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
             float r2 = 0.f;
             if (!skip_k) {
-                if (comp) local_records<MODE, NT, MT, MH>(rt, rh, sy, sd, ntri, nhin, 0, ntri, 0, nhin, cx, cy, cz);
+                if (comp) local_records<MODE, NT>(rc, rh, sy, sd, ncell, nhin, 0, ncell, 0, nhin, cx, cy, cz);
                 __syncthreads();
                 if (own) {
                     vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
@@ -370,29 +342,26 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     if (own) finalize_vertex(g, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
 }
 
-// MT x NT triangles and MH x NT hinges per block of NT compute threads plus
-// the signal warp.  480 + 32 threads: one block (one patch) per SM;
-// 224 + 32: two half-size patches per SM.  The smaller record set (fewer
-// registers) is used when the patches fit it.
-struct ResVariant { int nt, mt, mh; void* f[2]; };
+// NT compute threads plus the signal warp: 480 + 32 threads, one block (one
+// patch) per SM; 224 + 32, two half-size patches per SM.
+struct ResVariant { int nt; void* f[2]; };
 
 static const ResVariant* res_variants(int* n)
 {
     static const ResVariant v[] = {
-        {480, 2, 3, {(void*)k_resident<kModeConsistent, 480, 2, 3>, (void*)k_resident<kModeLiteral, 480, 2, 3>}},
-        {480, 3, 4, {(void*)k_resident<kModeConsistent, 480, 3, 4>, (void*)k_resident<kModeLiteral, 480, 3, 4>}},
-        {224, 3, 4, {(void*)k_resident<kModeConsistent, 224, 3, 4>, (void*)k_resident<kModeLiteral, 224, 3, 4>}},
+        {480, {(void*)k_resident<kModeConsistent, 480>, (void*)k_resident<kModeLiteral, 480>}},
+        {224, {(void*)k_resident<kModeConsistent, 224>, (void*)k_resident<kModeLiteral, 224>}},
     };
-    *n = 3;
+    *n = 2;
     return v;
 }
 
-int resident_pick(int nt, int max_ntri, int max_nhinge)
+int resident_pick(int nt)
 {
     int n = 0;
     const ResVariant* v = res_variants(&n);
     for (int i = 0; i < n; ++i)
-        if (v[i].nt == nt && max_ntri <= v[i].mt * nt && max_nhinge <= v[i].mh * nt) return i;
+        if (v[i].nt == nt) return i;
     return -1;
 }
 

@@ -2,7 +2,7 @@
 // graph) with a persistent grid of a few blocks per SM.  Each block walks the
 // patches blockIdx.x, blockIdx.x + gridDim.x, ... and double-buffers them in
 // shared memory: while it projects and gathers patch i, the TMA engine copies
-// the contiguous per-patch data of patch i + gridDim.x (triangle and hinge
+// the contiguous per-patch data of patch i + gridDim.x (cell and lone hinge
 // records, gather pointers and entries, halo index list, y, d^k and d^(k-1)
 // of the owned vertices) into the other stage with cp.async.bulk, completing
 // on an mbarrier.  Only the halo vertices' y and d^k are gathered with plain
@@ -106,11 +106,11 @@ __device__ __forceinline__ void issue_patch(const IterArgs& a, const StreamArgs&
 {
     const PatchHdr h = a.patches[p];
     *hs = h;
-    const uint32_t b_tri = 32u * h.ntri, b_hin = 32u * h.nhinge;
+    const uint32_t b_cell = (uint32_t)sizeof(CellRec) * h.ncell, b_hin = 32u * h.nhinge;
     const uint32_t b_ptr = round16(4u * (h.nown + 1)), b_ent = round16(2u * h.nent);
     const uint32_t b_hidx = round16(4u * (h.nlocal - h.nown)), b_v = 16u * h.nown;
-    mbar_arrive_expect_tx(bar, b_tri + b_hin + b_ptr + b_ent + b_hidx + 3 * b_v);
-    if (b_tri) bulk_g2s(stage + sa.o_tri, a.tris + h.tri_off, b_tri, bar);
+    mbar_arrive_expect_tx(bar, b_cell + b_hin + b_ptr + b_ent + b_hidx + 3 * b_v);
+    if (b_cell) bulk_g2s(stage + sa.o_cell, a.cells + h.cell_off, b_cell, bar);
     if (b_hin) bulk_g2s(stage + sa.o_hin, a.hinges + h.hinge_off, b_hin, bar);
     bulk_g2s(stage + sa.o_ptr, a.csr_ptr + h.csr_off, b_ptr, bar);
     if (b_ent) bulk_g2s(stage + sa.o_ent, a.csr_ent + h.ent_off, b_ent, bar);
@@ -189,11 +189,11 @@ __global__ void __launch_bounds__(NT) k_stream(IterArgs a, StreamArgs sa, int k,
         }
         __syncthreads();
         if (!skip) {
-            const int ntri = h.ntri, nhin = h.nhinge;
-            const TriRec* tr = reinterpret_cast<const TriRec*>(st + sa.o_tri);
+            const int ncell = h.ncell, nhin = h.nhinge;
+            const CellRec* cr = reinterpret_cast<const CellRec*>(st + sa.o_cell);
             const HingeRec* hr = reinterpret_cast<const HingeRec*>(st + sa.o_hin);
-            for (int t = tid; t < ntri; t += NT) triangle_contrib<MODE>(tr[t], sy, sd, t, ntri, cx, cy, cz);
-            for (int e = tid; e < nhin; e += NT) hinge_contrib<MODE>(hr[e], sy, sd, e, 3 * ntri, nhin, cx, cy, cz);
+            for (int c = tid; c < ncell; c += NT) cell_contrib<MODE>(cr[c], sy, sd, c, ncell, cx, cy, cz);
+            for (int e = tid; e < nhin; e += NT) hinge_contrib<MODE>(hr[e], sy, sd, e, 6 * ncell, nhin, cx, cy, cz);
             __syncthreads();
             const bool ro = res_only != 0 || k >= a.cinfo[h.cloth].max_iter;
             const float gamma = a.cinfo[h.cloth].gamma;
@@ -223,12 +223,12 @@ __global__ void __launch_bounds__(NT) k_stream(IterArgs a, StreamArgs sa, int k,
 }
 
 // Stage layout: every region starts on a 16-byte boundary.
-bool stream_layout(int max_ntri, int max_nhinge, int max_nown, int max_nent, int max_nhalo, int max_nlocal,
+bool stream_layout(int max_ncell, int max_nhinge, int max_nown, int max_nent, int max_nhalo, int max_nlocal,
                    int max_nslot, StreamArgs& sa, size_t& smem)
 {
     auto r16 = [](size_t b) { return (b + 15) / 16 * 16; };
     size_t o = 0;
-    sa.o_tri = (int)o;  o += 32 * (size_t)max_ntri;
+    sa.o_cell = (int)o; o += sizeof(CellRec) * (size_t)max_ncell;
     sa.o_hin = (int)o;  o += 32 * (size_t)max_nhinge;
     sa.o_ptr = (int)o;  o += r16(4 * (size_t)(max_nown + 1));
     sa.o_ent = (int)o;  o += r16(2 * (size_t)max_nent);

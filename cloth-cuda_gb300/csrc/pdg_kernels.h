@@ -60,13 +60,10 @@ struct PersistArgs {
 cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s);
 int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
 
-// Resident persistent kernel (pd_resident.cu): one patch per block, records
-// in registers; nt compute threads (480: one block per SM, 224: two) plus a
-// signal warp.  Limits: nown <= nt, ntri <= mt*nt, nhinge <= mh*nt for the
-// variant's (mt, mh).
-// Kernel variant for nt threads whose record capacity holds the patches
-// (-1: none).
-int resident_pick(int nt, int max_ntri, int max_nhinge);
+// Resident persistent kernel (pd_resident.cu): one patch per block for the
+// whole frame; nt compute threads (480: one block per SM, 224: two) plus a
+// signal warp.  Limit: nown <= nt.  Kernel variant for nt threads (-1: none).
+int resident_pick(int nt);
 int resident_max_blocks(int mode, int variant, size_t smem);
 cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t smem, cudaStream_t s);
 
@@ -74,7 +71,7 @@ cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t 
 // double-buffered in shared memory by bulk copies.  Byte offsets of the
 // regions of one stage; the contribution slots follow the two stages.
 struct StreamArgs {
-    int o_tri, o_hin, o_ptr, o_ent, o_hidx, o_y, o_d, o_dp;
+    int o_cell, o_hin, o_ptr, o_ent, o_hidx, o_y, o_d, o_dp;
     int stage_bytes;
     int slot_off;
     int max_nslot;
@@ -82,7 +79,7 @@ struct StreamArgs {
     int* err;               // set when a copy wait times out
     long long spin_budget;  // clock64 cycles a wait may take
 };
-bool stream_layout(int max_ntri, int max_nhinge, int max_nown, int max_nent, int max_nhalo, int max_nlocal,
+bool stream_layout(int max_ncell, int max_nhinge, int max_nown, int max_nent, int max_nhalo, int max_nlocal,
                    int max_nslot, StreamArgs& sa, size_t& smem);
 int stream_max_blocks(int mode, int nt, size_t smem);
 cudaError_t launch_stream(const IterArgs& a, const StreamArgs& sa, int mode, int nt, int grid, size_t smem, int k,

@@ -4,9 +4,9 @@
 // The cloths of a solver are concatenated in one Morton-reordered vertex
 // numbering.  Each cloth's vertices are cut into patches of up to
 // `patch_verts` consecutive vertices; one CUDA block processes one patch.  A
-// patch carries every triangle and bend hinge that touches one of its owned
-// vertices, with vertex references rewritten as 16-bit local indices into
-// the patch's vertex list (owned vertices first, then the halo).
+// patch carries every cell and every lone bend hinge that touches one of its
+// owned vertices, with vertex references rewritten as 16-bit local indices
+// into the patch's vertex list (owned vertices first, then the halo).
 #pragma once
 
 #include <cstdint>
@@ -20,27 +20,44 @@ struct PatchHdr {            // 80 B
     int nown;                // owned vertices
     int nlocal;              // owned + halo
     int halo_off;            // into halo[]
-    int tri_off, ntri;       // into tri_rec[]
-    int hinge_off, nhinge;   // into hinge_rec[]
+    int cell_off, ncell;     // into cells[]
+    int hinge_off, nhinge;   // into hinges[] (lone hinges)
     int csr_off;             // into csr_ptr[] (nown + 1 entries, relative to ent_off)
     int ent_off;             // into csr_ent[]
-    int nslot;               // 3*ntri + 4*nhinge contribution slots
+    int nslot;               // 6*ncell + 4*nhinge contribution slots
     int nent;                // gather-list entries of the owned vertices
     int nbnd;                // owned vertices 0..nbnd-1 are in other patches' halos
-    int ntri_a, nhin_a;      // records 0..ntri_a-1 / 0..nhin_a-1 touch one of them
+    int ncell_a, nhin_a;     // records 0..ncell_a-1 / 0..nhin_a-1 touch one of them
     int vm_npad;             // vertex-major slots: contribution j of owned vertex l at j*vm_npad + l
     int vm_nslot;            // vertex-major slot array length
     int pad[2];
 };
 
-struct TriRec {              // 32 B
-    float4   G;              // Dm_inv col-major (g00, g10, g01, g11)
-    float    h2wA;           // h^2 * k_stretch * rest area
-    uint32_t l01;            // local indices of corners 0 | 1 << 16
-    uint32_t l2;             // local index of corner 2 | vertex-major slot of corner 0 << 16
-    uint32_t vm12;           // vertex-major slots of corners 1 | 2 << 16 (0xffff: halo corner)
+// A cell groups the records around one pair of triangles so that their four
+// shared corners are read once and their contributions are summed before
+// they are stored:
+//   t0 = (c0, c1, c2) and t1 = (c1, c0, c3), two triangles sharing the edge
+//      c0-c1, corners rotated so that edge comes first (G in that order);
+//   h0, the bend hinge of c0-c1, weights W0 over c0..c3;
+//   h1, h2, up to two hinges of the pair's outer edges, each with three
+//      corners among c0..c3 (weights W1, W2) and one outer corner x1 / x2
+//      (weight wx1 / wx2).
+// Absent parts carry zero weights and stiffness: a lone triangle has G1 = 0
+// and c3 = c0.  Outputs o0..o3 are the summed contributions to c0..c3 and
+// o4 / o5 those to x1 / x2.
+struct CellRec {             // 144 B
+    float4   G0, G1;         // Dm_inv of t0, t1, col-major (g00, g10, g01, g11)
+    float4   W0, W1, W2;     // weights of c0..c3 in h0, h1, h2
+    float    h2wA0, h2wA1;   // h^2 * k_stretch * rest area of t0, t1
+    float    h2k0, nrest0;   // h0: h^2 * bend stiffness, rest curvature norm
+    float    h2k1, nrest1, wx1;
+    float    h2k2, nrest2, wx2;
+    uint32_t c01, c23;       // local indices c0 | c1 << 16, c2 | c3 << 16
+    uint32_t x12;            // local indices x1 | x2 << 16 (c0 when absent)
+    uint32_t vm01, vm23, vm45;   // vertex-major slots of o0..o5 (0xffff: halo corner or absent)
 };
 
+// A bend hinge that no cell holds.
 struct HingeRec {            // 32 B
     float4   w;              // cotangent weights w0..w3
     float    h2k;            // h^2 * bend stiffness
@@ -77,7 +94,7 @@ struct ClothRT {
 struct IterArgs {
     const PatchHdr*  patches;
     const int*       halo;
-    const TriRec*    tris;
+    const CellRec*   cells;
     const HingeRec*  hinges;
     const uint2*     hvm;         // per hinge: vertex-major slots of corners 0 | 1 << 16, 2 | 3 << 16
     const int*       csr_ptr;

@@ -23,7 +23,7 @@ struct ClothSetup {
 
 struct HostLayout {
     int ntot = 0, ncloth = 0, npatch = 0, cap = 0, omega_stride = 1;
-    int max_nlocal = 0, max_nslot = 0, max_nown = 0, max_ntri = 0, max_nhinge = 0, max_nent = 0, max_nhalo = 0;
+    int max_nlocal = 0, max_nslot = 0, max_nown = 0, max_ncell = 0, max_nhinge = 0, max_nent = 0, max_nhalo = 0;
     size_t smem_bytes = 0;          // per-patch sweep kernels (vertex-major slots)
     size_t max_vm_slot = 0;         // largest 32*nlocal + 12*vm_nslot of a patch
     size_t smem_resident = 0;       // resident kernel: + gather lists
@@ -36,7 +36,7 @@ struct HostLayout {
     std::vector<float> omega;
     std::vector<PatchHdr> patches;
     std::vector<int> halo;
-    std::vector<TriRec> tris;
+    std::vector<CellRec> cells;
     std::vector<HingeRec> hinges;
     std::vector<uint2> hvm;         // per hinge: its vertex-major slot addresses
     std::vector<int> csr_ptr;
@@ -101,7 +101,7 @@ struct pdg_solver {
     int nbr_sync = 0;
     pdg::DevBuf<uint16_t> csr_ent;
     pdg::DevBuf<pdg::PatchHdr> patches;
-    pdg::DevBuf<pdg::TriRec> tris;
+    pdg::DevBuf<pdg::CellRec> cells;
     pdg::DevBuf<pdg::HingeRec> hinges;
     pdg::DevBuf<uint2> hvm;
     pdg::DevBuf<pdg::ClothInfo> cinfo;

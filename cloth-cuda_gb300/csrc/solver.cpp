@@ -63,7 +63,7 @@ int upload_all(pdg_solver* s)
     CK(s->csr_ptr.upload(L.csr_ptr, st));
     CK(s->csr_ent.upload(L.csr_ent, st));
     CK(s->patches.upload(L.patches, st));
-    CK(s->tris.upload(L.tris, st));
+    CK(s->cells.upload(L.cells, st));
     CK(s->hinges.upload(L.hinges, st));
     CK(s->hvm.upload(L.hvm, st));
     CK(s->cinfo.upload(L.cinfo, st));
@@ -99,7 +99,7 @@ int upload_all(pdg_solver* s)
 IterArgs iter_args(pdg_solver* s)
 {
     IterArgs a;
-    a.patches = s->patches.p; a.halo = s->halo.p; a.tris = s->tris.p; a.hinges = s->hinges.p; a.hvm = s->hvm.p;
+    a.patches = s->patches.p; a.halo = s->halo.p; a.cells = s->cells.p; a.hinges = s->hinges.p; a.hvm = s->hvm.p;
     a.csr_ptr = s->csr_ptr.p; a.csr_ent = s->csr_ent.p; a.cinfo = s->cinfo.p; a.crt = s->crt.p;
     a.omega = s->omega.p; a.omega_stride = s->L.omega_stride;
     a.Y = s->Y.p; a.buf[0] = s->A.p; a.buf[1] = s->B.p; a.ncloth = s->L.ncloth;
@@ -227,7 +227,7 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
         bool ok = P <= rnt && build_layout(s->cloths, P, s->L, err);
         int variant = -1;
         if (ok) {
-            variant = resident_pick(rnt, s->L.max_ntri, s->L.max_nhinge);
+            variant = resident_pick(rnt);
             ok = variant >= 0 && s->L.max_nown <= rnt &&
                  s->L.smem_resident <= (size_t)std::min(smem_optin / per_sm - 8192, 216 * 1024);
             if (ok) ok = s->L.npatch <= resident_max_blocks(s->mode, variant, s->L.smem_resident);
@@ -251,7 +251,7 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
         if (!build_layout(s->cloths, s->patch_verts, s->L, err)) return set_error(PDG_ERR_ARG, "%s", err.c_str());
         if (s->kernel == PDG_KERNEL_STREAM) {
             const HostLayout& L = s->L;
-            stream_layout(L.max_ntri, L.max_nhinge, L.max_nown, L.max_nent, L.max_nhalo, L.max_nlocal, L.max_nslot,
+            stream_layout(L.max_ncell, L.max_nhinge, L.max_nown, L.max_nent, L.max_nhalo, L.max_nlocal, L.max_nslot,
                           s->sargs, s->stream_smem);
             if (s->stream_smem + 2048 <= (size_t)smem_optin) break;
         } else if (s->L.smem_bytes + 1024 <= (size_t)std::min(smem_optin, 200 * 1024)) {
