@@ -581,7 +581,8 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.max_nown = std::max(L.max_nown, nown);
             L.max_ncell = std::max(L.max_ncell, ncell);
             L.max_nhinge = std::max(L.max_nhinge, nhin);
-            const size_t res = 32 * (size_t)nlocal + 12 * (size_t)nslot + 4 * (size_t)(nown + 1) + 2 * (size_t)cnt[nown];
+            const size_t res = sizeof(CellRec) * (size_t)ncell + sizeof(HingeRec) * (size_t)nhin + 32 * (size_t)nlocal +
+                               12 * (size_t)nslot + 4 * (size_t)(nown + 1) + 2 * (size_t)cnt[nown];
             L.smem_resident = std::max(L.smem_resident, (res + 15) / 16 * 16);
             L.patches.push_back(ph);
         }

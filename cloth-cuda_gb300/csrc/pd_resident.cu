@@ -1,8 +1,8 @@
 // Resident persistent PD kernel: one cooperative launch per frame, one patch
-// per block for the whole frame.  Each thread keeps its triangle and hinge
-// records in registers and its owned vertex's previous offset d^(k-1) in a
-// register; the patch's gather lists, y and d^k live in shared memory.  Per
-// sweep only the owned offsets go out to L2 and the halo offsets come back.
+// per block for the whole frame.  The patch's cell and hinge records, gather
+// lists, y and d^k live in shared memory and each thread keeps its owned
+// vertex's previous offset d^(k-1) in a register.  Per sweep only the owned
+// offsets go out to L2 and the halo offsets come back.
 //
 // Synchronisation between sweeps: with fixed sweep counts a block waits only
 // for the patches that own its halo vertices (per-patch completion marks in
@@ -90,10 +90,9 @@ __device__ __forceinline__ bool poll_neighbours(int lane, const int* nb, int nnb
 constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 
 // Local step over the records with list index in [t0, t1) (cells) and
-// [e0, e1) (lone hinges), read through the read-only data path: a patch's
-// records stay in L1 for the whole frame.
+// [e0, e1) (lone hinges), read from the patch's copy in shared memory.
 template <int MODE, int NT>
-__device__ __forceinline__ void local_records(const CellRec* __restrict__ rc, const HingeRec* __restrict__ rh,
+__device__ __forceinline__ void local_records(const CellRec* rc, const HingeRec* rh,
                                               const float4* sy, const float4* sd, int ncell, int nhin, int t0, int t1,
                                               int e0, int e1, float* cx, float* cy, float* cz)
 {
@@ -173,7 +172,11 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     if (tid == 0) ph = a.patches[blockIdx.x];
     __syncthreads();
     const int nown = ph.nown, nlocal = ph.nlocal, ncell = ph.ncell, nhin = ph.nhinge;
-    float4* sy = smem;
+    // shared memory: the patch's records (read every sweep), y and d of the
+    // local vertices, the contribution slots and the gather lists
+    CellRec* rc = reinterpret_cast<CellRec*>(smem);
+    HingeRec* rh = reinterpret_cast<HingeRec*>(rc + ncell);
+    float4* sy = reinterpret_cast<float4*>(rh + nhin);
     float4* sd = sy + nlocal;
     float* cx = reinterpret_cast<float*>(sd + nlocal);
     float* cy = cx + ph.nslot;
@@ -181,8 +184,15 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     int* sptr = reinterpret_cast<int*>(cz + ph.nslot);
     uint16_t* sent = reinterpret_cast<uint16_t*>(sptr + nown + 1);
 
-    const CellRec* __restrict__ rc = a.cells + ph.cell_off;
-    const HingeRec* __restrict__ rh = a.hinges + ph.hinge_off;
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(a.cells + ph.cell_off);
+        uint4* dst = reinterpret_cast<uint4*>(rc);
+        const int n4 = ncell * (int)(sizeof(CellRec) / 16);
+        for (int q = tid; q < n4; q += NTT) dst[q] = __ldg(&src[q]);
+        const uint4* hsrc = reinterpret_cast<const uint4*>(a.hinges + ph.hinge_off);
+        uint4* hdst = reinterpret_cast<uint4*>(rh);
+        for (int q = tid; q < 2 * nhin; q += NTT) hdst[q] = __ldg(&hsrc[q]);
+    }
     // gather lists and Chebyshev weights in shared memory
     for (int l = tid; l <= nown; l += NTT) sptr[l] = a.csr_ptr[ph.csr_off + l];
     for (int k = tid; k < a.omega_stride && k < kResOmega; k += NTT) som[k] = a.omega[ph.cloth * a.omega_stride + k];
