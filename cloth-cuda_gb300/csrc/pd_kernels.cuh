@@ -160,17 +160,22 @@ __device__ __forceinline__ void tri_force(float3 d1, float3 d2, float4 G, float 
 
 // Hinge: e = sum w_i x_i, target p = e * n_rest / |e| (0 if |e| or
 // n_rest <= 1e-10, src/pd_solver.cu:304-335); corner i receives w_i q with
-// q = h^2 k (p - e) (consistent) or h^2 k p (literal).
+// q = h^2 k (p - e) (consistent) or h^2 k p (literal).  The consistent form
+// scales by n_rest * rsqrt(|e|^2), like the stretch projection; the literal
+// form keeps the reference kernel's square root and division.
 template <int MODE>
 __device__ __forceinline__ float3 hinge_q(float3 e, float h2k, float nrest)
 {
     float3 p = make_float3(0.f, 0.f, 0.f);
+    if (MODE == kModeConsistent) {
+        const float n2 = dot3(e, e);
+        if (nrest > 1e-10f && n2 > 1e-20f) p = scale3(e, fmul(nrest, rsqrtf(n2)));
+        return make_float3(fmul(h2k, fsub(p.x, e.x)), fmul(h2k, fsub(p.y, e.y)), fmul(h2k, fsub(p.z, e.z)));
+    }
     if (nrest > 1e-10f) {
         const float len = __fsqrt_rn(dot3(e, e));
         if (len > 1e-10f) p = scale3(e, fdiv(nrest, len));
     }
-    if (MODE == kModeConsistent)
-        return make_float3(fmul(h2k, fsub(p.x, e.x)), fmul(h2k, fsub(p.y, e.y)), fmul(h2k, fsub(p.z, e.z)));
     return scale3(p, h2k);
 }
 
