@@ -80,7 +80,12 @@ def test_adam_step_matches_oracle(pdg):
 def test_training_on_solver_data_beats_inertial_start_and_never_hurts(pdg):
     import scenes
     w = pdg.WarmStart(seed=0)
-    for b in range(10):   # fresh trajectories of cloths from the batched distribution
+    # fresh trajectories of cloths from the batched distribution; training
+    # is not bit-reproducible (the blocks add their weight-gradient partial
+    # sums with float atomics), so it
+    # runs long enough to clear the bar by a wide margin (measured: held-out
+    # ratio 0.88-0.91 after 10 batches, 0.50-0.52 after 20)
+    for b in range(20):
         ms, cs, cfgs, _ = scenes.batch(16, seed=100 + b, max_iterations=300, tolerance=1e-6, n_range=(17, 33),
                                        kernel=pdg.KERNEL_GRAPH)
         s = pdg.Solver(cfgs, ms, cs)
