@@ -19,7 +19,7 @@
 namespace pdg {
 
 template <int MODE, int NT>
-__global__ void __launch_bounds__(NT) k_iter(IterArgs a, int k, int res_only)
+__global__ void __launch_bounds__(NT, 768 / NT) k_iter(IterArgs a, int k, int res_only)
 {
     extern __shared__ float4 smem[];
     __shared__ PatchHdr ph;
