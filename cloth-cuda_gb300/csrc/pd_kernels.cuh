@@ -428,11 +428,37 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     float4* sd = sy + ph.nlocal;
     const int tid = threadIdx.x;
 
-    // 1. stage y and d^k of owned + halo vertices
-    for (int l = tid; l < ph.nlocal; l += NT) {
-        const int g = l < ph.nown ? ph.vbegin + l : __ldg(&a.halo[ph.halo_off + l - ph.nown]);
-        sy[l] = __ldcg(&a.Y[g]);
-        sd[l] = __ldcg(&Dk[g]);
+    const int nlocal = ph.nlocal, nown = ph.nown, vbegin = ph.vbegin;
+    const int* __restrict__ halo = a.halo + ph.halo_off - nown;   // halo list, indexed by local vertex
+    const int* __restrict__ cp = a.csr_ptr + ph.csr_off;
+    const CellRec* __restrict__ cr = a.cells + ph.cell_off;
+    const int ncell = ph.ncell, nhin = ph.nhinge;
+
+    // 0. loads issued before the staging barrier, so that their memory round
+    // trips overlap the staging: the gather pointers and d^(k-1) of this
+    // thread's first owned vertex.  (Loading its first cell record here too
+    // costs more in register spills than it saves.)
+    int cp0 = 0, cp1 = 0;
+    float4 dp0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tid < nown) {
+        cp0 = __ldg(&cp[tid]);
+        cp1 = __ldg(&cp[tid + 1]);
+        if (MODE == kModeConsistent && !res_only) dp0 = __ldcg(&Dn[vbegin + tid]);
+    }
+
+    // 1. stage y and d^k of owned + halo vertices, two per thread and pass
+    // with both index loads issued before the position loads
+    for (int l0 = tid; l0 < nlocal; l0 += 2 * NT) {
+        const int l1 = l0 + NT;
+        const bool has1 = l1 < nlocal;
+        const int l1c = has1 ? l1 : l0;
+        const int g0 = l0 < nown ? vbegin + l0 : __ldg(&halo[l0]);
+        const int g1 = l1c < nown ? vbegin + l1c : __ldg(&halo[l1c]);
+        const float4 y0 = __ldcg(&a.Y[g0]), d0 = __ldcg(&Dk[g0]);
+        const float4 y1 = __ldcg(&a.Y[g1]), d1 = __ldcg(&Dk[g1]);
+        sy[l0] = y0;
+        sd[l0] = d0;
+        if (has1) { sy[l1] = y1; sd[l1] = d1; }
     }
     __syncthreads();
     // a skip decision and weight taken by thread 0 while the block staged
@@ -440,8 +466,6 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     if (omega_s) omega = *(const volatile float*)omega_s;
 
     // 2. local step: cells then lone hinges, contributions to shared slots
-    const CellRec* __restrict__ cr = a.cells + ph.cell_off;
-    const int ncell = ph.ncell, nhin = ph.nhinge;
     for (int c = tid; c < ncell; c += NT) {
         const CellRec r = cr[c];
         cell_contrib_vm<MODE>(r, sy, sd, cx, cy, cz);
@@ -456,20 +480,20 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
 
     // 3. global step per owned vertex
     const float gamma = a.cinfo[ph.cloth].gamma;
-    const int* __restrict__ cp = a.csr_ptr + ph.csr_off;
     const int npad = ph.vm_npad;
     float r2 = 0.f;
-    for (int l = tid; l < ph.nown; l += NT) {
+    for (int l = tid; l < nown; l += NT) {
         // contributions j = 0..deg-1 of vertex l: first half + second half
-        const int deg = __ldg(&cp[l + 1]) - __ldg(&cp[l]);
+        const bool first = l == tid;
+        const int deg = first ? cp1 - cp0 : __ldg(&cp[l + 1]) - __ldg(&cp[l]);
         const int h = gather_half(deg);
         const float3 f = fadd3(gather_vm(l, 0, h, npad, cx, cy, cz), gather_vm(l, h, deg, npad, cx, cy, cz));
-        const int g = ph.vbegin + l;
+        const int g = vbegin + l;
         const float4 d = sd[l];
         const float4 y = sy[l];
         if (MODE == kModeConsistent) {
             float rv;
-            const float4 dp = res_only ? d : __ldcg(&Dn[g]);
+            const float4 dp = res_only ? d : (first ? dp0 : __ldcg(&Dn[g]));
             const float4 o = update_consistent(d, y, f, dp, gamma, omega, rv);
             r2 += rv;
             if (!res_only) Dn[g] = o;
@@ -480,25 +504,46 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     if (MODE == kModeConsistent) block_residual<NT>(r2, red, a.acc + (size_t)ph.cloth * a.acc_stride + k);
 }
 
+// Loads that are issued in program order and not moved past later branches
+// (asm volatile): a chain of dependent decisions then waits for one memory
+// round trip instead of one per condition.
+__device__ __forceinline__ int ld_cg_s32(const int* p)
+{
+    int v;
+    asm volatile("ld.global.cg.s32 %0, [%1];" : "=r"(v) : "l"(__cvta_generic_to_global(p)));
+    return v;
+}
+__device__ __forceinline__ double ld_cg_f64(const double* p)
+{
+    double v;
+    asm volatile("ld.global.cg.f64 %0, [%1];" : "=d"(v) : "l"(__cvta_generic_to_global(p)));
+    return v;
+}
+
 // Per-cloth decision at the start of sweep k, taken by one thread per block;
 // every block of a cloth reaches the same answer from the same data.
 // Returns true if the cloth is done.  The cloth's first patch records it.
 // With check == false only the static cap is applied (the per-sweep sums may
-// still be incomplete: sweeps synchronised with neighbours only).
+// still be incomplete: sweeps synchronised with neighbours only).  Every
+// value it may need is loaded up front.
 __device__ __forceinline__ bool cloth_done(const IterArgs& a, int c, int k, bool designated, bool check = true)
 {
     ClothRT* rt = a.crt + c;
-    if (!__ldcg(&rt->active)) return true;
     const ClothInfo& ci = a.cinfo[c];
     const double* acc = a.acc + (size_t)c * a.acc_stride;
-    if (check && k >= 1 && ci.mode == kModeConsistent) {
-        const double acc0 = __ldcg(&acc[0]);
-        const double rk2 = __ldcg(&acc[k - 1]);          // ||r(x^(k-1))||^2
+    const int active = ld_cg_s32(&rt->active);
+    const double acc0 = ld_cg_f64(&acc[0]);
+    const double rk2 = ld_cg_f64(&acc[k >= 1 ? k - 1 : 0]);      // ||r(x^(k-1))||^2
+    const double ry2_rt = ld_cg_f64(&rt->res_y2);
+    const int mode = ci.mode, init = ci.init, max_iter = ci.max_iter;
+    const float tol = ci.tol;
+    if (!active) return true;
+    if (check && k >= 1 && mode == kModeConsistent) {
         // normaliser: the residual of the inertial start, measured by the
         // warm-start selection when a learned start was evaluated, else the
         // residual of the start iterate itself
-        const bool own_start = !(ci.init >= 2 && a.warm_active);
-        const double ry2 = (k == 1 && own_start) ? acc0 : __ldcg(&rt->res_y2);
+        const bool own_start = !(init >= 2 && a.warm_active);
+        const double ry2 = (k == 1 && own_start) ? acc0 : ry2_rt;
         if (k == 1 && designated) {
             rt->res0_2 = acc0;
             if (own_start) rt->res_y2 = acc0;
@@ -507,18 +552,18 @@ __device__ __forceinline__ bool cloth_done(const IterArgs& a, int c, int k, bool
             if (designated) { rt->status = -6; rt->used = k - 1; rt->resf_2 = rk2; rt->active = 0; }
             return true;
         }
-        if (ci.tol > 0.f && rk2 <= (double)ci.tol * (double)ci.tol * ry2) {
+        if (tol > 0.f && rk2 <= (double)tol * (double)tol * ry2) {
             if (designated) { rt->used = k - 1; rt->resf_2 = rk2; rt->active = 0; }
             return true;
         }
-        if (k > ci.max_iter) {   // this cloth's cap: x^max_iter and its residual are final
-            if (designated) { rt->used = ci.max_iter; rt->resf_2 = rk2; rt->active = 0; }
+        if (k > max_iter) {   // this cloth's cap: x^max_iter and its residual are final
+            if (designated) { rt->used = max_iter; rt->resf_2 = rk2; rt->active = 0; }
             return true;
         }
     }
-    if (k >= ci.max_iter && (k > ci.max_iter || !a.have_final)) {
-        if (designated && (check || ci.mode != kModeConsistent)) {
-            rt->used = ci.max_iter; rt->resf_2 = -1.0; rt->active = 0;
+    if (k >= max_iter && (k > max_iter || !a.have_final)) {
+        if (designated && (check || mode != kModeConsistent)) {
+            rt->used = max_iter; rt->resf_2 = -1.0; rt->active = 0;
         }
         return true;
     }
