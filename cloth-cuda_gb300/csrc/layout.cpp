@@ -570,6 +570,7 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             ph.vm_npad = npad;
             ph.vm_nslot = (int)vm_nslot;
             L.max_vm_slot = std::max(L.max_vm_slot, 32 * (size_t)nlocal + 12 * (size_t)vm_nslot);
+            L.max_vm_nslot = std::max(L.max_vm_nslot, (int)vm_nslot);
             ph.nent = cnt[nown];
             ph.nbnd = nbnd_p;
             ph.ncell_a = ncell_a;

@@ -1,13 +1,21 @@
 // Streaming sweep: one launch per Jacobi sweep (replayed from the frame's CUDA
-// graph) with a persistent grid of a few blocks per SM.  Each block walks the
-// patches blockIdx.x, blockIdx.x + gridDim.x, ... and double-buffers them in
-// shared memory: while it projects and gathers patch i, the TMA engine copies
-// the contiguous per-patch data of patch i + gridDim.x (cell and lone hinge
-// records, gather pointers and entries, halo index list, y, d^k and d^(k-1)
-// of the owned vertices) into the other stage with cp.async.bulk, completing
-// on an mbarrier.  Only the halo vertices' y and d^k are gathered with plain
-// loads.  The per-vertex arithmetic is the one of the per-patch sweep
-// (same device functions, same slot order), so the results are bitwise equal.
+// graph) on a persistent grid of resident blocks.  Block b walks the patches
+// b, b + G, b + 2G, ... (G = grid size) and software-pipelines their staging
+// so that the memory round trips of patch p + G overlap the arithmetic of
+// patch p:
+//   - the TMA engine bulk-copies p + G's contiguous lists (halo index list,
+//     gather pointers, y, d^k and d^(k-1) of the owned vertices) into the
+//     other of two stages while the block projects patch p's cells;
+//   - after p's cell step every thread gathers p + G's halo y and d^k into
+//     that stage with asynchronous 16-byte copies (cp.async), which land
+//     while the block gathers patch p's contributions;
+//   - the header of p + 2G is copied into a three-entry ring, and the
+//     per-cloth decision for p + G is taken one patch ahead.
+// Cell and hinge records are read from global memory as in the per-patch
+// sweep, so a stage holds only vertex data and several blocks fit per SM.
+// The per-vertex arithmetic, the vertex-major slots and the gather order are
+// those of the per-patch sweep (same device functions), so the results are
+// bitwise equal.
 //
 // Every mbarrier wait is bounded by a clock64 budget.  On expiry the block
 // records an error code, waits (bounded) for its copies still in flight and
@@ -98,149 +106,251 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 
 __device__ __forceinline__ uint32_t round16(uint32_t b) { return (b + 15u) & ~15u; }
 
-// Thread 0: header of patch p into *hs, then every contiguous list of the
-// patch into `stage`, completing on `bar`.
+// Per-thread asynchronous 16-byte copy global -> shared (cached in L2 only),
+// tracked by the thread's cp.async groups.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)),
+                 "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Bulk prefetch into L2 of the 16-byte-aligned part of [p, p + bytes).
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes)
+{
+    const size_t g = __cvta_generic_to_global(p);
+    const size_t b = (g + 15) & ~(size_t)15;
+    const size_t e = (g + bytes) & ~(size_t)15;
+    if (e > b) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b), "r"((unsigned)(e - b)) : "memory");
+}
+
+// Thread 0: every contiguous list of patch h into `stage`, completing on
+// `bar`; the patch's cell records are started towards L2.
 __device__ __forceinline__ void issue_patch(const IterArgs& a, const StreamArgs& sa, const float4* Dk,
-                                            const float4* Dn, int p, PatchHdr* hs, unsigned char* stage,
+                                            const float4* Dn, const PatchHdr& h, unsigned char* stage,
                                             uint64_t* bar)
 {
-    const PatchHdr h = a.patches[p];
-    *hs = h;
-    const uint32_t b_cell = (uint32_t)sizeof(CellRec) * h.ncell, b_hin = 32u * h.nhinge;
-    const uint32_t b_ptr = round16(4u * (h.nown + 1)), b_ent = round16(2u * h.nent);
+    const uint32_t b_ptr = round16(4u * (h.nown + 1));
     const uint32_t b_hidx = round16(4u * (h.nlocal - h.nown)), b_v = 16u * h.nown;
-    mbar_arrive_expect_tx(bar, b_cell + b_hin + b_ptr + b_ent + b_hidx + 3 * b_v);
-    if (b_cell) bulk_g2s(stage + sa.o_cell, a.cells + h.cell_off, b_cell, bar);
-    if (b_hin) bulk_g2s(stage + sa.o_hin, a.hinges + h.hinge_off, b_hin, bar);
+    mbar_arrive_expect_tx(bar, b_ptr + b_hidx + 3 * b_v);
     bulk_g2s(stage + sa.o_ptr, a.csr_ptr + h.csr_off, b_ptr, bar);
-    if (b_ent) bulk_g2s(stage + sa.o_ent, a.csr_ent + h.ent_off, b_ent, bar);
     if (b_hidx) bulk_g2s(stage + sa.o_hidx, a.halo + h.halo_off, b_hidx, bar);
     if (b_v) {
         bulk_g2s(stage + sa.o_y, a.Y + h.vbegin, b_v, bar);
         bulk_g2s(stage + sa.o_d, Dk + h.vbegin, b_v, bar);
         bulk_g2s(stage + sa.o_dp, Dn + h.vbegin, b_v, bar);
     }
+    prefetch_l2(a.cells + h.cell_off, sizeof(CellRec) * (size_t)h.ncell);
+}
+
+// Thread 0: asynchronous copy of a patch header (80 bytes, 16-byte aligned
+// in both spaces) into the header ring.
+__device__ __forceinline__ void copy_header(const PatchHdr* src, PatchHdr* dst)
+{
+    static_assert(sizeof(PatchHdr) % 16 == 0, "PatchHdr is copied in 16-byte pieces");
+    #pragma unroll
+    for (int i = 0; i < (int)(sizeof(PatchHdr) / 16); ++i)
+        cp_async16(reinterpret_cast<unsigned char*>(dst) + 16 * i, reinterpret_cast<const unsigned char*>(src) + 16 * i);
+}
+
+// Per-patch decision, taken by thread 0 one patch ahead.
+struct PatchDecision {
+    int   skip;    // cloth done: nothing to compute
+    int   ro;      // residual only (no update)
+    float omega;   // Chebyshev weight of this sweep
+    float gamma;   // under-relaxation
+};
+
+__device__ __forceinline__ void decide(const IterArgs& a, const PatchHdr& h, int p, int k, int res_only,
+                                       PatchDecision* out)
+{
+    const int c = h.cloth;
+    const ClothInfo& ci = a.cinfo[c];
+    PatchDecision d;
+    d.skip = cloth_done(a, c, k, p == ci.patch_begin) ? 1 : 0;
+    d.ro = (res_only != 0 || k >= ci.max_iter) ? 1 : 0;
+    d.omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
+    d.gamma = ci.gamma;
+    *out = d;
+}
+
+// Every thread: its share of patch h's halo y and d^k into `stage`.
+__device__ __forceinline__ void gather_halo(const IterArgs& a, const StreamArgs& sa, const float4* Dk,
+                                            const PatchHdr& h, unsigned char* stage, int tid, int nt)
+{
+    const int* hidx = reinterpret_cast<const int*>(stage + sa.o_hidx);
+    float4* sy = reinterpret_cast<float4*>(stage + sa.o_y);
+    float4* sd = reinterpret_cast<float4*>(stage + sa.o_d);
+    const int nown = h.nown, nlocal = h.nlocal;
+    for (int l = nown + tid; l < nlocal; l += nt) {
+        const int g = hidx[l - nown];
+        cp_async16(&sy[l], &a.Y[g]);
+        cp_async16(&sd[l], &Dk[g]);
+    }
+    cp_async_commit();
 }
 
 template <int MODE, int NT>
-__global__ void __launch_bounds__(NT) k_stream(IterArgs a, StreamArgs sa, int k, int res_only)
+__global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs sa, int k, int res_only)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ PatchHdr ph[2];
+    __shared__ __align__(16) PatchHdr hring[3];
+    __shared__ PatchDecision dec[2];
     __shared__ float red[NT / 32];
-    __shared__ int skip;
-    __shared__ float omega;
     const int tid = threadIdx.x;
+    const int G = gridDim.x;
     const float4* __restrict__ Dk = (k & 1) ? a.buf[1] : a.buf[0];
     float4* __restrict__ Dn = (k & 1) ? a.buf[0] : a.buf[1];
     float* cx = reinterpret_cast<float*>(smem_raw + sa.slot_off);
     float* cy = cx + sa.max_nslot;
     float* cz = cy + sa.max_nslot;
+    const int p0 = blockIdx.x;
+    if (p0 >= sa.npatch) return;
 
+    // prologue: headers of the first two patches, the first patch's lists,
+    // its decision and its halo
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_fence_init();
+        hring[0] = a.patches[p0];
+        if (p0 + G < sa.npatch) copy_header(a.patches + p0 + G, &hring[1]);
+        cp_async_commit();
     }
     __syncthreads();
-    if (tid == 0 && (int)blockIdx.x < sa.npatch)
-        issue_patch(a, sa, Dk, Dn, blockIdx.x, &ph[0], smem_raw, &bar[0]);
-
+    if (tid == 0) {
+        issue_patch(a, sa, Dk, Dn, hring[0], smem_raw, &bar[0]);
+        decide(a, hring[0], p0, k, res_only, &dec[0]);
+    }
     uint32_t parity = 0;   // bit s: parity of the next phase of bar[s]
-    int it = 0;
-    for (int p = blockIdx.x; p < sa.npatch; p += gridDim.x, ++it) {
-        const int s = it & 1;
-        unsigned char* st = smem_raw + s * sa.stage_bytes;
-        const bool got = mbar_wait(&bar[s], (parity >> s) & 1u, sa.spin_budget);
-        parity ^= 1u << s;
-        const bool has_next = p + (int)gridDim.x < sa.npatch;
+    {
+        const bool got = mbar_wait(&bar[0], 0, sa.spin_budget);
+        parity ^= 1u;
         if (!__syncthreads_and(got)) {
-            // give up: record the error, let copies in flight land, leave
             if (tid == 0) {
                 atomicCAS(sa.err, 0, 4);
-                // the drain has its own budget (about 2 s): the copies are
-                // bounded in size and land unless the memory system failed
-                if (!got) mbar_wait(&bar[s], ((parity >> s) & 1u) ^ 1u, 4000000000LL);
+                if (!got) mbar_wait(&bar[0], 0, 4000000000LL);
             }
+            cp_async_wait_all();
             __syncthreads();
             return;
         }
-        if (tid == 0) {
-            if (has_next) {   // stage s^1 was released by the sync that ended the previous patch
-                fence_proxy_async_smem();
-                issue_patch(a, sa, Dk, Dn, p + gridDim.x, &ph[s ^ 1], smem_raw + (s ^ 1) * sa.stage_bytes,
-                            &bar[s ^ 1]);
-            }
-            const PatchHdr& h = ph[s];
-            const ClothInfo& ci = a.cinfo[h.cloth];
-            skip = cloth_done(a, h.cloth, k, p == ci.patch_begin) ? 1 : 0;
-            omega = (k < a.omega_stride) ? a.omega[h.cloth * a.omega_stride + k] : 1.f;
+    }
+    gather_halo(a, sa, Dk, hring[0], smem_raw, tid, NT);
+
+    int it = 0;
+    for (int p = p0; p < sa.npatch; p += G, ++it) {
+        const int s = it & 1;
+        const int q = p + G;
+        unsigned char* st = smem_raw + s * sa.stage_bytes;
+        unsigned char* st1 = smem_raw + (s ^ 1) * sa.stage_bytes;
+        // patch p's stage, header and decision are complete; the other stage
+        // and the slots are free
+        cp_async_wait_all();
+        __syncthreads();
+        const PatchHdr& h = hring[it % 3];
+        if (tid == 0 && q < sa.npatch) {
+            const PatchHdr& hq = hring[(it + 1) % 3];
+            fence_proxy_async_smem();
+            issue_patch(a, sa, Dk, Dn, hq, st1, &bar[s ^ 1]);
+            if (q + G < sa.npatch) copy_header(a.patches + q + G, &hring[(it + 2) % 3]);
+            cp_async_commit();
+            decide(a, hq, q, k, res_only, &dec[s ^ 1]);
         }
-        const PatchHdr& h = ph[s];
-        const int nown = h.nown, nlocal = h.nlocal;
-        float4* sy = reinterpret_cast<float4*>(st + sa.o_y);
-        float4* sd = reinterpret_cast<float4*>(st + sa.o_d);
-        const int* hidx = reinterpret_cast<const int*>(st + sa.o_hidx);
-        for (int l = nown + tid; l < nlocal; l += NT) {
-            const int g = hidx[l - nown];
-            sy[l] = __ldcg(&a.Y[g]);
-            sd[l] = __ldcg(&Dk[g]);
+        const PatchDecision dp_ = dec[s];
+        const float4* sy = reinterpret_cast<const float4*>(st + sa.o_y);
+        const float4* sd = reinterpret_cast<const float4*>(st + sa.o_d);
+
+        // local step of patch p: records from global memory, contributions
+        // to the vertex-major slots.  Odd rounds run in reverse thread order,
+        // so thread 0, which takes the decision above, gets the lighter load.
+        if (!dp_.skip) {
+            const CellRec* __restrict__ cr = a.cells + h.cell_off;
+            const int ncell = h.ncell, nhin = h.nhinge;
+            for (int r = 0; r * NT < ncell; ++r) {
+                const int c = r * NT + ((r & 1) ? NT - 1 - tid : tid);
+                if (c < ncell) {
+                    const CellRec rec = cr[c];
+                    cell_contrib_vm<MODE>(rec, const_cast<float4*>(sy), const_cast<float4*>(sd), cx, cy, cz);
+                }
+            }
+            const HingeRec* __restrict__ hr = a.hinges + h.hinge_off;
+            const uint2* __restrict__ hv = a.hvm + h.hinge_off;
+            for (int e = tid; e < nhin; e += NT) {
+                const HingeRec rec = hr[e];
+                hinge_contrib_vm<MODE>(rec, __ldg(&hv[e]), const_cast<float4*>(sy), const_cast<float4*>(sd), cx,
+                                       cy, cz);
+            }
         }
         __syncthreads();
-        if (!skip) {
-            const int ncell = h.ncell, nhin = h.nhinge;
-            const CellRec* cr = reinterpret_cast<const CellRec*>(st + sa.o_cell);
-            const HingeRec* hr = reinterpret_cast<const HingeRec*>(st + sa.o_hin);
-            for (int c = tid; c < ncell; c += NT) cell_contrib<MODE>(cr[c], sy, sd, c, ncell, cx, cy, cz);
-            for (int e = tid; e < nhin; e += NT) hinge_contrib<MODE>(hr[e], sy, sd, e, 6 * ncell, nhin, cx, cy, cz);
-            __syncthreads();
-            const bool ro = res_only != 0 || k >= a.cinfo[h.cloth].max_iter;
-            const float gamma = a.cinfo[h.cloth].gamma;
+
+        // patch q's halo, gathered while patch p is finished
+        if (q < sa.npatch) {
+            const int b1 = s ^ 1;
+            const bool got = mbar_wait(&bar[b1], (parity >> b1) & 1u, sa.spin_budget);
+            parity ^= 1u << b1;
+            if (!__syncthreads_and(got)) {
+                // give up: record the error, let copies in flight land, leave
+                if (tid == 0) {
+                    atomicCAS(sa.err, 0, 4);
+                    // the drain has its own budget (about 2 s): the copies are
+                    // bounded in size and land unless the memory system failed
+                    if (!got) mbar_wait(&bar[b1], ((parity >> b1) & 1u) ^ 1u, 4000000000LL);
+                }
+                cp_async_wait_all();
+                __syncthreads();
+                return;
+            }
+            gather_halo(a, sa, Dk, hring[(it + 1) % 3], st1, tid, NT);
+        }
+
+        // global step of patch p
+        if (!dp_.skip) {
+            const int nown = h.nown, vbegin = h.vbegin, npad = h.vm_npad;
             const int* cp = reinterpret_cast<const int*>(st + sa.o_ptr);
-            const uint16_t* ce = reinterpret_cast<const uint16_t*>(st + sa.o_ent);
             const float4* sdp = reinterpret_cast<const float4*>(st + sa.o_dp);
             float r2 = 0.f;
             for (int l = tid; l < nown; l += NT) {
-                const float3 f = gather_force(ce, cp[l], cp[l + 1], cx, cy, cz);
-                const int g = h.vbegin + l;
+                const int deg = cp[l + 1] - cp[l];
+                const int hh = gather_half(deg);
+                const float3 f = fadd3(gather_vm(l, 0, hh, npad, cx, cy, cz), gather_vm(l, hh, deg, npad, cx, cy, cz));
+                const int g = vbegin + l;
                 const float4 d = sd[l];
                 const float4 y = sy[l];
                 if (MODE == kModeConsistent) {
                     float rv;
-                    const float4 dp = ro ? d : sdp[l];
-                    const float4 o = update_consistent(d, y, f, dp, gamma, omega, rv);
+                    const float4 dprev = dp_.ro ? d : sdp[l];
+                    const float4 o = update_consistent(d, y, f, dprev, dp_.gamma, dp_.omega, rv);
                     r2 += rv;
-                    if (!ro) Dn[g] = o;
-                } else if (!ro) {
+                    if (!dp_.ro) Dn[g] = o;
+                } else if (!dp_.ro) {
                     Dn[g] = update_literal(d, y, f);
                 }
             }
             if (MODE == kModeConsistent) block_residual<NT>(r2, red, a.acc + (size_t)h.cloth * a.acc_stride + k);
         }
-        __syncthreads();   // stage s, the slots and the header are free again
     }
+    cp_async_wait_all();
 }
 
 // Stage layout: every region starts on a 16-byte boundary.
-bool stream_layout(int max_ncell, int max_nhinge, int max_nown, int max_nent, int max_nhalo, int max_nlocal,
-                   int max_nslot, StreamArgs& sa, size_t& smem)
+bool stream_layout(int max_nown, int max_nhalo, int max_nlocal, int max_vm_nslot, StreamArgs& sa, size_t& smem)
 {
     auto r16 = [](size_t b) { return (b + 15) / 16 * 16; };
     size_t o = 0;
-    sa.o_cell = (int)o; o += sizeof(CellRec) * (size_t)max_ncell;
-    sa.o_hin = (int)o;  o += 32 * (size_t)max_nhinge;
-    sa.o_ptr = (int)o;  o += r16(4 * (size_t)(max_nown + 1));
-    sa.o_ent = (int)o;  o += r16(2 * (size_t)max_nent);
     sa.o_hidx = (int)o; o += r16(4 * (size_t)max_nhalo);
+    sa.o_ptr = (int)o;  o += r16(4 * (size_t)(max_nown + 1));
     sa.o_y = (int)o;    o += 16 * (size_t)max_nlocal;
     sa.o_d = (int)o;    o += 16 * (size_t)max_nlocal;
     sa.o_dp = (int)o;   o += 16 * (size_t)max_nown;
     o = (o + 127) / 128 * 128;
     sa.stage_bytes = (int)o;
     sa.slot_off = (int)(2 * o);
-    sa.max_nslot = max_nslot;
-    smem = 2 * o + 12 * (size_t)max_nslot;
+    sa.max_nslot = max_vm_nslot;
+    smem = 2 * o + 12 * (size_t)max_vm_nslot;
     return smem < (1u << 31);
 }
 

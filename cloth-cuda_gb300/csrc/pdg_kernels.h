@@ -67,20 +67,20 @@ int resident_pick(int nt);
 int resident_max_blocks(int mode, int variant, size_t smem);
 cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t smem, cudaStream_t s);
 
-// Streaming per-sweep kernel (pd_stream.cu): persistent grid, patches
-// double-buffered in shared memory by bulk copies.  Byte offsets of the
-// regions of one stage; the contribution slots follow the two stages.
+// Streaming per-sweep kernel (pd_stream.cu): persistent grid, the vertex
+// data of each block's next patch double-buffered in shared memory by bulk
+// and asynchronous copies.  Byte offsets of the regions of one stage; the
+// vertex-major contribution slots follow the two stages.
 struct StreamArgs {
-    int o_cell, o_hin, o_ptr, o_ent, o_hidx, o_y, o_d, o_dp;
+    int o_hidx, o_ptr, o_y, o_d, o_dp;
     int stage_bytes;
     int slot_off;
-    int max_nslot;
+    int max_nslot;          // vertex-major slots per patch (largest)
     int npatch;
     int* err;               // set when a copy wait times out
     long long spin_budget;  // clock64 cycles a wait may take
 };
-bool stream_layout(int max_ncell, int max_nhinge, int max_nown, int max_nent, int max_nhalo, int max_nlocal,
-                   int max_nslot, StreamArgs& sa, size_t& smem);
+bool stream_layout(int max_nown, int max_nhalo, int max_nlocal, int max_vm_nslot, StreamArgs& sa, size_t& smem);
 int stream_max_blocks(int mode, int nt, size_t smem);
 cudaError_t launch_stream(const IterArgs& a, const StreamArgs& sa, int mode, int nt, int grid, size_t smem, int k,
                           int res_only, cudaStream_t s);

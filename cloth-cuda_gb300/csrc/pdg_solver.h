@@ -26,6 +26,7 @@ struct HostLayout {
     int max_nlocal = 0, max_nslot = 0, max_nown = 0, max_ncell = 0, max_nhinge = 0, max_nent = 0, max_nhalo = 0;
     size_t smem_bytes = 0;          // per-patch sweep kernels (vertex-major slots)
     size_t max_vm_slot = 0;         // largest 32*nlocal + 12*vm_nslot of a patch
+    int max_vm_nslot = 0;           // largest vertex-major slot count of a patch
     size_t smem_resident = 0;       // resident kernel: records, y, d, slots, gather lists
     std::vector<int> perm_global;   // reordered vertex -> index in the batch's caller order
     std::vector<int> perm_local;    // reordered vertex -> index within its cloth

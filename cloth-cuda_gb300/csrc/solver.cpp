@@ -251,8 +251,7 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
         if (!build_layout(s->cloths, s->patch_verts, s->L, err)) return set_error(PDG_ERR_ARG, "%s", err.c_str());
         if (s->kernel == PDG_KERNEL_STREAM) {
             const HostLayout& L = s->L;
-            stream_layout(L.max_ncell, L.max_nhinge, L.max_nown, L.max_nent, L.max_nhalo, L.max_nlocal, L.max_nslot,
-                          s->sargs, s->stream_smem);
+            stream_layout(L.max_nown, L.max_nhalo, L.max_nlocal, L.max_vm_nslot, s->sargs, s->stream_smem);
             if (s->stream_smem + 2048 <= (size_t)smem_optin) break;
         } else if (s->L.smem_bytes + 1024 <= (size_t)std::min(smem_optin, 200 * 1024)) {
             break;

@@ -83,9 +83,9 @@ std::vector<Plan> candidates(bool warm)
     // step's dependent arithmetic)
     for (Plan p : {Plan{PDG_KERNEL_GRAPH, 64, 128}, Plan{PDG_KERNEL_GRAPH, 128, 128}, Plan{PDG_KERNEL_GRAPH, 128, 256},
                    Plan{PDG_KERNEL_GRAPH, 256, 256}, Plan{PDG_KERNEL_GRAPH, 256, 512}, Plan{PDG_KERNEL_GRAPH, 512, 512},
-                   Plan{PDG_KERNEL_GRAPH, 1024, 512}, Plan{PDG_KERNEL_STREAM, 64, 128},
-                   Plan{PDG_KERNEL_STREAM, 128, 256}, Plan{PDG_KERNEL_STREAM, 256, 256},
-                   Plan{PDG_KERNEL_STREAM, 256, 512}})
+                   Plan{PDG_KERNEL_GRAPH, 1024, 512}, Plan{PDG_KERNEL_STREAM, 112, 128},
+                   Plan{PDG_KERNEL_STREAM, 128, 128}, Plan{PDG_KERNEL_STREAM, 160, 128},
+                   Plan{PDG_KERNEL_STREAM, 256, 256}})
         c.push_back(p);
     return c;
 }

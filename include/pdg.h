@@ -56,9 +56,10 @@ extern "C" {
                                     the choice is cached per device and
                                     problem shape for the process           */
 #define PDG_KERNEL_STREAM     5  /* one launch per iteration (CUDA graph) on a
-                                    persistent grid; each block prefetches its
-                                    next patch with bulk copies (TMA) while it
-                                    solves the current one                   */
+                                    persistent grid; each block stages its
+                                    next patch's vertex data with bulk (TMA)
+                                    and asynchronous copies while it solves
+                                    the current one                          */
 
 /* Solver configuration.  Mirrors PDSolverConfig (include/pd_solver.h:4-15);
  * fields after `damping` extend it. */
