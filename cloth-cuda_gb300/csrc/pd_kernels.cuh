@@ -247,7 +247,147 @@ __device__ __forceinline__ void cell_force(const CellRec& r, const float4* sy, c
     o[5] = scale3(q2, r.wx2);
 }
 
-// Corner-major slots (resident and streaming kernels): output k of local
+// ---------------------------------------------------------------------------
+// Packed form of the cell arithmetic: x and y components in one float2 and
+// one two-lane instruction (add/mul/fma .f32x2), z alone.  Every lane is
+// rounded exactly like the scalar operation it replaces (a - b is formed as
+// fma(b, -1, a), which is exact before its single rounding), so the packed
+// functions give the bits of the scalar ones above with about a third fewer
+// floating-point instructions.
+// ---------------------------------------------------------------------------
+struct V3 {
+    float2 xy;
+    float  z;
+};
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ V3 v3(float4 a) { return V3{make_float2(a.x, a.y), a.z}; }
+__device__ __forceinline__ V3 v3(float3 a) { return V3{make_float2(a.x, a.y), a.z}; }
+__device__ __forceinline__ float3 f3(V3 a) { return make_float3(a.xy.x, a.xy.y, a.z); }
+__device__ __forceinline__ V3 vadd(V3 a, V3 b) { return V3{add2(a.xy, b.xy), fadd(a.z, b.z)}; }
+__device__ __forceinline__ V3 vsub(V3 a, V3 b) { return V3{sub2(a.xy, b.xy), fsub(a.z, b.z)}; }
+__device__ __forceinline__ V3 vneg(V3 a) { return V3{make_float2(-a.xy.x, -a.xy.y), -a.z}; }
+__device__ __forceinline__ V3 vscale(V3 a, float s) { return V3{mul2(a.xy, bc2(s)), fmul(a.z, s)}; }
+// a * s + c
+__device__ __forceinline__ V3 vfma(V3 a, float s, V3 c) { return V3{fma2(a.xy, bc2(s), c.xy), ffma(a.z, s, c.z)}; }
+__device__ __forceinline__ float vdot(V3 a, V3 b) { return ffma(a.xy.x, b.xy.x, ffma(a.xy.y, b.xy.y, fmul(a.z, b.z))); }
+
+// (y_j - y_i) + (d_j - d_i)
+__device__ __forceinline__ V3 edge4_p(float4 yi, float4 di, float4 yj, float4 dj)
+{
+    return vadd(vsub(v3(yj), v3(yi)), vsub(v3(dj), v3(di)));
+}
+
+// polar_consistent in packed form
+__device__ __forceinline__ void polar_consistent_p(V3 F0, V3 F1, V3& R0, V3& R1)
+{
+    const float n0sq = vdot(F0, F0);
+    const V3 b0 = n0sq > 1e-20f ? vscale(F0, rsqrtf(n0sq)) : V3{make_float2(1.f, 0.f), 0.f};
+    const float a01 = vdot(F1, b0);
+    const V3 c1 = vfma(b0, -a01, F1);
+    const float n1sq = vdot(c1, c1);
+    V3 b1;
+    if (n1sq > 1e-20f) {
+        b1 = vscale(c1, rsqrtf(n1sq));
+    } else {   // F1 parallel to F0: any unit vector orthogonal to b0
+        float3 q = make_float3(-b0.xy.y, b0.xy.x, 0.f);
+        float nq = ffma(q.x, q.x, fmul(q.y, q.y));
+        if (nq < 1e-20f) { q = make_float3(0.f, -b0.z, b0.xy.y); nq = ffma(q.y, q.y, fmul(q.z, q.z)); }
+        b1 = v3(scale3(q, rsqrtf(nq)));
+    }
+    const float a00 = vdot(b0, F0), a10 = vdot(b1, F0), a11 = vdot(b1, F1);
+    const float s = fadd(a00, a11), t = fsub(a10, a01);
+    const float rr = ffma(s, s, fmul(t, t));
+    float c = 1.f, sn = 0.f;
+    if (rr > 1e-30f) { const float r = rsqrtf(rr); c = fmul(s, r); sn = fmul(t, r); }
+    R0 = vfma(b0, c, vscale(b1, sn));
+    R1 = vfma(b1, c, vscale(vneg(b0), sn));
+}
+
+// tri_force in packed form
+template <int MODE>
+__device__ __forceinline__ void tri_force_p(V3 d1, V3 d2, float4 G, float h2wA, V3& c0, V3& c1, V3& c2)
+{
+    const float g00 = G.x, g10 = G.y, g01 = G.z, g11 = G.w;
+    const V3 F0 = vfma(d1, g00, vscale(d2, g10));
+    const V3 F1 = vfma(d1, g01, vscale(d2, g11));
+    V3 q0, q1;
+    if (MODE == kModeConsistent) {
+        V3 R0, R1;
+        polar_consistent_p(F0, F1, R0, R1);
+        q0 = vscale(vsub(R0, F0), h2wA);
+        q1 = vscale(vsub(R1, F1), h2wA);
+    } else {
+        float3 R0, R1;
+        polar_literal(f3(F0), f3(F1), R0, R1);
+        q0 = vscale(v3(R0), h2wA);
+        q1 = vscale(v3(R1), h2wA);
+    }
+    const float s0 = -fadd(g00, g10), s1 = -fadd(g01, g11);
+    c0 = vfma(q0, s0, vscale(q1, s1));
+    c1 = vfma(q0, g00, vscale(q1, g01));
+    c2 = vfma(q0, g10, vscale(q1, g11));
+}
+
+// hinge_q in packed form
+template <int MODE>
+__device__ __forceinline__ V3 hinge_q_p(V3 e, float h2k, float nrest)
+{
+    if (MODE == kModeConsistent) {
+        const float n2 = vdot(e, e);
+        V3 p = V3{make_float2(0.f, 0.f), 0.f};
+        if (nrest > 1e-10f && n2 > 1e-20f) p = vscale(e, fmul(nrest, rsqrtf(n2)));
+        return vscale(vsub(p, e), h2k);
+    }
+    return v3(hinge_q<MODE>(f3(e), h2k, nrest));
+}
+
+// hinge_force / hinge_force_x in packed form (wx = 0 terms absent: x = false)
+template <int MODE, bool X>
+__device__ __forceinline__ V3 hinge_force_p(V3 e1, V3 e2, V3 e3, V3 ex, V3 x0, float4 w, float wx, float h2k,
+                                            float nrest)
+{
+    float ws = fadd(fadd(w.x, w.y), fadd(w.z, w.w));
+    if (X) ws = fadd(ws, wx);
+    V3 e = vfma(e1, w.y, vfma(e2, w.z, vfma(e3, w.w, vscale(x0, ws))));
+    if (X) e = vfma(ex, wx, e);
+    return hinge_q_p<MODE>(e, h2k, nrest);
+}
+
+// cell_force in packed form (bitwise the same outputs).  It needs more
+// registers at once; the resident kernel, which has them, uses it.
+template <int MODE>
+__device__ __forceinline__ void cell_force_p(const CellRec& r, const float4* sy, const float4* sd, float3 (&o)[6])
+{
+    const int i0 = r.c01 & 0xffffu, i1 = r.c01 >> 16, i2 = r.c23 & 0xffffu, i3 = r.c23 >> 16;
+    const int j1 = r.x12 & 0xffffu, j2 = r.x12 >> 16;
+    const float4 y0 = sy[i0], d0 = sd[i0], y1 = sy[i1], d1 = sd[i1];
+    const float4 y2 = sy[i2], d2 = sd[i2], y3 = sy[i3], d3 = sd[i3];
+    const float4 yx1 = sy[j1], dx1 = sd[j1], yx2 = sy[j2], dx2 = sd[j2];
+    const V3 e01 = edge4_p(y0, d0, y1, d1), e02 = edge4_p(y0, d0, y2, d2), e03 = edge4_p(y0, d0, y3, d3);
+    const V3 e13 = edge4_p(y1, d1, y3, d3);
+    const V3 ex1 = edge4_p(y0, d0, yx1, dx1), ex2 = edge4_p(y0, d0, yx2, dx2);
+    const V3 x0 = vadd(v3(y0), v3(d0));
+    V3 a0, a1, a2, b0, b1, b3;
+    tri_force_p<MODE>(e01, e02, r.G0, r.h2wA0, a0, a1, a2);
+    tri_force_p<MODE>(vneg(e01), e13, r.G1, r.h2wA1, b1, b0, b3);
+    const V3 q0 = hinge_force_p<MODE, false>(e01, e02, e03, e03, x0, r.W0, 0.f, r.h2k0, r.nrest0);
+    const V3 q1 = hinge_force_p<MODE, true>(e01, e02, e03, ex1, x0, r.W1, r.wx1, r.h2k1, r.nrest1);
+    const V3 q2 = hinge_force_p<MODE, true>(e01, e02, e03, ex2, x0, r.W2, r.wx2, r.h2k2, r.nrest2);
+    // t + w0 q0 + w1 q1 + w2 q2, in that order
+    auto acc = [&](V3 t, float w0, float w1, float w2) { return vfma(q2, w2, vfma(q1, w1, vfma(q0, w0, t))); };
+    o[0] = f3(acc(vadd(a0, b0), r.W0.x, r.W1.x, r.W2.x));
+    o[1] = f3(acc(vadd(a1, b1), r.W0.y, r.W1.y, r.W2.y));
+    o[2] = f3(acc(a2, r.W0.z, r.W1.z, r.W2.z));
+    o[3] = f3(acc(b3, r.W0.w, r.W1.w, r.W2.w));
+    o[4] = f3(vscale(q1, r.wx1));
+    o[5] = f3(vscale(q2, r.wx2));
+}
+
+// Corner-major slots (resident kernel): output k of local
 // cell lc at k*ncell + lc, so a warp's stores are unit-stride and free of
 // bank conflicts.
 template <int MODE>
@@ -255,7 +395,7 @@ __device__ __forceinline__ void cell_contrib(const CellRec& r, const float4* sy,
                                              float* cx, float* cy, float* cz)
 {
     float3 o[6];
-    cell_force<MODE>(r, sy, sd, o);
+    cell_force_p<MODE>(r, sy, sd, o);
     #pragma unroll
     for (int k = 0; k < 6; ++k) {
         const int s = k * ncell + lc;
