@@ -490,6 +490,26 @@ __device__ __forceinline__ float3 gather_vm(int l, int j0, int j1, int npad, con
     return make_float3(fx, fy, fz);
 }
 
+// gather_vm for at most M contributions: every slot load is issued before
+// the additions, which run in the same order (same bits).
+template <int M>
+__device__ __forceinline__ float3 gather_vm_u(int l, int j0, int j1, int npad, const float* cx, const float* cy,
+                                              const float* cz)
+{
+    float vx[M], vy[M], vz[M];
+    #pragma unroll
+    for (int i = 0; i < M; ++i) {
+        const bool ok = j0 + i < j1;
+        const int s = ok ? (j0 + i) * npad + l : l;   // always inside the slot arrays
+        vx[i] = cx[s]; vy[i] = cy[s]; vz[i] = cz[s];
+    }
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    #pragma unroll
+    for (int i = 0; i < M; ++i)
+        if (j0 + i < j1) { fx = fadd(fx, vx[i]); fy = fadd(fy, vy[i]); fz = fadd(fz, vz[i]); }
+    return make_float3(fx, fy, fz);
+}
+
 // Jacobi update of one owned vertex in the consistent form:
 // -r = f - m d;  d_hat = d + gamma D^-1 (-r);  d' = omega (d_hat - d_prev) + d_prev.
 __device__ __forceinline__ float4 update_consistent(float4 d, float4 y, float3 f, float4 dp, float gamma,

@@ -285,27 +285,29 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
                                        cy, cz);
             }
         }
-        __syncthreads();
 
-        // patch q's halo, gathered while patch p is finished
+        // patch q's lists have landed (or the wait gave up) and every
+        // thread's contributions to p's slots are stored: one barrier
+        const int b1 = s ^ 1;
+        bool got = true;
         if (q < sa.npatch) {
-            const int b1 = s ^ 1;
-            const bool got = mbar_wait(&bar[b1], (parity >> b1) & 1u, sa.spin_budget);
+            got = mbar_wait(&bar[b1], (parity >> b1) & 1u, sa.spin_budget);
             parity ^= 1u << b1;
-            if (!__syncthreads_and(got)) {
-                // give up: record the error, let copies in flight land, leave
-                if (tid == 0) {
-                    atomicCAS(sa.err, 0, 4);
-                    // the drain has its own budget (about 2 s): the copies are
-                    // bounded in size and land unless the memory system failed
-                    if (!got) mbar_wait(&bar[b1], ((parity >> b1) & 1u) ^ 1u, 4000000000LL);
-                }
-                cp_async_wait_all();
-                __syncthreads();
-                return;
-            }
-            gather_halo(a, sa, Dk, hring[(it + 1) % 3], st1, tid, NT);
         }
+        if (!__syncthreads_and(got)) {
+            // give up: record the error, let copies in flight land, leave
+            if (tid == 0) {
+                atomicCAS(sa.err, 0, 4);
+                // the drain has its own budget (about 2 s): the copies are
+                // bounded in size and land unless the memory system failed
+                if (!got) mbar_wait(&bar[b1], ((parity >> b1) & 1u) ^ 1u, 4000000000LL);
+            }
+            cp_async_wait_all();
+            __syncthreads();
+            return;
+        }
+        // patch q's halo, gathered while patch p is finished
+        if (q < sa.npatch) gather_halo(a, sa, Dk, hring[(it + 1) % 3], st1, tid, NT);
 
         // global step of patch p
         if (!dp_.skip) {
@@ -316,7 +318,9 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
             for (int l = tid; l < nown; l += NT) {
                 const int deg = cp[l + 1] - cp[l];
                 const int hh = gather_half(deg);
-                const float3 f = fadd3(gather_vm(l, 0, hh, npad, cx, cy, cz), gather_vm(l, hh, deg, npad, cx, cy, cz));
+                const float3 f =
+                    deg <= 10 ? fadd3(gather_vm_u<5>(l, 0, hh, npad, cx, cy, cz), gather_vm_u<5>(l, hh, deg, npad, cx, cy, cz))
+                              : fadd3(gather_vm(l, 0, hh, npad, cx, cy, cz), gather_vm(l, hh, deg, npad, cx, cy, cz));
                 const int g = vbegin + l;
                 const float4 d = sd[l];
                 const float4 y = sy[l];
