@@ -155,7 +155,7 @@ __device__ __forceinline__ void copy_header(const PatchHdr* src, PatchHdr* dst)
         cp_async16(reinterpret_cast<unsigned char*>(dst) + 16 * i, reinterpret_cast<const unsigned char*>(src) + 16 * i);
 }
 
-// Per-patch decision, taken by thread 0 one patch ahead.
+// Per-patch decision, taken by one thread one patch ahead.
 struct PatchDecision {
     int   skip;    // cloth done: nothing to compute
     int   ro;      // residual only (no update)
@@ -258,15 +258,18 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
             issue_patch(a, sa, Dk, Dn, hq, st1, &bar[s ^ 1]);
             if (q + G < sa.npatch) copy_header(a.patches + q + G, &hring[(it + 2) % 3]);
             cp_async_commit();
-            decide(a, hq, q, k, res_only, &dec[s ^ 1]);
         }
+        // the decision for q (one memory round trip) is taken by another
+        // warp than the copy issue, so neither warp carries both
+        if (tid == 32 && q < sa.npatch) decide(a, hring[(it + 1) % 3], q, k, res_only, &dec[s ^ 1]);
         const PatchDecision dp_ = dec[s];
         const float4* sy = reinterpret_cast<const float4*>(st + sa.o_y);
         const float4* sd = reinterpret_cast<const float4*>(st + sa.o_d);
 
         // local step of patch p: records from global memory, contributions
         // to the vertex-major slots.  Odd rounds run in reverse thread order,
-        // so thread 0, which takes the decision above, gets the lighter load.
+        // so warps 0 and 1, which issue the copies and take the decision
+        // above, get the lighter load.
         if (!dp_.skip) {
             const CellRec* __restrict__ cr = a.cells + h.cell_off;
             const int ncell = h.ncell, nhin = h.nhinge;
