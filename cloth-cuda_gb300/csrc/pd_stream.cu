@@ -192,8 +192,10 @@ __device__ __forceinline__ void gather_halo(const IterArgs& a, const StreamArgs&
     cp_async_commit();
 }
 
+// Shared memory holds 5 blocks of 128 threads per SM (a 128-vertex patch plan),
+// so the register cap is set for 5 blocks (96 registers) rather than 6.
 template <int MODE, int NT>
-__global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs sa, int k, int res_only)
+__global__ void __launch_bounds__(NT, 640 / NT) k_stream(IterArgs a, StreamArgs sa, int k, int res_only)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar[2];
