@@ -176,6 +176,60 @@ __device__ __forceinline__ void decide(const IterArgs& a, const PatchHdr& h, int
     *out = d;
 }
 
+// Programmatic dependent launch: wait until the grids this one depends on
+// have completed and their memory is visible (returns at once without
+// such a dependency), and allow the dependent grid to be scheduled.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch_dependents()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Thread 0, first patch only: the lists of patch h that the previous sweep
+// does not write (halo index list, gather pointers, y and d^(k-1) of the
+// owned vertices) into `stage`, completing on `bar`.
+__device__ __forceinline__ void issue_static(const IterArgs& a, const StreamArgs& sa, const float4* Dn,
+                                             const PatchHdr& h, unsigned char* stage, uint64_t* bar)
+{
+    const uint32_t b_ptr = round16(4u * (h.nown + 1));
+    const uint32_t b_hidx = round16(4u * (h.nlocal - h.nown)), b_v = 16u * h.nown;
+    mbar_arrive_expect_tx(bar, b_ptr + b_hidx + 2 * b_v);
+    bulk_g2s(stage + sa.o_ptr, a.csr_ptr + h.csr_off, b_ptr, bar);
+    if (b_hidx) bulk_g2s(stage + sa.o_hidx, a.halo + h.halo_off, b_hidx, bar);
+    if (b_v) {
+        bulk_g2s(stage + sa.o_y, a.Y + h.vbegin, b_v, bar);
+        bulk_g2s(stage + sa.o_dp, Dn + h.vbegin, b_v, bar);
+    }
+    prefetch_l2(a.cells + h.cell_off, sizeof(CellRec) * (size_t)h.ncell);
+}
+
+// Thread 0, first patch only: d^k of the owned vertices, completing on `bar`.
+__device__ __forceinline__ void issue_dk(const StreamArgs& sa, const float4* Dk, const PatchHdr& h,
+                                         unsigned char* stage, uint64_t* bar)
+{
+    const uint32_t b_v = 16u * h.nown;
+    mbar_arrive_expect_tx(bar, b_v);
+    if (b_v) bulk_g2s(stage + sa.o_d, Dk + h.vbegin, b_v, bar);
+}
+
+// Every thread, first patch only: its share of the halo y, then of the halo
+// d^k (after the previous sweep completed), into `stage`.
+__device__ __forceinline__ void gather_halo_y(const IterArgs& a, const StreamArgs& sa, const PatchHdr& h,
+                                              unsigned char* stage, int tid, int nt)
+{
+    const int* hidx = reinterpret_cast<const int*>(stage + sa.o_hidx);
+    float4* sy = reinterpret_cast<float4*>(stage + sa.o_y);
+    for (int l = h.nown + tid; l < h.nlocal; l += nt) cp_async16(&sy[l], &a.Y[hidx[l - h.nown]]);
+}
+__device__ __forceinline__ void gather_halo_d(const StreamArgs& sa, const float4* Dk, const PatchHdr& h,
+                                              unsigned char* stage, int tid, int nt)
+{
+    const int* hidx = reinterpret_cast<const int*>(stage + sa.o_hidx);
+    float4* sd = reinterpret_cast<float4*>(stage + sa.o_d);
+    for (int l = h.nown + tid; l < h.nlocal; l += nt) cp_async16(&sd[l], &Dk[hidx[l - h.nown]]);
+    cp_async_commit();
+}
+
 // Every thread: its share of patch h's halo y and d^k into `stage`.
 __device__ __forceinline__ void gather_halo(const IterArgs& a, const StreamArgs& sa, const float4* Dk,
                                             const PatchHdr& h, unsigned char* stage, int tid, int nt)
@@ -198,7 +252,7 @@ template <int MODE, int NT>
 __global__ void __launch_bounds__(NT, 640 / NT) k_stream(IterArgs a, StreamArgs sa, int k, int res_only)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[3];   // the two stages; the first patch's static lists
     __shared__ __align__(16) PatchHdr hring[3];
     __shared__ PatchDecision dec[2];
     __shared__ float red[NT / 32];
@@ -212,21 +266,45 @@ __global__ void __launch_bounds__(NT, 640 / NT) k_stream(IterArgs a, StreamArgs 
     const int p0 = blockIdx.x;
     if (p0 >= sa.npatch) return;
 
-    // prologue: headers of the first two patches, the first patch's lists,
-    // its decision and its halo
+    // Prologue.  Launched as a programmatic dependent of the previous sweep,
+    // the block may start while that sweep's last blocks still run.  Before
+    // griddepcontrol.wait it reads only what no sweep of this frame writes
+    // (patch headers, halo lists, gather pointers, y) or what the sweep
+    // before the previous one wrote (d^(k-1)); it signals its own
+    // dependents only after the wait, so when the next sweep's blocks start
+    // early, the previous sweep has completed.  d^k, the per-sweep sums and
+    // the runtime records are read after the wait.
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
         mbar_fence_init();
         hring[0] = a.patches[p0];
         if (p0 + G < sa.npatch) copy_header(a.patches + p0 + G, &hring[1]);
         cp_async_commit();
     }
     __syncthreads();
+    if (tid == 0) issue_static(a, sa, Dn, hring[0], smem_raw, &bar[2]);
+    {
+        const bool got = mbar_wait(&bar[2], 0, sa.spin_budget);
+        if (!__syncthreads_and(got)) {
+            if (tid == 0) {
+                atomicCAS(sa.err, 0, 4);
+                if (!got) mbar_wait(&bar[2], 0, 4000000000LL);
+            }
+            cp_async_wait_all();
+            __syncthreads();
+            return;
+        }
+    }
+    gather_halo_y(a, sa, hring[0], smem_raw, tid, NT);
+    grid_dep_wait();
+    grid_dep_launch_dependents();
     if (tid == 0) {
-        issue_patch(a, sa, Dk, Dn, hring[0], smem_raw, &bar[0]);
+        issue_dk(sa, Dk, hring[0], smem_raw, &bar[0]);
         decide(a, hring[0], p0, k, res_only, &dec[0]);
     }
+    gather_halo_d(sa, Dk, hring[0], smem_raw, tid, NT);
     uint32_t parity = 0;   // bit s: parity of the next phase of bar[s]
     {
         const bool got = mbar_wait(&bar[0], 0, sa.spin_budget);
@@ -241,7 +319,6 @@ __global__ void __launch_bounds__(NT, 640 / NT) k_stream(IterArgs a, StreamArgs 
             return;
         }
     }
-    gather_halo(a, sa, Dk, hring[0], smem_raw, tid, NT);
 
     int it = 0;
     for (int p = p0; p < sa.npatch; p += G, ++it) {
@@ -395,14 +472,25 @@ int stream_max_blocks(int mode, int nt, size_t smem)
 }
 
 cudaError_t launch_stream(const IterArgs& a, const StreamArgs& sa, int mode, int nt, int grid, size_t smem, int k,
-                          int res_only, cudaStream_t s)
+                          int res_only, cudaStream_t s, bool after_sweep)
 {
     void* f = pick_stream(mode, nt);
     if (!f || grid <= 0) return cudaErrorInvalidValue;
     IterArgs ac = a;
     StreamArgs sc = sa;
     void* args[] = {&ac, &sc, &k, &res_only};
-    return cudaLaunchKernel(f, dim3(grid), dim3(nt), args, smem, s);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(nt);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    // directly after another sweep: start as a programmatic dependent of it
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = after_sweep ? 1 : 0;
+    return cudaLaunchKernelExC(&cfg, f, args);
 }
 
 }  // namespace pdg

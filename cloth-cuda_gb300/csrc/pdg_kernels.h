@@ -82,7 +82,9 @@ struct StreamArgs {
 };
 bool stream_layout(int max_nown, int max_nhalo, int max_nlocal, int max_vm_nslot, StreamArgs& sa, size_t& smem);
 int stream_max_blocks(int mode, int nt, size_t smem);
+// after_sweep: the previous launch on the stream is a sweep of this kernel;
+// the launch then overlaps its tail (programmatic dependent launch).
 cudaError_t launch_stream(const IterArgs& a, const StreamArgs& sa, int mode, int nt, int grid, size_t smem, int k,
-                          int res_only, cudaStream_t s);
+                          int res_only, cudaStream_t s, bool after_sweep);
 
 }  // namespace pdg

@@ -129,7 +129,7 @@ cudaError_t launch_sweep(pdg_solver* s, const IterArgs& a, int k, int res_only, 
 {
     if (s->kernel == PDG_KERNEL_STREAM) {
         s->sargs.spin_budget = s->wait_budget;
-        return launch_stream(a, s->sargs, s->mode, s->nt, s->persist_grid, s->stream_smem, k, res_only, st);
+        return launch_stream(a, s->sargs, s->mode, s->nt, s->persist_grid, s->stream_smem, k, res_only, st, k >= 1);
     }
     return launch_iter(a, s->mode, s->nt, s->L.npatch, s->L.smem_bytes, k, res_only, st, s->carveout);
 }
