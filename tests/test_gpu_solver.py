@@ -382,6 +382,30 @@ def test_stream_kernel_walks_many_patches_per_block(pdg, oracle):
     assert abs(stg[0]["res_final"] - sts[0]["res_final"]) <= 1e-5 * stg[0]["res_final"]
 
 
+def test_stream_sweeps_overlapping_their_predecessor_match_graph(pdg, oracle):
+    # Each streaming sweep after the first is a programmatic dependent launch
+    # of the previous one: its blocks start while that sweep's last blocks
+    # still run and stage what the previous sweep does not write.  Many
+    # frames of 24 sweeps, through the frame's CUDA graph and through the
+    # eagerly launched timing path, must keep the bits of the per-patch graph
+    # kernel.
+    m, c, cfg, sc, a = scene(pdg, oracle, n=257, side=2.0, max_iterations=24, kernel=pdg.KERNEL_GRAPH,
+                             patch_verts=128, block_threads=128)
+    g = pdg.Solver(cfg, m, c)
+    cfg.kernel = pdg.KERNEL_STREAM
+    s = pdg.Solver(cfg, m, c)
+    assert s.launch_info()["kernel"] == pdg.KERNEL_STREAM
+    for _ in range(3):
+        stg = g.step(2)
+        sts = s.step(2)
+        assert all(np.array_equal(u, w) for u, w in zip(g.get_state(), s.get_state()))
+        # the per-sweep sums are double atomics, so only their order may differ
+        assert abs(stg[0]["res_final"] - sts[0]["res_final"]) <= 1e-9 * stg[0]["res_final"]
+    g.time_frames(3)
+    s.time_frames(3)
+    assert all(np.array_equal(u, w) for u, w in zip(g.get_state(), s.get_state()))
+
+
 def test_stream_kernel_tolerance_batch(pdg, oracle):
     scenes = [scene(pdg, oracle, n=n, seed=n, side=0.5, ks=20.0, kb=1e-3, rho=0.9, max_iterations=400,
                     tolerance=1e-4) for n in (9, 10, 11, 40)]
