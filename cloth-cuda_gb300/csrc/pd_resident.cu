@@ -90,15 +90,18 @@ __device__ __forceinline__ bool poll_neighbours(int lane, const int* nb, int nnb
 constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 
 // Local step over the records with list index in [t0, t1) (cells) and
-// [e0, e1) (lone hinges), read from the patch's copy in shared memory.
+// [e0, e1) (lone hinges), read from the patch's copy in shared memory.  With
+// `rev` the records go to the threads in reverse order (the last thread takes
+// the first record), which leaves the first threads free; a record's
+// contributions and slots do not depend on the thread that computes them.
 template <int MODE, int NT>
 __device__ __forceinline__ void local_records(const CellRec* rc, const HingeRec* rh,
                                               const float4* sy, const float4* sd, int ncell, int nhin, int t0, int t1,
-                                              int e0, int e1, float* cx, float* cy, float* cz)
+                                              int e0, int e1, float* cx, float* cy, float* cz, bool rev = false)
 {
-    const int tid = threadIdx.x;
-    for (int t = t0 + tid; t < t1; t += NT) cell_contrib<MODE>(rc[t], sy, sd, t, ncell, cx, cy, cz);
-    for (int e = e0 + tid; e < e1; e += NT) hinge_contrib<MODE>(rh[e], sy, sd, e, 6 * ncell, nhin, cx, cy, cz);
+    const int j0 = rev ? NT - 1 - (int)threadIdx.x : (int)threadIdx.x;
+    for (int t = t0 + j0; t < t1; t += NT) cell_contrib<MODE>(rc[t], sy, sd, t, ncell, cx, cy, cz);
+    for (int e = e0 + j0; e < e1; e += NT) hinge_contrib<MODE>(rh[e], sy, sd, e, 6 * ncell, nhin, cx, cy, cz);
 }
 
 // Jacobi update of owned vertex l with force f: o = d^(k+1), d = d^k.
@@ -294,10 +297,15 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             named_arrive(2, NTT);
-            // Phase B: the remaining records, then the interior vertices
+            // Phase B: the remaining records, then the interior vertices.  At
+            // most a warp's worth of records goes to the last threads, which
+            // are idle while the first ones sum the boundary vertices; a larger
+            // phase B stays on the first threads, which reach it after the
+            // boundary offsets are out, so that it does not compete with the
+            // boundary sums the neighbouring patches wait for.
             if (!skip_k)
                 local_records<MODE, NT>(rc, rh, sy, sd, ncell, nhin, ph.ncell_a, ncell, ph.nhin_a, nhin, cx,
-                                                cy, cz);
+                                                cy, cz, (ncell - ph.ncell_a) + (nhin - ph.nhin_a) <= 32);
             named_sync(1, NT);
             if (!skip_k && own && tid >= ph.nbnd) {
                 vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
