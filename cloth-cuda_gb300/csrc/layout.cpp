@@ -1,6 +1,8 @@
-// Host-side construction of the device layout: Morton reorder of every
-// cloth, cut into patches, local triangle/hinge records with 16-bit vertex
-// references, and per-vertex gather lists (CSR) over contribution slots.
+// Host-side construction of the device layout: every cloth reordered so that
+// its patches are compact tiles (recursive coordinate bisection, Z-order
+// inside a tile), cut into patches, local triangle/hinge records with 16-bit
+// vertex references, and per-vertex gather lists (CSR) over contribution
+// slots.
 #include "pdg_solver.h"
 
 #include <algorithm>
@@ -48,6 +50,48 @@ void morton_order(const MeshData& m, std::vector<int>& perm)
     std::sort(key.begin(), key.end());
     perm.resize(m.N);
     for (int i = 0; i < m.N; ++i) perm[i] = (int)(key[i] & 0xffffffffu);
+}
+
+// Vertex order whose consecutive runs of `pv` vertices are compact regions of
+// the rest shape: recursive coordinate bisection.  A range holding np
+// patches is split across its bounding box's longest axis so that the lower
+// part holds floor(np/2) whole patches; a range of one patch keeps the
+// Z-order curve inside (ties by vertex index, so the order is deterministic).
+void bisection_order(const MeshData& m, int pv, std::vector<int>& perm)
+{
+    std::vector<int> z;
+    morton_order(m, z);
+    std::vector<int> zrank(m.N);
+    for (int i = 0; i < m.N; ++i) zrank[z[i]] = i;
+    perm = z;
+    struct Range { int b, e; };
+    std::vector<Range> stack{{0, m.N}};
+    while (!stack.empty()) {
+        const Range r = stack.back();
+        stack.pop_back();
+        const int n = r.e - r.b;
+        const int np = (n + pv - 1) / pv;
+        if (np <= 1) {
+            std::sort(perm.begin() + r.b, perm.begin() + r.e, [&](int a, int b) { return zrank[a] < zrank[b]; });
+            continue;
+        }
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int i = r.b; i < r.e; ++i)
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = std::min(lo[d], m.rest[3 * perm[i] + d]);
+                hi[d] = std::max(hi[d], m.rest[3 * perm[i] + d]);
+            }
+        int ax = 0;
+        for (int d = 1; d < 3; ++d)
+            if (hi[d] - lo[d] > hi[ax] - lo[ax]) ax = d;
+        const int mid = r.b + (np / 2) * pv;
+        std::nth_element(perm.begin() + r.b, perm.begin() + mid, perm.begin() + r.e, [&](int a, int b) {
+            const float fa = m.rest[3 * a + ax], fb = m.rest[3 * b + ax];
+            return fa < fb || (fa == fb && a < b);
+        });
+        stack.push_back({r.b, mid});
+        stack.push_back({mid, r.e});
+    }
 }
 
 // Dm_inv of a triangle whose corners are rotated by r places, (p0, p1, p2)
@@ -289,7 +333,7 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
         const pdg_config& cfg = cl[ci].cfg;
         const int N = m.N;
         std::vector<int> perm, iperm(N);
-        morton_order(m, perm);
+        bisection_order(m, patch_verts, perm);
         for (int i = 0; i < N; ++i) iperm[perm[i]] = i;
         const float h2 = cfg.dt * cfg.dt;
         std::vector<CellBuild> cells;
@@ -426,7 +470,7 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             for (int l = 0; l < nown; ++l) vloc[p0 + l] = l;
             for (size_t q = 0; q < halo.size(); ++q) vloc[halo[q]] = nown + (int)q;
             auto loc = [&](int o) { return (uint32_t)vloc[iperm[o]]; };
-            // record placement follows the Morton order of the lowest local
+            // record placement follows the vertex order of the lowest local
             // corner, so the lanes of a warp touch neighbouring vertices and
             // neighbouring slots (fewer shared-memory bank conflicts); the
             // summation order is fixed separately below

@@ -1,9 +1,11 @@
 // Device data layout of the PD solver, shared by the host patch builder
 // (layout.cpp) and the kernels (pd_kernels.cu).
 //
-// The cloths of a solver are concatenated in one Morton-reordered vertex
-// numbering.  Each cloth's vertices are cut into patches of up to
-// `patch_verts` consecutive vertices; one CUDA block processes one patch.  A
+// The cloths of a solver are concatenated in one reordered vertex numbering:
+// recursive coordinate bisection of each cloth's rest shape into compact
+// tiles of `patch_verts` vertices, Z-order inside a tile.  Each cloth's
+// vertices are cut into patches of up to `patch_verts` consecutive vertices
+// (one tile each); one CUDA block processes one patch.  A
 // patch carries every cell and every lone bend hinge that touches one of its
 // owned vertices, with vertex references rewritten as 16-bit local indices
 // into the patch's vertex list (owned vertices first, then the halo).

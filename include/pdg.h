@@ -8,7 +8,8 @@
  * interface each group replaces is cited beside it.
  *
  * Vertex arrays crossing this boundary are AoS xyz float32 in the caller's
- * vertex order.  Internally the solver keeps a Morton-reordered float4 layout;
+ * vertex order.  Internally the solver keeps a reordered float4 layout (compact
+ * patches by recursive coordinate bisection, Z-order inside a patch);
  * the permutation never leaves the library.
  *
  * Threading: one host thread per handle.  Work is stream-ordered on the
