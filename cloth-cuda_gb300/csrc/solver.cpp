@@ -192,17 +192,20 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     const pdg_config& c0 = cfgs[0];
     s->mode = c0.mode;
     s->have_final = (c0.mode == PDG_MODE_CONSISTENT) && (c0.compute_final_residual || c0.tolerance > 0.f);
-    s->nt = c0.block_threads ? c0.block_threads : 256;
+    // defaults: the streaming kernel's measured best plan (128-vertex patches,
+    // 128 threads); the per-patch graph kernel's, 256 / 256
+    const bool stream_plan = c0.kernel == PDG_KERNEL_AUTO || c0.kernel == PDG_KERNEL_STREAM;
+    s->nt = c0.block_threads ? c0.block_threads : (stream_plan ? 128 : 256);
     if (s->nt != 128 && s->nt != 256 && s->nt != 512)
         return set_error(PDG_ERR_ARG, "block_threads must be 128, 256 or 512");
-    s->patch_verts = c0.patch_verts ? c0.patch_verts : 256;
+    s->patch_verts = c0.patch_verts ? c0.patch_verts : (stream_plan ? 128 : 256);
     if (c0.smem_carveout < 0 || c0.smem_carveout > 100) return set_error(PDG_ERR_ARG, "smem_carveout must be in [0, 100]");
     s->carveout = c0.smem_carveout;
     if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
     if (c0.kernel == PDG_KERNEL_AUTOTUNE) return autotune_create(n, cfgs, meshes, cons, stream, out);
     if (c0.kernel < PDG_KERNEL_AUTO || (c0.kernel > PDG_KERNEL_RESIDENT && c0.kernel != PDG_KERNEL_STREAM))
         return set_error(PDG_ERR_ARG, "unknown kernel");
-    s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_GRAPH : c0.kernel;
+    s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_STREAM : c0.kernel;
     for (const auto& c : s->cloths)
         s->any_warm = s->any_warm || c.cfg.init == PDG_INIT_WARMSTART || c.cfg.init == PDG_INIT_WARMSTART_KEEP;
     if (s->any_warm && (c0.kernel == PDG_KERNEL_PERSISTENT || c0.kernel == PDG_KERNEL_RESIDENT))

@@ -47,7 +47,8 @@ extern "C" {
                                  residual judge; for evaluating the network) */
 
 /* Launch structure of the iteration loop. */
-#define PDG_KERNEL_AUTO       0  /* resident when it fits, else graph (no timing) */
+#define PDG_KERNEL_AUTO       0  /* resident when it fits, else the streaming
+                                    kernel (no timing)                       */
 #define PDG_KERNEL_GRAPH      1  /* one fused launch per iteration, frame in a CUDA graph */
 #define PDG_KERNEL_PERSISTENT 2  /* one cooperative launch per frame, bounded grid barrier */
 #define PDG_KERNEL_RESIDENT   3  /* persistent, one patch per block, records kept on chip */
