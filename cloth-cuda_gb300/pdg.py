@@ -88,6 +88,9 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.pdg_last_error_string.restype = C.c_char_p
         L.pdg_version.restype = C.c_char_p
+        # the per-frame host-buffer call takes plain addresses (int or None):
+        # converting them costs far less than building ctypes pointers
+        L.pdg_solver_step_host.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 5
         _lib = L
     return _lib
 
@@ -100,6 +103,9 @@ def _check(rc):
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+_F32 = np.dtype(np.float32)
 
 
 def _f32(a):
@@ -306,12 +312,16 @@ class Solver:
         copy fastest); any may be None.  Input and output may be the same
         arrays."""
         n = int(self.offsets[-1])
+        addr = {}
         for arr in (x_in, v_in, x_out, v_out):
-            if arr is not None and (arr.dtype != np.float32 or not arr.flags.c_contiguous or arr.size != 3 * n):
-                raise ValueError("state arrays must be C-contiguous float32 with N*3 elements")
+            if arr is not None and id(arr) not in addr:
+                if arr.dtype != _F32 or not arr.flags.c_contiguous or arr.size != 3 * n:
+                    raise ValueError("state arrays must be C-contiguous float32 with N*3 elements")
+                addr[id(arr)] = arr.ctypes.data
+        a = lambda arr: addr[id(arr)] if arr is not None else None
         st = (FrameStats * self.n)() if stats else None
-        q = lambda a: _p(a) if a is not None else None
-        _check(lib().pdg_solver_step_host(self.h, nframes, q(x_in), q(v_in), q(x_out), q(v_out), st))
+        _check(lib().pdg_solver_step_host(self.h, nframes, a(x_in), a(v_in), a(x_out), a(v_out),
+                                          C.cast(st, C.c_void_p) if stats else None))
         return [s.as_dict() for s in st] if stats else None
 
     def set_pin_targets(self, targets, cloth=0):
