@@ -406,6 +406,20 @@ def test_stream_sweeps_overlapping_their_predecessor_match_graph(pdg, oracle):
     assert all(np.array_equal(u, w) for u, w in zip(g.get_state(), s.get_state()))
 
 
+def test_auto_plan_streams_what_the_resident_kernel_cannot_hold(pdg, oracle):
+    # 513x513 cloth: more 448-vertex patches than SMs, so AUTO falls back to
+    # the streaming kernel at its default 128-vertex / 128-thread plan
+    m, c, cfg, sc, a = scene(pdg, oracle, n=513, side=2.0, max_iterations=8, kernel=pdg.KERNEL_AUTO)
+    s = pdg.Solver(cfg, m, c)
+    info = s.launch_info()
+    assert info["kernel"] == pdg.KERNEL_STREAM
+    assert (info["patch_verts"], info["block_threads"]) == (128, 128)
+    cfg.kernel = pdg.KERNEL_GRAPH
+    g = pdg.Solver(cfg, m, c)
+    s.step(1, stats=False); g.step(1, stats=False)
+    assert all(np.array_equal(u, w) for u, w in zip(g.get_state(), s.get_state()))
+
+
 def test_stream_kernel_tolerance_batch(pdg, oracle):
     scenes = [scene(pdg, oracle, n=n, seed=n, side=0.5, ks=20.0, kb=1e-3, rho=0.9, max_iterations=400,
                     tolerance=1e-4) for n in (9, 10, 11, 40)]
