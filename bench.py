@@ -164,6 +164,47 @@ def cpu_baseline_sample(wl, seed=0, iters=1):
     return sc.N / frame_s, dt, frame_s, sc.N
 
 
+def accuracy_vs_f64(pdg, m, c, cfg, what):
+    """Positions, velocities and residual of one frame of the solve (GPU, the
+    default launch plan: every plan gives the same bits) against the oracle's
+    float64 Jacobi-Chebyshev run of the same sweep count, both from the rest
+    shape at rest.  Part of the CPU leg: the oracle is only the checker."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.build()
+    cfg.kernel = pdg.KERNEL_AUTO
+    s = pdg.Solver(cfg, m, c)
+    st = s.step(1)[0]
+    x, v = s.get_state()
+    a = m.arrays(); ca = c.arrays()
+    kb = float(ca["bend_k"][0]) if len(ca["bend_k"]) else 0.0
+    sc = orc.Scene(a["rest"], a["tris"], k_stretch=ca["k_stretch"], k_bend=kb, pins=ca["pins"], h=cfg.dt,
+                   gravity=cfg.gravity, wind=tuple(cfg.wind), damping=cfg.damping)
+    x0 = a["rest"].astype(np.float64).reshape(-1)
+    t0 = time.perf_counter()
+    x64, v64, info = sc.step_jacobi(x0, np.zeros_like(x0), st["iterations"], rho=cfg.rho)
+    dt = time.perf_counter() - t0
+    rel = lambda p, q: float(np.linalg.norm(np.asarray(p, np.float64).reshape(-1) - q) / max(np.linalg.norm(q), 1e-300))
+    res64 = float(info["res"][-1] / info["res_y"])
+    return {"sample": what, "sweeps": int(st["iterations"]), "position_rel_err": rel(x, x64),
+            "velocity_rel_err": rel(v, v64), "rel_residual_gpu": float(st["rel_residual"]),
+            "rel_residual_f64": res64, "f64_seconds": round(dt, 2)}
+
+
+def accuracy_sample(pdg, scenes, wl, meshes, cons, cfgs, seed):
+    """(mesh, constraints, config, description) of the accuracy check: the
+    workload itself up to 257x257, a 257x257 cloth with the same cell size and
+    physics for larger ones, the batch's first cloth."""
+    cfg = type(cfgs[0]).from_buffer_copy(cfgs[0])
+    if wl["kind"] != "plain":
+        return meshes[0], cons[0], cfg, "the batch's first cloth (%d vertices)" % meshes[0].N
+    if wl["n"] <= 257:
+        return meshes[0], cons[0], cfg, "the workload (%d vertices)" % meshes[0].N
+    side = wl["side"] * 256 / (wl["n"] - 1)
+    m, c = scenes.hanging(257, side, ks=wl["ks"], kb=wl["kb"], seed=seed)
+    return m, c, cfg, "a 257x257 cloth with the workload's cell size (%.2f m side) and physics" % side
+
+
 def run_reference(args, rank, world):
     wl = WORKLOADS[args.workload]
     if rank != 0:
@@ -307,7 +348,9 @@ def run_ours(args, rank, world, local_rank):
     value = N * world * args.steps / total_s
     e2e_value = N * world * args.steps / e2e_s
     cpu = None
+    acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        acc = accuracy_vs_f64(pdg, *accuracy_sample(pdg, scenes, wl, meshes, cons, cfgs, rank))
         v_cpu, dt_cpu, frame_s, n_s = cpu_baseline_sample(wl, iters=1)
         cpu = {"value": v_cpu, "unit": "vertex-steps/s", "cores": 1, "kind": "port",
                "sample": "reference CPU path (stretch-only local/global + sparse LDL^T) restated in the oracle: "
@@ -343,6 +386,7 @@ def run_ours(args, rank, world, local_rank):
                                   "HBM copy peak is not a DRAM utilisation" % (Bs_full / 1e6)) if Bs_full < 100e6
                          else "working set %.0f MB per sweep streams from HBM" % (Bs_full / 1e6)},
             "cpu_baseline": cpu,
+            "accuracy_vs_f64": acc,
             "clocks": clocks,
             "gpu_launches": launches,
         }
