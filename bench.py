@@ -164,6 +164,22 @@ def cpu_baseline_sample(wl, seed=0, iters=1):
     return sc.N / frame_s, dt, frame_s, sc.N
 
 
+def host_info():
+    """Core count and CPU model of the host the CPU legs ran on."""
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            key = line.split(":")[0].strip().lower()
+            if key in ("model name", "cpu model") and not model:
+                model = line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    if not model:
+        import platform
+        model = platform.machine()
+    return {"nproc": os.cpu_count(), "cpu": model}
+
+
 def accuracy_vs_f64(pdg, m, c, cfg, what):
     """Positions, velocities and residual of one frame of the solve (GPU, the
     default launch plan: every plan gives the same bits) against the oracle's
@@ -234,7 +250,7 @@ def run_reference(args, rank, world):
                    "note": "reference CPU path restated in the oracle (Eigen absent here and on the GPU host): "
                            "stretch-only, 50 local/global iterations per frame with a sparse LDL^T each; each step "
                            "times one iteration of one frame and scales by 50"},
-        "cpu_baseline": {"value": value, "unit": "vertex-steps/s", "cores": 1, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "vertex-steps/s", "cores": 1, "kind": "port", "host": host_info(),
                          "sample": "1 of the 50 local/global iterations of frame 1 (%s), scaled x50"
                                    % ("257x257 cloth" if wl.get("n", 0) >= 257 else "%dx%d cloth" % (
                                        wl.get("n", 73), wl.get("n", 73)))},
@@ -352,7 +368,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         acc = accuracy_vs_f64(pdg, *accuracy_sample(pdg, scenes, wl, meshes, cons, cfgs, rank))
         v_cpu, dt_cpu, frame_s, n_s = cpu_baseline_sample(wl, iters=1)
-        cpu = {"value": v_cpu, "unit": "vertex-steps/s", "cores": 1, "kind": "port",
+        cpu = {"value": v_cpu, "unit": "vertex-steps/s", "cores": 1, "kind": "port", "host": host_info(),
                "sample": "reference CPU path (stretch-only local/global + sparse LDL^T) restated in the oracle: "
                          "1 of the 50 iterations of frame 1 of a %d-vertex cloth took %.2f s, scaled x50"
                          % (n_s, dt_cpu)}
