@@ -174,6 +174,16 @@ def host_info():
                 model = line.split(":", 1)[1].strip()
     except OSError:
         pass
+    if not model:   # Arm hosts: /proc/cpuinfo has no model name, lscpu has
+        try:
+            out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                                 timeout=10).stdout
+            for line in out.splitlines():
+                if line.lower().startswith("model name:"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
     if not model:
         import platform
         model = platform.machine()
