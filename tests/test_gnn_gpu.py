@@ -135,3 +135,26 @@ def test_keep_mode_always_uses_the_learned_start(pdg):
         st = s.step(1)
     assert all(x["warm_start_used"] == 1 for x in st)
     assert all(np.isfinite(x["res_initial"]) and x["status"] == 0 for x in st)
+
+
+@pytest.mark.parametrize("init_name", ["INIT_WARMSTART", "INIT_WARMSTART_KEEP"])
+def test_learned_start_on_the_streaming_kernel_matches_graph(pdg, init_name):
+    # The learned start (judged or always kept) is selected before the first
+    # sweep; the streaming kernel's sweeps then give the per-patch kernel's bits
+    import scenes
+    init = getattr(pdg, init_name)
+    w = pdg.WarmStart(seed=3)
+    outs = []
+    for kern in (pdg.KERNEL_GRAPH, pdg.KERNEL_STREAM):
+        # the same patch plan for both, so the network sees the same layout
+        ms, cs, cfgs, _ = scenes.batch(5, seed=21, max_iterations=24, tolerance=0.0, n_range=(17, 41),
+                                       kernel=kern, init=init, patch_verts=128, block_threads=128)
+        s = pdg.Solver(cfgs, ms, cs)
+        assert s.launch_info()["kernel"] == kern
+        w.attach(s)
+        sts = [s.step(1) for _ in range(3)]
+        outs.append((s.get_state_all(), [[x["warm_start_used"] for x in st] for st in sts]))
+    (xa, va), ua = outs[0]
+    (xb, vb), ub = outs[1]
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    assert ua == ub
