@@ -568,13 +568,13 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.csr_ent.resize(e0 + cnt[nown]);
             for (int l = 0; l <= nown; ++l) L.csr_ptr.push_back(cnt[l]);
             std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-            // Two slot addressings hold the same contributions.  Corner-major
-            // (resident and streaming kernels, summed through the gather
-            // lists): output k of cell lc at k*ncell + lc, hinge corner a at
-            // 6*ncell + a*nhin + lh.  Vertex-major (per-patch sweep kernels):
-            // contribution j of owned vertex l at j*npad + l, so a warp's
-            // gather loads are unit-stride and need no list entries; halo
-            // corners and absent outputs get 0xffff and store nothing.
+            // Vertex-major slot addressing (every kernel): contribution j of
+            // owned vertex l at j*npad + l, so a warp's gather loads are
+            // unit-stride and need no list entries; halo corners and absent
+            // outputs get 0xffff and store nothing.  The per-vertex lists of
+            // corner-major slot numbers (output k of cell lc at k*ncell + lc,
+            // hinge corner a at 6*ncell + a*nhin + lh) stay on the host as the
+            // record of each vertex's canonical summation order.
             int maxdeg = 0;
             for (int l = 0; l < nown; ++l) maxdeg = std::max(maxdeg, cnt[l + 1] - cnt[l]);
             const int npad = nown | 1;
@@ -626,8 +626,9 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             L.max_nown = std::max(L.max_nown, nown);
             L.max_ncell = std::max(L.max_ncell, ncell);
             L.max_nhinge = std::max(L.max_nhinge, nhin);
-            const size_t res = sizeof(CellRec) * (size_t)ncell + sizeof(HingeRec) * (size_t)nhin + 32 * (size_t)nlocal +
-                               12 * (size_t)nslot + 4 * (size_t)(nown + 1) + 2 * (size_t)cnt[nown];
+            const size_t res = sizeof(CellRec) * (size_t)ncell + sizeof(HingeRec) * (size_t)nhin +
+                               8 * (size_t)((nhin + 1) & ~1) + 32 * (size_t)nlocal + 12 * (size_t)vm_nslot +
+                               4 * (size_t)(nown + 1);
             L.smem_resident = std::max(L.smem_resident, (res + 15) / 16 * 16);
             L.patches.push_back(ph);
         }

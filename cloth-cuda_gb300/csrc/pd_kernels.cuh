@@ -387,23 +387,7 @@ __device__ __forceinline__ void cell_force_p(const CellRec& r, const float4* sy,
     o[5] = f3(vscale(q2, r.wx2));
 }
 
-// Corner-major slots (resident kernel): output k of local
-// cell lc at k*ncell + lc, so a warp's stores are unit-stride and free of
-// bank conflicts.
-template <int MODE>
-__device__ __forceinline__ void cell_contrib(const CellRec& r, const float4* sy, const float4* sd, int lc, int ncell,
-                                             float* cx, float* cy, float* cz)
-{
-    float3 o[6];
-    cell_force_p<MODE>(r, sy, sd, o);
-    #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const int s = k * ncell + lc;
-        cx[s] = o[k].x; cy[s] = o[k].y; cz[s] = o[k].z;
-    }
-}
-
-// Vertex-major slots (per-patch sweep kernels): the record carries each
+// Vertex-major slots (every sweep kernel): the record carries each
 // output's slot address (0xffff for a halo corner or an absent output).
 template <int MODE>
 __device__ __forceinline__ void cell_contrib_vm(const CellRec& r, const float4* sy, const float4* sd, float* cx,
@@ -418,23 +402,18 @@ __device__ __forceinline__ void cell_contrib_vm(const CellRec& r, const float4* 
         if (vm[k] != 0xffffu) { cx[vm[k]] = o[k].x; cy[vm[k]] = o[k].y; cz[vm[k]] = o[k].z; }
 }
 
-// Lone hinge: slot s of local hinge e_ sits at hbase + s*nhin + e_ (hbase =
-// 6*ncell).
+// Vertex-major slots with the packed cell arithmetic (same bits).
 template <int MODE>
-__device__ __forceinline__ void hinge_contrib(const HingeRec& r, const float4* sy, const float4* sd, int e_,
-                                              int hbase, int nhin, float* cx, float* cy, float* cz)
+__device__ __forceinline__ void cell_contrib_vm_p(const CellRec& r, const float4* sy, const float4* sd, float* cx,
+                                                  float* cy, float* cz)
 {
-    const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
-    const float4 y0 = sy[i0], d0 = sd[i0];
-    const float3 x0 = make_float3(fadd(y0.x, d0.x), fadd(y0.y, d0.y), fadd(y0.z, d0.z));
-    const float4 w = r.w;
-    const float3 q = hinge_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), edge(sy, sd, i0, i3), x0, w,
-                                       r.h2k, r.nrest);
-    const int s0 = hbase + e_, s1 = s0 + nhin, s2 = s1 + nhin, s3 = s2 + nhin;
-    cx[s0] = fmul(w.x, q.x); cy[s0] = fmul(w.x, q.y); cz[s0] = fmul(w.x, q.z);
-    cx[s1] = fmul(w.y, q.x); cy[s1] = fmul(w.y, q.y); cz[s1] = fmul(w.y, q.z);
-    cx[s2] = fmul(w.z, q.x); cy[s2] = fmul(w.z, q.y); cz[s2] = fmul(w.z, q.z);
-    cx[s3] = fmul(w.w, q.x); cy[s3] = fmul(w.w, q.y); cz[s3] = fmul(w.w, q.z);
+    float3 o[6];
+    cell_force_p<MODE>(r, sy, sd, o);
+    const uint32_t vm[6] = {r.vm01 & 0xffffu, r.vm01 >> 16, r.vm23 & 0xffffu, r.vm23 >> 16,
+                            r.vm45 & 0xffffu, r.vm45 >> 16};
+    #pragma unroll
+    for (int k = 0; k < 6; ++k)
+        if (vm[k] != 0xffffu) { cx[vm[k]] = o[k].x; cy[vm[k]] = o[k].y; cz[vm[k]] = o[k].z; }
 }
 
 template <int MODE>
@@ -454,31 +433,12 @@ __device__ __forceinline__ void hinge_contrib_vm(const HingeRec& r, uint2 hs, co
     if (s3 != 0xffffu) { cx[s3] = fmul(w.w, q.x); cy[s3] = fmul(w.w, q.y); cz[s3] = fmul(w.w, q.z); }
 }
 
-// Sum of the contribution slots of list entries [b, e), in list order.
-template <class IDX>
-__device__ __forceinline__ float3 gather_slots(const IDX* ent, int b, int e, const float* cx, const float* cy,
-                                               const float* cz)
-{
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int q = b; q < e; ++q) {
-        const int s = ent[q];
-        fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
-    }
-    return make_float3(fx, fy, fz);
-}
-
 // The force on an owned vertex is defined as (sum of the first half of its
-// list) + (sum of the second half), the first half holding ceil(deg/2)
-// entries, each half in list order.  Every kernel forms exactly this, so
+// contributions) + (sum of the second half), the first half holding
+// ceil(deg/2) of them, each half in the canonical order (the cloth's cells,
+// then its lone hinges).  Every kernel forms exactly this, so
 // one that gives the two halves to two threads produces the same bits.
 __device__ __forceinline__ int gather_half(int deg) { return (deg + 1) >> 1; }
-template <class IDX>
-__device__ __forceinline__ float3 gather_force(const IDX* ent, int b, int e, const float* cx, const float* cy,
-                                               const float* cz)
-{
-    const int h = b + gather_half(e - b);
-    return fadd3(gather_slots(ent, b, h, cx, cy, cz), gather_slots(ent, h, e, cx, cy, cz));
-}
 // vertex-major slots: contribution j of vertex l at j*npad + l
 __device__ __forceinline__ float3 gather_vm(int l, int j0, int j1, int npad, const float* cx, const float* cy,
                                             const float* cz)

@@ -1,7 +1,8 @@
 // Resident persistent PD kernel: one cooperative launch per frame, one patch
-// per block for the whole frame.  The patch's cell and hinge records, gather
-// lists, y and d^k live in shared memory and each thread keeps its owned
-// vertex's previous offset d^(k-1) in a register.  Per sweep only the owned
+// per block for the whole frame.  The patch's cell and hinge records, the
+// hinges' slot addresses, the gather pointers, y and d^k live in shared
+// memory (vertex-major contribution slots, as in the per-sweep kernels), and
+// each thread keeps its owned vertex's previous offset d^(k-1) in a register.  Per sweep only the owned
 // offsets go out to L2 and the halo offsets come back.
 //
 // Synchronisation between sweeps: with fixed sweep counts a block waits only
@@ -95,13 +96,13 @@ constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 // the first record), which leaves the first threads free; a record's
 // contributions and slots do not depend on the thread that computes them.
 template <int MODE, int NT>
-__device__ __forceinline__ void local_records(const CellRec* rc, const HingeRec* rh,
+__device__ __forceinline__ void local_records(const CellRec* rc, const HingeRec* rh, const uint2* hvs,
                                               const float4* sy, const float4* sd, int ncell, int nhin, int t0, int t1,
                                               int e0, int e1, float* cx, float* cy, float* cz, bool rev = false)
 {
     const int j0 = rev ? NT - 1 - (int)threadIdx.x : (int)threadIdx.x;
-    for (int t = t0 + j0; t < t1; t += NT) cell_contrib<MODE>(rc[t], sy, sd, t, ncell, cx, cy, cz);
-    for (int e = e0 + j0; e < e1; e += NT) hinge_contrib<MODE>(rh[e], sy, sd, e, 6 * ncell, nhin, cx, cy, cz);
+    for (int t = t0 + j0; t < t1; t += NT) cell_contrib_vm_p<MODE>(rc[t], sy, sd, cx, cy, cz);
+    for (int e = e0 + j0; e < e1; e += NT) hinge_contrib_vm<MODE>(rh[e], hvs[e], sy, sd, cx, cy, cz);
 }
 
 // Jacobi update of owned vertex l with force f: o = d^(k+1), d = d^k.
@@ -117,12 +118,13 @@ __device__ __forceinline__ void vertex_update_f(float3 f, int l, const float4* s
 
 // Gather by one thread and update.
 template <int MODE>
-__device__ __forceinline__ void vertex_update(const uint16_t* sent, const int* sptr, int l, const float4* sy,
+__device__ __forceinline__ void vertex_update(int npad, const int* sptr, int l, const float4* sy,
                                               const float4* sd, const float* cx, const float* cy, const float* cz,
                                               float4 dprev, float gamma, float omega, float4& o, float4& d, float& r2)
 {
-    vertex_update_f<MODE>(gather_force(sent, sptr[l], sptr[l + 1], cx, cy, cz), l, sy, sd, dprev, gamma, omega, o,
-                          d, r2);
+    const int deg = sptr[l + 1] - sptr[l], h = gather_half(deg);
+    vertex_update_f<MODE>(fadd3(gather_vm(l, 0, h, npad, cx, cy, cz), gather_vm(l, h, deg, npad, cx, cy, cz)), l, sy,
+                          sd, dprev, gamma, omega, o, d, r2);
 }
 
 // Block sum of r2 over the NT compute threads (named barrier 1), added to
@@ -175,17 +177,19 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     if (tid == 0) ph = a.patches[blockIdx.x];
     __syncthreads();
     const int nown = ph.nown, nlocal = ph.nlocal, ncell = ph.ncell, nhin = ph.nhinge;
-    // shared memory: the patch's records (read every sweep), y and d of the
-    // local vertices, the contribution slots and the gather lists
+    // shared memory: the patch's records (read every sweep), the hinges' slot
+    // addresses, y and d of the local vertices, the vertex-major contribution
+    // slots and the gather pointers
     CellRec* rc = reinterpret_cast<CellRec*>(smem);
     HingeRec* rh = reinterpret_cast<HingeRec*>(rc + ncell);
-    float4* sy = reinterpret_cast<float4*>(rh + nhin);
+    uint2* hvs = reinterpret_cast<uint2*>(rh + nhin);
+    float4* sy = reinterpret_cast<float4*>(hvs + ((nhin + 1) & ~1));
     float4* sd = sy + nlocal;
     float* cx = reinterpret_cast<float*>(sd + nlocal);
-    float* cy = cx + ph.nslot;
-    float* cz = cy + ph.nslot;
-    int* sptr = reinterpret_cast<int*>(cz + ph.nslot);
-    uint16_t* sent = reinterpret_cast<uint16_t*>(sptr + nown + 1);
+    float* cy = cx + ph.vm_nslot;
+    float* cz = cy + ph.vm_nslot;
+    int* sptr = reinterpret_cast<int*>(cz + ph.vm_nslot);
+    const int npad = ph.vm_npad;
 
     {
         const uint4* src = reinterpret_cast<const uint4*>(a.cells + ph.cell_off);
@@ -195,13 +199,13 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
         const uint4* hsrc = reinterpret_cast<const uint4*>(a.hinges + ph.hinge_off);
         uint4* hdst = reinterpret_cast<uint4*>(rh);
         for (int q = tid; q < 2 * nhin; q += NTT) hdst[q] = __ldg(&hsrc[q]);
+        for (int q = tid; q < nhin; q += NTT) hvs[q] = __ldg(&a.hvm[ph.hinge_off + q]);
     }
-    // gather lists and Chebyshev weights in shared memory
+    // gather pointers (per-vertex contribution counts) and Chebyshev weights
     for (int l = tid; l <= nown; l += NTT) sptr[l] = a.csr_ptr[ph.csr_off + l];
     for (int k = tid; k < a.omega_stride && k < kResOmega; k += NTT) som[k] = a.omega[ph.cloth * a.omega_stride + k];
     __syncthreads();
-    const int nent = sptr[nown];
-    for (int q = tid; q < nent; q += NTT) sent[q] = a.csr_ent[ph.ent_off + q];
+
 
     // predict the owned vertices; the cloth's first block resets its record
     const int c = ph.cloth;
@@ -274,7 +278,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // each list), then the boundary vertices, which the neighbouring
             // patches read; the signal warp publishes them while phase B runs.
             if (!skip_k)
-                local_records<MODE, NT>(rc, rh, sy, sd, ncell, nhin, 0, ph.ncell_a, 0, ph.nhin_a, cx, cy, cz);
+                local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, 0, ph.ncell_a, 0, ph.nhin_a, cx, cy, cz);
             named_sync(1, NT);
             // The boundary vertices' sums are on the neighbours' critical path:
             // when the block has room, thread l sums the first half of vertex
@@ -282,18 +286,18 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // the owners' warps wait, the helpers' warps only arrive).
             if (!skip_k && split_a) {
                 if (tid < ph.nbnd) {
-                    const int b = sptr[tid], e = sptr[tid + 1];
-                    p1 = gather_slots(sent, b, b + gather_half(e - b), cx, cy, cz);
+                    const int deg = sptr[tid + 1] - sptr[tid];
+                    p1 = gather_vm(tid, 0, gather_half(deg), npad, cx, cy, cz);
                 } else if (tid >= hb && tid < hb + ph.nbnd) {
-                    const int l = tid - hb, b = sptr[l], e = sptr[l + 1];
-                    part[l] = gather_slots(sent, b + gather_half(e - b), e, cx, cy, cz);
+                    const int l = tid - hb, deg = sptr[l + 1] - sptr[l];
+                    part[l] = gather_vm(l, gather_half(deg), deg, npad, cx, cy, cz);
                 }
                 if (tid < hb) named_sync(4, 2 * hb);
                 else if (tid < 2 * hb) named_arrive(4, 2 * hb);
             }
             if (!skip_k && tid < ph.nbnd) {
                 if (split_a) vertex_update_f<MODE>(fadd3(p1, part[tid]), tid, sy, sd, dprev, gamma, omega_k, o, d, r2);
-                else         vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                else         vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             named_arrive(2, NTT);
@@ -304,11 +308,11 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // boundary offsets are out, so that it does not compete with the
             // boundary sums the neighbouring patches wait for.
             if (!skip_k)
-                local_records<MODE, NT>(rc, rh, sy, sd, ncell, nhin, ph.ncell_a, ncell, ph.nhin_a, nhin, cx,
+                local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, ph.ncell_a, ncell, ph.nhin_a, nhin, cx,
                                                 cy, cz, (ncell - ph.ncell_a) + (nhin - ph.nhin_a) <= 32);
             named_sync(1, NT);
             if (!skip_k && own && tid >= ph.nbnd) {
-                vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             // every record has read d^k: the owned offsets move on
@@ -338,10 +342,10 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
             float r2 = 0.f;
             if (!skip_k) {
-                if (comp) local_records<MODE, NT>(rc, rh, sy, sd, ncell, nhin, 0, ncell, 0, nhin, cx, cy, cz);
+                if (comp) local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, 0, ncell, 0, nhin, cx, cy, cz);
                 __syncthreads();
                 if (own) {
-                    vertex_update<MODE>(sent, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                    vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                     if (!res_only) {
                         ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
                         sd[tid] = o;

@@ -100,7 +100,6 @@ struct IterArgs {
     const HingeRec*  hinges;
     const uint2*     hvm;         // per hinge: vertex-major slots of corners 0 | 1 << 16, 2 | 3 << 16
     const int*       csr_ptr;
-    const uint16_t*  csr_ent;
     const ClothInfo* cinfo;
     ClothRT*         crt;
     const float*     omega;       // per cloth, omega_stride entries: omega_k

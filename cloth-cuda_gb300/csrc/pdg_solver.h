@@ -100,7 +100,6 @@ struct pdg_solver {
     unsigned long long frame_seq = 0;
     int acc_stride = 1;
     int nbr_sync = 0;
-    pdg::DevBuf<uint16_t> csr_ent;
     pdg::DevBuf<pdg::PatchHdr> patches;
     pdg::DevBuf<pdg::CellRec> cells;
     pdg::DevBuf<pdg::HingeRec> hinges;

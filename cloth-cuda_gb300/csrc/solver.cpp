@@ -61,7 +61,6 @@ int upload_all(pdg_solver* s)
     }
     CK(s->halo.upload(L.halo, st));
     CK(s->csr_ptr.upload(L.csr_ptr, st));
-    CK(s->csr_ent.upload(L.csr_ent, st));
     CK(s->patches.upload(L.patches, st));
     CK(s->cells.upload(L.cells, st));
     CK(s->hinges.upload(L.hinges, st));
@@ -100,7 +99,7 @@ IterArgs iter_args(pdg_solver* s)
 {
     IterArgs a;
     a.patches = s->patches.p; a.halo = s->halo.p; a.cells = s->cells.p; a.hinges = s->hinges.p; a.hvm = s->hvm.p;
-    a.csr_ptr = s->csr_ptr.p; a.csr_ent = s->csr_ent.p; a.cinfo = s->cinfo.p; a.crt = s->crt.p;
+    a.csr_ptr = s->csr_ptr.p; a.cinfo = s->cinfo.p; a.crt = s->crt.p;
     a.omega = s->omega.p; a.omega_stride = s->L.omega_stride;
     a.Y = s->Y.p; a.buf[0] = s->A.p; a.buf[1] = s->B.p; a.ncloth = s->L.ncloth;
     a.acc = s->acc.p; a.acc_stride = s->acc_stride;
