@@ -123,8 +123,9 @@ __device__ __forceinline__ void vertex_update(int npad, const int* sptr, int l, 
                                               float4 dprev, float gamma, float omega, float4& o, float4& d, float& r2)
 {
     const int deg = sptr[l + 1] - sptr[l], h = gather_half(deg);
-    vertex_update_f<MODE>(fadd3(gather_vm(l, 0, h, npad, cx, cy, cz), gather_vm(l, h, deg, npad, cx, cy, cz)), l, sy,
-                          sd, dprev, gamma, omega, o, d, r2);
+    const float3 f = deg <= 10 ? fadd3(gather_vm_u<5>(l, 0, h, npad, cx, cy, cz), gather_vm_u<5>(l, h, deg, npad, cx, cy, cz))
+                               : fadd3(gather_vm(l, 0, h, npad, cx, cy, cz), gather_vm(l, h, deg, npad, cx, cy, cz));
+    vertex_update_f<MODE>(f, l, sy, sd, dprev, gamma, omega, o, d, r2);
 }
 
 // Block sum of r2 over the NT compute threads (named barrier 1), added to
@@ -287,10 +288,12 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             if (!skip_k && split_a) {
                 if (tid < ph.nbnd) {
                     const int deg = sptr[tid + 1] - sptr[tid];
-                    p1 = gather_vm(tid, 0, gather_half(deg), npad, cx, cy, cz);
+                    p1 = deg <= 10 ? gather_vm_u<5>(tid, 0, gather_half(deg), npad, cx, cy, cz)
+                                   : gather_vm(tid, 0, gather_half(deg), npad, cx, cy, cz);
                 } else if (tid >= hb && tid < hb + ph.nbnd) {
                     const int l = tid - hb, deg = sptr[l + 1] - sptr[l];
-                    part[l] = gather_vm(l, gather_half(deg), deg, npad, cx, cy, cz);
+                    part[l] = deg <= 10 ? gather_vm_u<5>(l, gather_half(deg), deg, npad, cx, cy, cz)
+                                        : gather_vm(l, gather_half(deg), deg, npad, cx, cy, cz);
                 }
                 if (tid < hb) named_sync(4, 2 * hb);
                 else if (tid < 2 * hb) named_arrive(4, 2 * hb);
