@@ -170,7 +170,6 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     __shared__ float red[NTT / 32];
     __shared__ int skip;
     __shared__ int sig_ok;
-    __shared__ float3 part[NT / 2];   // second halves of the boundary vertices' sums
     __shared__ float som[kResOmega];   // Chebyshev weights of this cloth
     const IterArgs& a = p.it;
     const int tid = threadIdx.x;
@@ -254,10 +253,6 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
         }
     } else if (nbr) {
         // ---- compute threads, neighbour synchronisation ----
-        // helpers for the boundary sums: the warps right after the boundary
-        // warps, when the block has that many
-        const int hb = 32 * ((ph.nbnd + 31) / 32);
-        const bool split_a = ph.nbnd > 0 && 2 * hb <= NT;
         for (int k = 0; k < nsweep; ++k) {
             if (k > 0) {   // the neighbours' d^k: wait for the signal warp, then load the halo
                 named_sync(3, NTT);
@@ -273,7 +268,6 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 k < a.omega_stride ? (k < kResOmega ? som[k] : a.omega[c * a.omega_stride + k]) : 1.f;
             const bool res_only = k >= ci.max_iter;
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
-            float3 p1 = make_float3(0.f, 0.f, 0.f);
             float r2 = 0.f;
             // Phase A: the records through boundary vertices (a prefix of
             // each list), then the boundary vertices, which the neighbouring
@@ -282,25 +276,12 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, 0, ph.ncell_a, 0, ph.nhin_a, cx, cy, cz);
             named_sync(1, NT);
             // The boundary vertices' sums are on the neighbours' critical path:
-            // when the block has room, thread l sums the first half of vertex
-            // l's list and helper thread hb + l the second half (barrier 4:
-            // the owners' warps wait, the helpers' warps only arrive).
-            if (!skip_k && split_a) {
-                if (tid < ph.nbnd) {
-                    const int deg = sptr[tid + 1] - sptr[tid];
-                    p1 = deg <= 10 ? gather_vm_u<5>(tid, 0, gather_half(deg), npad, cx, cy, cz)
-                                   : gather_vm(tid, 0, gather_half(deg), npad, cx, cy, cz);
-                } else if (tid >= hb && tid < hb + ph.nbnd) {
-                    const int l = tid - hb, deg = sptr[l + 1] - sptr[l];
-                    part[l] = deg <= 10 ? gather_vm_u<5>(l, gather_half(deg), deg, npad, cx, cy, cz)
-                                        : gather_vm(l, gather_half(deg), deg, npad, cx, cy, cz);
-                }
-                if (tid < hb) named_sync(4, 2 * hb);
-                else if (tid < 2 * hb) named_arrive(4, 2 * hb);
-            }
+            // one thread per vertex, every slot load issued before the
+            // additions.  (Splitting each sum over an owner and a helper
+            // thread joined by a named barrier, the two halves of its
+            // definition, was slower once the loads were hoisted.)
             if (!skip_k && tid < ph.nbnd) {
-                if (split_a) vertex_update_f<MODE>(fadd3(p1, part[tid]), tid, sy, sd, dprev, gamma, omega_k, o, d, r2);
-                else         vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             named_arrive(2, NTT);
