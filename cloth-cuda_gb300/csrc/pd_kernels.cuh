@@ -704,13 +704,13 @@ __device__ __forceinline__ void reset_rt(ClothRT* crt, double* acc, int acc_stri
 
 // y = x + h v + h^2 a (w = mass); start offset d^0 = x^0 - y into both
 // buffers (w = inverse diagonal, -1 for pinned vertices).
-__device__ __forceinline__ void predict_vertex(int i, const float4* X, const float4* V, const float4* aux,
-                                               const float* mass, const int* vcloth, const ClothInfo* cinfo,
-                                               const float4* warm, float4* Y, float4* A, float4* B)
+__device__ __forceinline__ void predict_vertex_xv(int i, float4 x, float4 v, const float4* aux, const float* mass,
+                                                  const int* vcloth, const ClothInfo* cinfo, const float4* warm,
+                                                  float4* Y, float4* A, float4* B)
 {
     const ClothInfo& ci = cinfo[vcloth[i]];
     const float h = ci.h, h2 = fmul(h, h);
-    const float4 x = __ldcg(&X[i]), v = __ldcg(&V[i]), au = __ldcg(&aux[i]);
+    const float4 au = __ldcg(&aux[i]);
     float4 y;
     y.x = ffma(h2, ci.ext[0], ffma(h, v.x, x.x));
     y.y = ffma(h2, ci.ext[1], ffma(h, v.y, x.y));
@@ -724,6 +724,13 @@ __device__ __forceinline__ void predict_vertex(int i, const float4* X, const flo
     else                               s = make_float4(0.f, 0.f, 0.f, au.w);
     A[i] = s;
     B[i] = s;
+}
+
+__device__ __forceinline__ void predict_vertex(int i, const float4* X, const float4* V, const float4* aux,
+                                               const float* mass, const int* vcloth, const ClothInfo* cinfo,
+                                               const float4* warm, float4* Y, float4* A, float4* B)
+{
+    predict_vertex_xv(i, __ldcg(&X[i]), __ldcg(&V[i]), aux, mass, vcloth, cinfo, warm, Y, A, B);
 }
 
 // Cloths still active after the last sweep keep x^max_iter.  A non-finite

@@ -46,6 +46,31 @@ __device__ __forceinline__ bool grid_barrier_r(unsigned* bar, int* err, long lon
     return ok != 0;
 }
 
+// Predicts caller vertex o (layout vertex g) from the caller's x and v, which
+// replace the solver's state as the scatter copy before a frame would have.
+__device__ __forceinline__ void predict_caller_vertex(const PersistArgs& p, int o, int g)
+{
+    const float4 x = p.in_x ? make_float4(p.in_x[3 * o], p.in_x[3 * o + 1], p.in_x[3 * o + 2], 0.f) : __ldcg(&p.X[g]);
+    const float4 v = p.in_v ? make_float4(p.in_v[3 * o], p.in_v[3 * o + 1], p.in_v[3 * o + 2], 0.f) : __ldcg(&p.V[g]);
+    if (p.in_x) p.Xw[g] = x;
+    if (p.in_v) p.V[g] = v;
+    predict_vertex_xv(g, x, v, p.aux, p.mass, p.vcloth, p.it.cinfo, p.warm, p.Y, p.it.buf[0], p.it.buf[1]);
+}
+
+// Layout vertex g's state into the caller's arrays at caller vertex o (the
+// gather copy after a frame).
+__device__ __forceinline__ void store_frame_state(const PersistArgs& p, int o, int g)
+{
+    if (p.out_x) {
+        const float4 x = __ldcg(&p.Xw[g]);
+        p.out_x[3 * o] = x.x; p.out_x[3 * o + 1] = x.y; p.out_x[3 * o + 2] = x.z;
+    }
+    if (p.out_v) {
+        const float4 v = __ldcg(&p.V[g]);
+        p.out_v[3 * o] = v.x; p.out_v[3 * o + 1] = v.y; p.out_v[3 * o + 2] = v.z;
+    }
+}
+
 __device__ __forceinline__ void st_release_gpu(unsigned long long* p, unsigned long long v)
 {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
@@ -161,7 +186,9 @@ __device__ __forceinline__ void compute_residual(float r2, float* red, double* a
 // `sig_ok` at bar 3 and every thread leaves.
 // With a tolerance every sweep ends in a grid barrier instead and the
 // signal warp only takes part in the block-wide barriers.
-template <int MODE, int NT>
+// IO: the instance that also moves the caller's state (p.in_x ... p.out_v);
+// the other one compiles without that code.
+template <int MODE, int NT, bool IO>
 __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistArgs p)
 {
     constexpr int NTT = NT + 32;   // a multiple of 128: 4 warps per SM sub-partition
@@ -207,19 +234,26 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     __syncthreads();
 
 
-    // predict the owned vertices; the cloth's first block resets its record
+    // predict the owned vertices, or with caller arrays the vertices in caller
+    // order (a grid-stride walk over the compute threads); the cloth's first
+    // block resets its record
     const int c = ph.cloth;
     const ClothInfo& ci = a.cinfo[c];
     const bool own = tid < nown;
     const bool first = (int)blockIdx.x == ci.patch_begin;
     const int g = ph.vbegin + tid;
+    const bool caller_in = IO && (p.in_x || p.in_v), caller_out = IO && (p.out_x || p.out_v);
     float4 dprev = make_float4(0.f, 0.f, 0.f, 0.f);
     if (first) reset_rt(a.crt, a.acc, a.acc_stride, c, tid, NTT);
-    if (own) {
+    if (caller_in) {
+        for (int o = (int)blockIdx.x * NT + tid; comp && o < p.n; o += (int)gridDim.x * NT)
+            predict_caller_vertex(p, o, __ldg(&p.io_inv[o]));
+    } else if (own) {
         predict_vertex(g, p.X, p.V, p.aux, p.mass, p.vcloth, a.cinfo, p.warm, p.Y, a.buf[0], a.buf[1]);
         dprev = __ldcg(&a.buf[0][g]);
     }
     if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+    if (caller_in && own) dprev = __ldcg(&a.buf[0][g]);
     for (int l = tid; l < nlocal; l += NTT) {
         const int gg = l < nown ? ph.vbegin + l : __ldg(&a.halo[ph.halo_off + l - nown]);
         sy[l] = __ldcg(&a.Y[gg]);
@@ -345,18 +379,30 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     if (nbr && !grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
     if (first && tid == 0) frame_stats_cloth(a, c);
     if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
-    if (own) finalize_vertex(g, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
+    if (caller_out) {
+        for (int o = (int)blockIdx.x * NT + tid; comp && o < p.n; o += (int)gridDim.x * NT) {
+            const int gv = __ldg(&p.io_inv[o]);
+            finalize_vertex(gv, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
+            store_frame_state(p, o, gv);
+        }
+    } else if (own) {
+        finalize_vertex(g, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
+    }
 }
 
 // NT compute threads plus the signal warp: 480 + 32 threads, one block (one
-// patch) per SM; 224 + 32, two half-size patches per SM.
-struct ResVariant { int nt; void* f[2]; };
+// patch) per SM; 224 + 32, two half-size patches per SM.  Instances: the
+// consistent solve, the reference-literal solve, and the consistent solve
+// that moves the caller's state.
+struct ResVariant { int nt; void* f[3]; };
 
 static const ResVariant* res_variants(int* n)
 {
     static const ResVariant v[] = {
-        {480, {(void*)k_resident<kModeConsistent, 480>, (void*)k_resident<kModeLiteral, 480>}},
-        {224, {(void*)k_resident<kModeConsistent, 224>, (void*)k_resident<kModeLiteral, 224>}},
+        {480, {(void*)k_resident<kModeConsistent, 480, false>, (void*)k_resident<kModeLiteral, 480, false>,
+               (void*)k_resident<kModeConsistent, 480, true>}},
+        {224, {(void*)k_resident<kModeConsistent, 224, false>, (void*)k_resident<kModeLiteral, 224, false>,
+               (void*)k_resident<kModeConsistent, 224, true>}},
     };
     *n = 2;
     return v;
@@ -371,21 +417,26 @@ int resident_pick(int nt)
     return -1;
 }
 
-static void* variant_fn(int variant, int mode)
+static void* variant_fn(int variant, int mode, bool io)
 {
     int n = 0;
     const ResVariant* v = res_variants(&n);
     if (variant < 0 || variant >= n) return nullptr;
+    if (io) return mode == kModeConsistent ? v[variant].f[2] : nullptr;
     return v[variant].f[mode == kModeConsistent ? 0 : 1];
 }
 
+bool resident_moves_state(int mode) { return mode == kModeConsistent; }
+
 int resident_max_blocks(int mode, int variant, size_t smem)
 {
-    void* f = variant_fn(variant, mode);
+    void* f = variant_fn(variant, mode, false);
     if (!f) return 0;
     int n = 0;
     const int nt = res_variants(&n)[variant].nt;
-    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess) return 0;
+    for (void* fi : {f, variant_fn(variant, mode, true)})
+        if (fi && cudaFuncSetAttribute(fi, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess)
+            return 0;
     int dev = 0, nsm = 0, nb = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
@@ -395,7 +446,8 @@ int resident_max_blocks(int mode, int variant, size_t smem)
 
 cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t smem, cudaStream_t s)
 {
-    void* f = variant_fn(variant, p.mode);
+    const bool io = p.in_x || p.in_v || p.out_x || p.out_v;
+    void* f = variant_fn(variant, p.mode, io);
     if (!f || grid <= 0) return cudaErrorInvalidValue;
     int n = 0;
     const int nt = res_variants(&n)[variant].nt;

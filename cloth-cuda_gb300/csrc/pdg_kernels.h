@@ -56,6 +56,17 @@ struct PersistArgs {
     unsigned long long* pflag;   // per patch: last (frame, sweep) mark completed
     unsigned long long frame_seq;  // increments every frame
     int nbr_sync;        // 1: sweeps wait for neighbour patches only
+    // caller state moved inside the frame launch (resident kernel only): x, v
+    // read by the prediction and written by the finalisation, AoS xyz in
+    // caller order; any may be null.  Device or page-locked mapped host
+    // memory.  With caller arrays the prediction and the finalisation walk
+    // the vertices in caller order (io_inv: caller vertex -> layout vertex),
+    // so that host memory is read and written contiguously.
+    const float* in_x;
+    const float* in_v;
+    float* out_x;
+    float* out_v;
+    const int* io_inv;
 };
 cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t smem, cudaStream_t s);
 int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
@@ -65,6 +76,9 @@ int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
 // signal warp.  Limit: nown <= nt.  Kernel variant for nt threads (-1: none).
 int resident_pick(int nt);
 int resident_max_blocks(int mode, int variant, size_t smem);
+// Whether the kernel has an instance that moves the caller's state (PersistArgs
+// in_x ... out_v) for this mode.
+bool resident_moves_state(int mode);
 cudaError_t launch_resident(const PersistArgs& p, int variant, int grid, size_t smem, cudaStream_t s);
 
 // Streaming per-sweep kernel (pd_stream.cu): persistent grid, the vertex

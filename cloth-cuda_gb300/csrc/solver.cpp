@@ -120,6 +120,9 @@ PersistArgs persist_args(pdg_solver* s)
     p.nbr_ptr = s->nbr_ptr.p; p.nbr = s->nbr.p; p.pflag = s->pflag.p;
     p.frame_seq = ++s->frame_seq;
     p.nbr_sync = s->nbr_sync;
+    p.in_x = p.in_v = nullptr;
+    p.out_x = p.out_v = nullptr;
+    p.io_inv = s->inv_global.p;
     return p;
 }
 
@@ -358,16 +361,27 @@ static int take_wait_error(pdg_solver* s)
                      e == 1 ? "grid barrier" : e == 2 ? "resident grid barrier" : "neighbour mark");
 }
 
-int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
+// Caller state moved by the resident frame launch itself: inputs read by the
+// first frame, outputs written by the last (device or mapped host pointers).
+struct FrameIO {
+    const float* in_x;
+    const float* in_v;
+    float* out_x;
+    float* out_v;
+};
+
+// `nframes` frames, stream-ordered; `io` only with the resident kernel.
+static int enqueue_frames(pdg_solver* s, int nframes, const FrameIO* io)
 {
-    if (!s || nframes < 0) return set_error(PDG_ERR_ARG, "pdg_solver_step: bad arguments");
     for (int f = 0; f < nframes; ++f) {
         if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
             // barrier counter and generation start clean every frame; the
             // error word stays set until it is reported, and a kernel that
             // finds it set leaves at its first barrier
             CK(cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), s->stream));
-            const PersistArgs p = persist_args(s);
+            PersistArgs p = persist_args(s);
+            if (io && f == 0) { p.in_x = io->in_x; p.in_v = io->in_v; }
+            if (io && f == nframes - 1) { p.out_x = io->out_x; p.out_v = io->out_v; }
             if (s->kernel == PDG_KERNEL_PERSISTENT)
                 CK(launch_persistent(p, s->nt, s->persist_grid, s->L.smem_bytes, s->stream));
             else
@@ -382,6 +396,14 @@ int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
             s->launches += s->kernels_per_frame + ((s->ws && s->any_warm) ? warm_kernel_count() + 4 : 0);
         }
     }
+    return PDG_OK;
+}
+
+int pdg_solver_step(pdg_solver* s, int nframes, pdg_frame_stats* stats)
+{
+    if (!s || nframes < 0) return set_error(PDG_ERR_ARG, "pdg_solver_step: bad arguments");
+    const int rc = enqueue_frames(s, nframes, nullptr);
+    if (rc) return rc;
     if (stats) {
         CK(cudaMemcpyAsync(s->h_rt.data(), s->crt.p, sizeof(ClothRT) * s->L.ncloth, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
@@ -506,11 +528,40 @@ int pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const fl
                          float* v_out, pdg_frame_stats* stats)
 {
     if (!s || nframes < 0) return set_error(PDG_ERR_ARG, "pdg_solver_step_host: bad arguments");
-    // Page-locked caller buffers are read and written in place by the copy
-    // kernels (in caller order, so host memory is walked contiguously);
-    // pageable ones go through the device staging buffers.
+    // Page-locked caller buffers are read and written in place; pageable ones
+    // go through the device staging buffers.
     const int n = s->L.ntot;
     const size_t bytes = sizeof(float) * 3 * (size_t)n;
+    if (s->kernel == PDG_KERNEL_RESIDENT && nframes > 0 && resident_moves_state(s->mode)) {
+        // The frame launch itself reads the inputs before its prediction and
+        // writes the outputs after its last sweep: no copy launches around it.
+        FrameIO io{static_cast<const float*>(mapped_host(x_in)), static_cast<const float*>(mapped_host(v_in)),
+                   static_cast<float*>(mapped_host(x_out)), static_cast<float*>(mapped_host(v_out))};
+        if (x_in && !io.in_x) {
+            CK(cudaMemcpyAsync(s->stage_x.p, x_in, bytes, cudaMemcpyHostToDevice, s->stream));
+            io.in_x = s->stage_x.p;
+        }
+        if (v_in && !io.in_v) {
+            CK(cudaMemcpyAsync(s->stage_v.p, v_in, bytes, cudaMemcpyHostToDevice, s->stream));
+            io.in_v = s->stage_v.p;
+        }
+        // a staged output lands in the staging buffer after the input has
+        // been read from it (the input is read by the first frame, before
+        // its first grid barrier; the output is written by the last)
+        if (x_out && !io.out_x) io.out_x = s->stage_x.p;
+        if (v_out && !io.out_v) io.out_v = s->stage_v.p;
+        const int rc = enqueue_frames(s, nframes, &io);
+        if (rc) return rc;
+        if (x_out && io.out_x == s->stage_x.p)
+            CK(cudaMemcpyAsync(x_out, io.out_x, bytes, cudaMemcpyDeviceToHost, s->stream));
+        if (v_out && io.out_v == s->stage_v.p)
+            CK(cudaMemcpyAsync(v_out, io.out_v, bytes, cudaMemcpyDeviceToHost, s->stream));
+        if (stats) return pdg_solver_step(s, 0, stats);
+        CK(cudaStreamSynchronize(s->stream));
+        return PDG_OK;
+    }
+    // Other plans: copy kernels in caller order (host memory is walked
+    // contiguously) around the frames.
     if (x_in || v_in) {
         const float* dx = static_cast<const float*>(mapped_host(x_in));
         const float* dv = static_cast<const float*>(mapped_host(v_in));

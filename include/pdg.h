@@ -207,7 +207,10 @@ int  pdg_solver_get_state_all(pdg_solver* s, float* x, float* v, int on_device);
  * same as set_state_all + step + get_state_all, without their separate
  * synchronisations.  Replaces the step + cudaMemcpy of mesh.d_pos / d_vel
  * in the reference's frame loop (src/tools/sim_cloth.cpp:237-251 with
- * lines 44-45 and 82-83).  stats as for pdg_solver_step. */
+ * lines 44-45 and 82-83).  stats as for pdg_solver_step.  With the
+ * resident kernel the frame launch itself reads the inputs and writes the
+ * outputs (page-locked buffers in place); a wait that runs out leaves the
+ * outputs undefined, like the solver state. */
 int  pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const float* v_in,
                           float* x_out, float* v_out, pdg_frame_stats* stats);
 /* Move the pins of one cloth (Constraints::target_positions). */

@@ -261,6 +261,47 @@ def test_step_host_equals_set_step_get(pdg, oracle, kernel):
     assert np.array_equal(xa, qx)
 
 
+@pytest.mark.parametrize("kernel", [1, 3])
+def test_step_host_several_frames_mixed_buffers(pdg, oracle, kernel):
+    # Inputs are taken by the first frame of a call and outputs written by the
+    # last (the resident kernel does both inside its frame launch); pageable
+    # and page-locked buffers mix freely; an absent input keeps the state.
+    torch = pytest.importorskip("torch")
+    ms, cs, cfgs = [], [], []
+    for i, n in enumerate((9, 17)):
+        m, c, cfg, sc, a = scene(pdg, oracle, n=n, seed=i + 5, kernel=kernel)
+        ms.append(m); cs.append(c); cfgs.append(cfg)
+    s1 = pdg.Solver(cfgs, ms, cs)
+    s2 = pdg.Solver(cfgs, ms, cs)
+    n = int(s1.offsets[-1])
+    rng = np.random.default_rng(11)
+    rest = np.concatenate([np.asarray(m.arrays()["rest"]).reshape(-1, 3) for m in ms])
+    x = (rest + rng.normal(0, 1e-3, (n, 3))).astype(np.float32)
+    v = rng.normal(0, 1e-2, (n, 3)).astype(np.float32)
+    pinned = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    # three frames in one call: pinned x in, pageable v in, pageable x out, pinned v out
+    s1.set_state_all(x, v); s1.step(3, stats=False); xa, va = s1.get_state_all()
+    px, qv = pinned(x), pinned(np.zeros_like(v))
+    xo = np.full_like(x, np.nan)
+    st = s2.step_host(px, v.copy(), xo, qv, nframes=3, stats=True)
+    assert np.array_equal(xa, xo) and np.array_equal(va, qv)
+    assert all(t["status"] == 0 for t in st)
+    assert np.array_equal(px, x)   # an input that is not also an output stays as it was
+    # x alone in (v stays the solver's own), both out into one pageable pair
+    x2 = (xa + rng.normal(0, 1e-3, (n, 3))).astype(np.float32)
+    s1.set_state_all(x2, None); s1.step(1, stats=False); xb, vb = s1.get_state_all()
+    xo2, vo2 = np.empty_like(x), np.empty_like(v)
+    s2.step_host(x2, None, xo2, vo2)
+    assert np.array_equal(xb, xo2) and np.array_equal(vb, vo2)
+    # v alone in from pinned memory, two frames, x alone out in place of the input buffer
+    v3 = pinned(rng.normal(0, 1e-2, (n, 3)).astype(np.float32))
+    s1.set_state_all(None, v3); s1.step(2, stats=False); xc, vc = s1.get_state_all()
+    s2.step_host(None, v3, None, None, nframes=2)
+    xo3 = pinned(np.zeros_like(x))
+    s2.step_host(None, None, xo3, v3, nframes=0)   # no frame: the copies alone
+    assert np.array_equal(xc, xo3) and np.array_equal(vc, v3)
+
+
 def test_apply_pins_device(pdg):
     torch = pytest.importorskip("torch")
     pos = torch.arange(30, dtype=torch.float32, device="cuda")
