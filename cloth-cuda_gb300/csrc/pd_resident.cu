@@ -46,12 +46,19 @@ __device__ __forceinline__ bool grid_barrier_r(unsigned* bar, int* err, long lon
     return ok != 0;
 }
 
-// Predicts caller vertex o (layout vertex g) from the caller's x and v, which
-// replace the solver's state as the scatter copy before a frame would have.
-__device__ __forceinline__ void predict_caller_vertex(const PersistArgs& p, int o, int g)
+// Caller vertex o of an AoS xyz array, or zeros without one.
+__device__ __forceinline__ float3 caller_vec(const float* a, int o)
 {
-    const float4 x = p.in_x ? make_float4(p.in_x[3 * o], p.in_x[3 * o + 1], p.in_x[3 * o + 2], 0.f) : __ldcg(&p.X[g]);
-    const float4 v = p.in_v ? make_float4(p.in_v[3 * o], p.in_v[3 * o + 1], p.in_v[3 * o + 2], 0.f) : __ldcg(&p.V[g]);
+    return a ? make_float3(a[3 * o], a[3 * o + 1], a[3 * o + 2]) : make_float3(0.f, 0.f, 0.f);
+}
+
+// Predicts layout vertex g from the caller's x and v (xi, vi: its entries in
+// the caller's arrays), which replace the solver's state as the scatter copy
+// before a frame would have.
+__device__ __forceinline__ void predict_caller_vertex(const PersistArgs& p, int g, float3 xi, float3 vi)
+{
+    const float4 x = p.in_x ? make_float4(xi.x, xi.y, xi.z, 0.f) : __ldcg(&p.X[g]);
+    const float4 v = p.in_v ? make_float4(vi.x, vi.y, vi.z, 0.f) : __ldcg(&p.V[g]);
     if (p.in_x) p.Xw[g] = x;
     if (p.in_v) p.V[g] = v;
     predict_vertex_xv(g, x, v, p.aux, p.mass, p.vcloth, p.it.cinfo, p.warm, p.Y, p.it.buf[0], p.it.buf[1]);
@@ -201,6 +208,17 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     const IterArgs& a = p.it;
     const int tid = threadIdx.x;
     const bool comp = tid < NT;
+    // With caller arrays, this thread's first caller vertex is loaded before
+    // the patch's records are staged: the host round trip overlaps the staging.
+    const bool caller_in = IO && (p.in_x || p.in_v), caller_out = IO && (p.out_x || p.out_v);
+    const int o0 = (int)blockIdx.x * NT + tid;
+    float3 xi0 = make_float3(0.f, 0.f, 0.f), vi0 = xi0;
+    int gi0 = 0;
+    if (caller_in && comp && o0 < p.n) {
+        gi0 = __ldg(&p.io_inv[o0]);
+        xi0 = caller_vec(p.in_x, o0);
+        vi0 = caller_vec(p.in_v, o0);
+    }
     if (tid == 0) ph = a.patches[blockIdx.x];
     __syncthreads();
     const int nown = ph.nown, nlocal = ph.nlocal, ncell = ph.ncell, nhin = ph.nhinge;
@@ -242,12 +260,12 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     const bool own = tid < nown;
     const bool first = (int)blockIdx.x == ci.patch_begin;
     const int g = ph.vbegin + tid;
-    const bool caller_in = IO && (p.in_x || p.in_v), caller_out = IO && (p.out_x || p.out_v);
     float4 dprev = make_float4(0.f, 0.f, 0.f, 0.f);
     if (first) reset_rt(a.crt, a.acc, a.acc_stride, c, tid, NTT);
     if (caller_in) {
-        for (int o = (int)blockIdx.x * NT + tid; comp && o < p.n; o += (int)gridDim.x * NT)
-            predict_caller_vertex(p, o, __ldg(&p.io_inv[o]));
+        if (comp && o0 < p.n) predict_caller_vertex(p, gi0, xi0, vi0);
+        for (int o = o0 + (int)gridDim.x * NT; comp && o < p.n; o += (int)gridDim.x * NT)
+            predict_caller_vertex(p, __ldg(&p.io_inv[o]), caller_vec(p.in_x, o), caller_vec(p.in_v, o));
     } else if (own) {
         predict_vertex(g, p.X, p.V, p.aux, p.mass, p.vcloth, a.cinfo, p.warm, p.Y, a.buf[0], a.buf[1]);
         dprev = __ldcg(&a.buf[0][g]);
@@ -380,7 +398,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     if (first && tid == 0) frame_stats_cloth(a, c);
     if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
     if (caller_out) {
-        for (int o = (int)blockIdx.x * NT + tid; comp && o < p.n; o += (int)gridDim.x * NT) {
+        for (int o = o0; comp && o < p.n; o += (int)gridDim.x * NT) {
             const int gv = __ldg(&p.io_inv[o]);
             finalize_vertex(gv, p.Xw, p.V, p.Y, a.buf[0], a.buf[1], p.aux, p.vcloth, a.cinfo, a.crt);
             store_frame_state(p, o, gv);
