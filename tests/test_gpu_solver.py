@@ -300,6 +300,14 @@ def test_step_host_several_frames_mixed_buffers(pdg, oracle, kernel):
     xo3 = pinned(np.zeros_like(x))
     s2.step_host(None, None, xo3, v3, nframes=0)   # no frame: the copies alone
     assert np.array_equal(xc, xo3) and np.array_equal(vc, v3)
+    # page-locked arrays that start 4 bytes past a 16-byte boundary (an
+    # interior pointer of a page-locked allocation), in place
+    buf = pinned(np.zeros(3 * n + 1, np.float32))
+    ux = buf[1:].reshape(n, 3)
+    ux[:] = xc
+    s1.step(1, stats=False); xd, vd = s1.get_state_all()
+    s2.step_host(ux, None, ux, None)
+    assert np.array_equal(xd, ux) and buf[0] == 0
 
 
 def test_apply_pins_device(pdg):
