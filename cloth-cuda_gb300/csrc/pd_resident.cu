@@ -14,6 +14,12 @@
 //
 // Used when every patch fits one block (nown <= NT) and all patches are
 // co-resident.
+//
+// The instance with IO = true also moves the caller's state for the
+// host-buffer frame (pdg_solver_step_host): it reads x and v from the caller's
+// arrays for the prediction and writes them back after the finalisation, both
+// walked in caller order so that page-locked host memory is accessed
+// contiguously, which replaces the two copy launches around the frame.
 #include "pd_kernels.cuh"
 #include "pdg_kernels.h"
 
