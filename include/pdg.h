@@ -87,7 +87,7 @@ typedef struct pdg_config {
     int   compute_final_residual; /* evaluate r(x) of the returned iterate (1) */
     int   smem_carveout;      /* per-sweep kernels: percent of the unified
                                  L1/shared capacity given to shared memory
-                                 (1-100); 0 = the driver's choice (0)      */
+                                 (1-100); 0 = the CUDA runtime's choice (0) */
 } pdg_config;
 
 /* Per-frame statistics (one per cloth). */

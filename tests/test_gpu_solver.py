@@ -1,9 +1,9 @@
 """CUDA solver against the oracle, through the C ABI (GPU).
 
 Tolerances: float32 arithmetic on both sides with different summation
-order; one frame of 10 sweeps agrees to 1e-5 relative in positions (the
-spec bar), and every multi-frame comparison against the float64 oracle
-to 1e-4 relative.
+order; one frame of 10 sweeps agrees to 1e-5 relative in positions, and
+every multi-frame comparison against the float64 oracle to 1e-4 relative (the
+accuracy bar for positions).
 """
 import numpy as np
 import pytest

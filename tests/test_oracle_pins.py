@@ -172,7 +172,8 @@ def test_free_fall_known_answer(oracle):
 
 def test_rest_state_static_consistent(oracle):
     # rest shape, g = 0: the consistent step keeps the cloth still
-    # (the reference's literal step does not)
+    # (the reference's literal x = rhs/diag step, src/pd_solver.cu:371-398,
+    # does not)
     pos, tris = _grid(oracle, 10, 10, 0.1, 0)
     sc = oracle.Scene(pos, tris, k_stretch=1e3, k_bend=1.0, gravity=0.0, h=0.01, pins=[0, 9])
     x = pos.astype(np.float64).reshape(-1); v = np.zeros_like(x)
@@ -207,8 +208,9 @@ def test_direct_and_jacobi_same_fixed_point(oracle):
 
 
 def test_reference_pin_elimination_is_inconsistent(oracle):
-    # zeroing pinned rows/columns without moving K_fp x_p to the
-    # right-hand side drags the free vertices toward the origin
+    # The reference's CPU pin elimination zeroes pinned rows/columns without
+    # moving K_fp x_p to the right-hand side, which drags the free vertices
+    # toward the origin
     pos, tris = _grid(oracle, 10, 10, 0.1, 0)
     sc = oracle.Scene(pos, tris, k_stretch=1e3, k_bend=0.0, gravity=0.0, h=0.01, pins=[0, 9])
     x = pos.astype(np.float64).reshape(-1); v = np.zeros_like(x)
