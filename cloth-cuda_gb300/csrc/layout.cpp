@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 
 namespace pdg {
@@ -661,6 +662,165 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
     // per-patch sweep kernels: y, d per local vertex and the vertex-major slots
     L.smem_bytes = (L.max_vm_slot + 15) / 16 * 16;
     return true;
+}
+
+// The properties of a layout that the sweep kernels rely on, checked on the
+// host.  Returns an empty string, or the first violation found.
+std::string check_layout(const std::vector<ClothSetup>& cl, const HostLayout& L)
+{
+    char msg[256];
+    auto fail = [&](const char* fmt, auto... v) {
+        std::snprintf(msg, sizeof msg, fmt, v...);
+        return std::string(msg);
+    };
+    const int ntot = L.ntot;
+    // 1. the reorder: a permutation within each cloth
+    if ((int)L.perm_global.size() != ntot || (int)L.perm_local.size() != ntot || (int)L.vcloth.size() != ntot)
+        return "reorder arrays do not hold every vertex";
+    {
+        std::vector<char> seen(ntot, 0);
+        for (int ci = 0; ci < L.ncloth; ++ci) {
+            const ClothInfo& info = L.cinfo[ci];
+            if (info.nverts != cl[ci].mesh->N) return fail("cloth %d: %d vertices in the layout, %d in the mesh", ci,
+                                                          info.nverts, cl[ci].mesh->N);
+            for (int g = info.vbegin; g < info.vbegin + info.nverts; ++g) {
+                const int o = L.perm_local[g];
+                if (L.vcloth[g] != ci || o < 0 || o >= info.nverts || L.perm_global[g] != info.vbegin + o)
+                    return fail("vertex %d: cloth or caller index out of place (cloth %d, index %d)", g, ci, o);
+                if (seen[L.perm_global[g]]++) return fail("caller vertex %d appears twice (cloth %d)",
+                                                          L.perm_global[g], ci);
+            }
+        }
+    }
+    // 2. the patches: consecutive runs of owned vertices, each inside its cloth
+    std::vector<int> vpatch(ntot, -1);
+    {
+        int next = 0;
+        for (int p = 0; p < L.npatch; ++p) {
+            const PatchHdr& h = L.patches[p];
+            const ClothInfo& info = L.cinfo[h.cloth];
+            if (h.vbegin != next || h.nown < 1) return fail("patch %d: owns %d vertices from %d", p, h.nown, h.vbegin);
+            if (p < info.patch_begin || p >= info.patch_end || h.vbegin < info.vbegin ||
+                h.vbegin + h.nown > info.vbegin + info.nverts)
+                return fail("patch %d: not inside cloth %d", p, h.cloth);
+            for (int l = 0; l < h.nown; ++l) vpatch[h.vbegin + l] = p;
+            next += h.nown;
+        }
+        if (next != ntot) return fail("patches own %d of %d vertices", next, ntot);
+    }
+    // vertices that some patch reads as a halo vertex
+    std::vector<char> in_halo(ntot, 0);
+    for (const PatchHdr& h : L.patches)
+        for (int q = 0; q < h.nlocal - h.nown; ++q) in_halo[L.halo[h.halo_off + q]] = 1;
+
+    std::vector<int> stamp(ntot, -1), nslot_of;
+    std::vector<char> slot_seen;
+    for (int p = 0; p < L.npatch; ++p) {
+        const PatchHdr& h = L.patches[p];
+        const ClothSetup& c = cl[h.cloth];
+        const MeshData& m = *c.mesh;
+        const Topology& tp = *c.topo;
+        // 3. the halo: distinct vertices of the same cloth that the patch does
+        //    not own, each owner on the patch's neighbour list
+        for (int q = 0; q < h.nlocal - h.nown; ++q) {
+            const int g = L.halo[h.halo_off + q];
+            if (g < 0 || g >= ntot || L.vcloth[g] != h.cloth || vpatch[g] == p || stamp[g] == p)
+                return fail("patch %d: halo entry %d (vertex %d) is foreign, owned or repeated", p, q, g);
+            stamp[g] = p;
+            const int* nb = L.nbr.data() + L.nbr_ptr[p];
+            const int nnb = L.nbr_ptr[p + 1] - L.nbr_ptr[p];
+            if (!std::binary_search(nb, nb + nnb, vpatch[g]))
+                return fail("patch %d: owner %d of halo vertex %d is not a neighbour", p, vpatch[g], g);
+        }
+        // 4. boundary vertices first: every owned vertex another patch reads
+        //    is published with the first nbnd
+        for (int l = h.nbnd; l < h.nown; ++l)
+            if (in_halo[h.vbegin + l]) return fail("patch %d: owned vertex %d is read by another patch but not among "
+                                                   "the first %d", p, l, h.nbnd);
+        // 5. the records: local indices in range, and every owned vertex's
+        //    contributions j < deg written to slot j*npad + l exactly once,
+        //    by phase-A records (the prefix) if the vertex is a boundary one
+        const int npad = h.vm_npad;
+        if (npad < h.nown) return fail("patch %d: slot stride %d below %d owned vertices", p, npad, h.nown);
+        const int* ptr = L.csr_ptr.data() + h.csr_off;
+        int maxdeg = 0;
+        for (int l = 0; l < h.nown; ++l) maxdeg = std::max(maxdeg, ptr[l + 1] - ptr[l]);
+        if ((long)maxdeg * npad > h.vm_nslot) return fail("patch %d: %d slots, %d needed", p, h.vm_nslot, maxdeg * npad);
+        slot_seen.assign(h.vm_nslot, 0);
+        nslot_of.assign(h.nown, 0);
+        auto slot = [&](uint32_t s, uint32_t l, bool phase_a) -> std::string {
+            if (s == 0xffffu) return "";
+            if ((int)l >= h.nown || (int)(s % npad) != (int)l || (int)(s / npad) >= ptr[l + 1] - ptr[l] ||
+                (int)s >= h.vm_nslot)
+                return fail("patch %d: slot %d does not belong to local vertex %d", p, (int)s, (int)l);
+            if (slot_seen[s]++) return fail("patch %d: slot %d written twice (vertex %d)", p, (int)s, (int)l);
+            if ((int)l < h.nbnd && !phase_a)
+                return fail("patch %d: boundary vertex %d gets a contribution after phase A (slot %d)", p, (int)l,
+                            (int)s);
+            ++nslot_of[l];
+            return "";
+        };
+        // triangles held by the patch's cells, as mesh triangle ids
+        std::vector<int> held;
+        auto caller = [&](uint32_t l) {
+            const int g = (int)l < h.nown ? h.vbegin + (int)l : L.halo[h.halo_off + (int)l - h.nown];
+            return L.perm_local[g];
+        };
+        auto find_tri = [&](int a, int b, int d) {
+            for (int q = tp.vt_ptr[a]; q < tp.vt_ptr[a + 1]; ++q) {
+                const int t = tp.vt[q];
+                const int* v = &m.tris[3 * t];
+                const bool hb = v[0] == b || v[1] == b || v[2] == b, hd = v[0] == d || v[1] == d || v[2] == d;
+                if (hb && hd) return t;
+            }
+            return -1;
+        };
+        for (int q = 0; q < h.ncell; ++q) {
+            const CellRec& r = L.cells[h.cell_off + q];
+            const uint32_t cv[6] = {r.c01 & 0xffffu, r.c01 >> 16, r.c23 & 0xffffu, r.c23 >> 16, r.x12 & 0xffffu,
+                                    r.x12 >> 16};
+            const uint32_t sv[6] = {r.vm01 & 0xffffu, r.vm01 >> 16, r.vm23 & 0xffffu, r.vm23 >> 16, r.vm45 & 0xffffu,
+                                    r.vm45 >> 16};
+            for (int k = 0; k < 6; ++k) {
+                if ((int)cv[k] >= h.nlocal) return fail("patch %d: cell %d names local vertex %d", p, q, (int)cv[k]);
+                const std::string e = slot(sv[k], cv[k], q < h.ncell_a);
+                if (!e.empty()) return e;
+            }
+            const int t0 = find_tri(caller(cv[0]), caller(cv[1]), caller(cv[2]));
+            if (t0 < 0) return fail("patch %d: cell %d's first triangle is not a mesh triangle", p, q);
+            held.push_back(t0);
+            if (cv[3] != cv[0]) {   // paired: the second triangle shares the edge c0-c1
+                const int t1 = find_tri(caller(cv[0]), caller(cv[1]), caller(cv[3]));
+                if (t1 < 0) return fail("patch %d: cell %d's second triangle is not a mesh triangle", p, q);
+                held.push_back(t1);
+            }
+        }
+        for (int q = 0; q < h.nhinge; ++q) {
+            const HingeRec& r = L.hinges[h.hinge_off + q];
+            const uint2 vm = L.hvm[h.hinge_off + q];
+            const uint32_t lv[4] = {r.l01 & 0xffffu, r.l01 >> 16, r.l23 & 0xffffu, r.l23 >> 16};
+            const uint32_t sv[4] = {vm.x & 0xffffu, vm.x >> 16, vm.y & 0xffffu, vm.y >> 16};
+            for (int a = 0; a < 4; ++a) {
+                if ((int)lv[a] >= h.nlocal) return fail("patch %d: hinge %d names local vertex %d", p, q, (int)lv[a]);
+                const std::string e = slot(sv[a], lv[a], q < h.nhin_a);
+                if (!e.empty()) return e;
+            }
+        }
+        for (int l = 0; l < h.nown; ++l)
+            if (nslot_of[l] != ptr[l + 1] - ptr[l])
+                return fail("patch %d: vertex %d has %d contributions written", p, l, nslot_of[l]);
+        // 6. every triangle through an owned vertex is held once by the patch
+        std::sort(held.begin(), held.end());
+        if (std::adjacent_find(held.begin(), held.end()) != held.end())
+            return fail("patch %d: a triangle is held twice", p);
+        for (int l = 0; l < h.nown; ++l) {
+            const int o = L.perm_local[h.vbegin + l];
+            for (int q = tp.vt_ptr[o]; q < tp.vt_ptr[o + 1]; ++q)
+                if (!std::binary_search(held.begin(), held.end(), tp.vt[q]))
+                    return fail("patch %d: triangle %d through owned vertex %d is missing", p, tp.vt[q], l);
+        }
+    }
+    return "";
 }
 
 }  // namespace pdg

@@ -46,6 +46,10 @@ struct HostLayout {
 };
 
 bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout& L, std::string& err);
+// The properties the sweep kernels rely on (partition, halo, neighbour lists,
+// boundary-first order, each contribution slot written once, every incident
+// triangle held): empty if they hold, else the first violation.
+std::string check_layout(const std::vector<ClothSetup>& cl, const HostLayout& L);
 
 // Owning device allocation.
 template <class T>

@@ -171,11 +171,11 @@ int build_graph(pdg_solver* s)
 
 }  // namespace
 
-int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
-                       void* stream, pdg_solver** out)
+// The cloths of a solver, checked: each mesh with its own constraints, valid
+// configurations, one mode.
+static int collect_cloths(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes,
+                          const pdg_constraints* const* cons, std::vector<ClothSetup>& out)
 {
-    if (!out || n <= 0 || !cfgs || !meshes || !cons) return set_error(PDG_ERR_ARG, "solver create: bad arguments");
-    std::unique_ptr<pdg_solver> s(new pdg_solver);
     for (int i = 0; i < n; ++i) {
         if (!meshes[i] || !cons[i]) return set_error(PDG_ERR_ARG, "cloth %d: null mesh or constraints", i);
         if (cons[i]->mesh != meshes[i]->data)
@@ -189,7 +189,19 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
         c.cons = cons[i]->c;
         if (c.cons.k_stretch.empty()) c.cons.k_stretch.assign(c.mesh->T, 0.f);  // no stretch data: no stretch term
         c.cfg = cfgs[i];
-        s->cloths.push_back(std::move(c));
+        out.push_back(std::move(c));
+    }
+    return PDG_OK;
+}
+
+int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                       void* stream, pdg_solver** out)
+{
+    if (!out || n <= 0 || !cfgs || !meshes || !cons) return set_error(PDG_ERR_ARG, "solver create: bad arguments");
+    std::unique_ptr<pdg_solver> s(new pdg_solver);
+    {
+        const int rc = collect_cloths(n, cfgs, meshes, cons, s->cloths);
+        if (rc) return rc;
     }
     const pdg_config& c0 = cfgs[0];
     s->mode = c0.mode;
@@ -326,6 +338,39 @@ int pdg_solver_create_batch(int n, const pdg_config* cfgs, const pdg_mesh* const
 {
     try {
         return pdg::create_solver(n, cfgs, meshes, cons, stream, out);
+    } catch (const std::bad_alloc&) {
+        return set_error(PDG_ERR_ALLOC, "host allocation failed");
+    }
+}
+
+int pdg_layout_check(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                     int patch_verts, pdg_layout_info* info)
+{
+    try {
+        if (n <= 0 || !cfgs || !meshes || !cons || !info) return set_error(PDG_ERR_ARG, "pdg_layout_check: bad arguments");
+        if (patch_verts < 16 || patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");
+        std::vector<ClothSetup> cl;
+        int rc = collect_cloths(n, cfgs, meshes, cons, cl);
+        if (rc) return rc;
+        HostLayout L;
+        std::string err;
+        if (!build_layout(cl, patch_verts, L, err)) return set_error(PDG_ERR_ARG, "%s", err.c_str());
+        *info = pdg_layout_info{};
+        info->vertices = L.ntot;
+        info->patches = L.npatch;
+        info->max_owned = L.max_nown;
+        info->max_local = L.max_nlocal;
+        for (const PatchHdr& h : L.patches) {
+            info->halo_total += h.nlocal - h.nown;
+            info->boundary_total += h.nbnd;
+            info->phase_a_cells += h.ncell_a;
+        }
+        info->cells = (long long)L.cells.size();
+        info->lone_hinges = (long long)L.hinges.size();
+        info->smem_resident = (long long)L.smem_resident;
+        err = check_layout(cl, L);
+        if (!err.empty()) return set_error(PDG_ERR_STATE, "layout check: %s", err.c_str());
+        return PDG_OK;
     } catch (const std::bad_alloc&) {
         return set_error(PDG_ERR_ALLOC, "host allocation failed");
     }

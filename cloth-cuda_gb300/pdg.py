@@ -76,6 +76,30 @@ def autotune_clear_cache():
     lib().pdg_autotune_clear_cache()
 
 
+class LayoutInfo(C.Structure):
+    _fields_ = [("vertices", C.c_int), ("patches", C.c_int), ("max_owned", C.c_int), ("max_local", C.c_int),
+                ("halo_total", C.c_longlong), ("boundary_total", C.c_longlong), ("cells", C.c_longlong),
+                ("phase_a_cells", C.c_longlong), ("lone_hinges", C.c_longlong), ("smem_resident", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def layout_check(cfg, meshes, cons, patch_verts):
+    """pdg_layout_check: build the patch layout of these cloths on the host
+    and check the properties the kernels rely on.  Returns the layout summary
+    as a dict; raises PDGError with the first violation.  No GPU needed."""
+    single = isinstance(meshes, Mesh)
+    meshes = [meshes] if single else list(meshes)
+    cons = [cons] if single else list(cons)
+    cfgs = [cfg] * len(meshes) if isinstance(cfg, Config) else list(cfg)
+    n = len(meshes)
+    info = LayoutInfo()
+    _check(lib().pdg_layout_check(n, (Config * n)(*cfgs), (C.c_void_p * n)(*[m.h.value for m in meshes]),
+                                  (C.c_void_p * n)(*[c.h.value for c in cons]), patch_verts, C.byref(info)))
+    return info.as_dict()
+
+
 _lib = None
 
 

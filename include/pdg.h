@@ -182,6 +182,28 @@ int  pdg_solver_create_batch(int ncloths, const pdg_config* cfgs,
                              const pdg_mesh* const* meshes,
                              const pdg_constraints* const* cons, void* stream,
                              pdg_solver** out);
+/* Host-side check of the patch layout a solver builds for these cloths with
+ * `patch_verts`-vertex patches; needs no GPU.  It checks the vertex reorder
+ * and partition, the halo and neighbour lists, that every owned vertex
+ * another patch reads comes first (boundary vertices), that every
+ * contribution slot of an owned vertex is written exactly once (for a
+ * boundary vertex, by the records before its sum), and that every triangle
+ * through an owned vertex is held by the patch.  PDG_OK with a summary in
+ * *info; PDG_ERR_STATE with the first violation in pdg_last_error_string();
+ * PDG_ERR_ARG for bad arguments.  No counterpart in the reference. */
+typedef struct pdg_layout_info {
+    int       vertices, patches, max_owned, max_local;
+    long long halo_total;      /* halo entries over all patches            */
+    long long boundary_total;  /* owned vertices that other patches read   */
+    long long cells;           /* cell records (triangle pairs)            */
+    long long phase_a_cells;   /* cell records through boundary vertices   */
+    long long lone_hinges;     /* bend hinges that no cell holds           */
+    long long smem_resident;   /* resident kernel: shared bytes per patch  */
+} pdg_layout_info;
+int  pdg_layout_check(int ncloths, const pdg_config* cfgs,
+                      const pdg_mesh* const* meshes,
+                      const pdg_constraints* const* cons, int patch_verts,
+                      pdg_layout_info* info);
 int  pdg_solver_num_cloths(const pdg_solver* s, int* n);
 int  pdg_solver_cloth_counts(const pdg_solver* s, int cloth, int* N, int* T);
 /* PDSolver::step (src/pd_solver.cu:496-621): `nframes` frames.  stats: NULL
