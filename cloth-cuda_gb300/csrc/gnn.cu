@@ -32,11 +32,14 @@ struct pdg_warmstart {
     int N = 0, E = 0;
     DevBuf<int> ptr, adj, rev;
     DevBuf<float> rest, deg_inv;
-    DevBuf<float4> ef, stat, Xn, Vn;
+    DevBuf<float4> ef, stat, Xn, Vn, Dn;
+    DevBuf<float> ew;     // per directed edge: weight of the energy-norm term of the loss
     DevBuf<bf16> xin, cat[L], pq[L], uo[L], hfin;
     DevBuf<float> out, target, freew, dout, dh, dtmp, dcat, dpq;
     DevBuf<double> loss;
     float smooth = 0.f;   // weight of the neighbour-difference term of the loss
+    int energy = 0;       // 1: that term weighted by the PD system's stiffness per edge
+    int judge = 4;        // sweeps each start runs before the judge compares them
     pdg_solver* solver = nullptr;
     ~pdg_warmstart()
     {
@@ -96,7 +99,7 @@ int alloc_graph(pdg_warmstart* w, int N, int E)
     w->N = N; w->E = E;
     GK(w->ptr.alloc(N + 1)); GK(w->adj.alloc(E)); GK(w->rev.alloc(E));
     GK(w->rest.alloc(E)); GK(w->deg_inv.alloc(N)); GK(w->ef.alloc(E)); GK(w->stat.alloc(N));
-    GK(w->Xn.alloc(N)); GK(w->Vn.alloc(N));
+    GK(w->Xn.alloc(N)); GK(w->Vn.alloc(N)); GK(w->Dn.alloc(N)); GK(w->ew.alloc(E));
     GK(w->xin.alloc((size_t)N * NFP));
     for (int l = 0; l < L; ++l) {
         GK(w->cat[l].alloc((size_t)N * 2 * H)); GK(w->pq[l].alloc((size_t)N * 2 * H)); GK(w->uo[l].alloc((size_t)N * H));
@@ -134,8 +137,9 @@ int forward(pdg_warmstart* w, cudaStream_t st)
 int wgrad_grid(int M) { return std::max(1, std::min(304, nb(M, 32))); }
 
 // gradients of the loss w.r.t. all parameters into w->g (zeroed here);
-// loss accumulated into w->loss
-int backward(pdg_warmstart* w, float inv_cnt, cudaStream_t st)
+// loss accumulated into w->loss; ew: per-edge weights of the smoothness term
+// (null: 1)
+int backward(pdg_warmstart* w, float inv_cnt, const float* ew, cudaStream_t st)
 {
     const int N = w->N, gb = nb(N, 64), gw = wgrad_grid(N);
     const Layout& y = w->lay;
@@ -143,7 +147,7 @@ int backward(pdg_warmstart* w, float inv_cnt, cudaStream_t st)
     float* g = w->g.p;
     GK(cudaMemsetAsync(g, 0, sizeof(float) * y.total, st));
     GK(cudaMemsetAsync(w->loss.p, 0, sizeof(double), st));
-    k_loss<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, w->target.p, w->freew.p, w->ptr.p, w->adj.p, w->smooth,
+    k_loss<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, w->target.p, w->freew.p, w->ptr.p, w->adj.p, ew, w->smooth,
                                        inv_cnt, w->dout.p, w->loss.p);
     k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dout.p, 16, NO, w->hfin.p, H, H, N, g + y.Wd, g + y.bd);
     k_gemm<float, 16, H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dout.p, 16, N, w->W.Wdt, nullptr, nullptr, 0, nullptr, 0,
@@ -223,11 +227,11 @@ int warm_infer_enqueue(pdg_warmstart* w, pdg_solver* s)
     cudaStream_t st = s->stream;
     const int N = w->N;
     k_node_feat<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->V.p, s->Y.p, s->aux.p, w->stat.p, s->vcloth.p, s->cinfo.p,
-                                            w->xin.p);
+                                            s->dprev.p, w->xin.p);
     k_edge_feat<<<nb(N, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rest.p, s->Y.p, w->ef.p);
     const int rc = forward(w, st);
     if (rc) return rc;
-    k_warm_out<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, s->A.p, s->warm.p);
+    k_warm_out<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, s->A.p, s->dprev.p, s->warm.p);
     GK(cudaGetLastError());
     return PDG_OK;
 }
@@ -238,6 +242,8 @@ void warm_detach(pdg_warmstart* w)
 {
     if (w) w->solver = nullptr;
 }
+
+int warm_judge_sweeps(const pdg_warmstart* w) { return w ? w->judge : 0; }
 
 }  // namespace pdg
 
@@ -308,7 +314,8 @@ int pdg_warmstart_set_params(pdg_warmstart* w, const float* host)
 }
 
 int pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr, const int* adj, const float* ef,
-                       const float* target, const float* freew, float* out, float* loss, float* grads)
+                       const float* target, const float* freew, const float* ew, float* out, float* loss,
+                       float* grads)
 {
     if (!w || N <= 0 || !x || !ptr || !target || !freew) return set_error(PDG_ERR_ARG, "pdg_warmstart_eval: bad arguments");
     if (w->solver) return set_error(PDG_ERR_STATE, "pdg_warmstart_eval: the network is attached to a solver");
@@ -325,11 +332,12 @@ int pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr, 
     if (E) GK(cudaMemcpyAsync(w->ef.p, ef, sizeof(float4) * E, cudaMemcpyHostToDevice, st));
     GK(cudaMemcpyAsync(w->target.p, target, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, st));
     GK(cudaMemcpyAsync(w->freew.p, freew, sizeof(float) * N, cudaMemcpyHostToDevice, st));
+    if (ew && E) GK(cudaMemcpyAsync(w->ew.p, ew, sizeof(float) * E, cudaMemcpyHostToDevice, st));
     double cnt = 0.0;
     for (int i = 0; i < N; ++i) cnt += freew[i] > 0.f ? 3.0 : 0.0;
     rc = forward(w, st);
     if (rc) return rc;
-    rc = backward(w, (float)(1.0 / std::max(cnt, 1.0)), st);
+    rc = backward(w, (float)(1.0 / std::max(cnt, 1.0)), (ew && E) ? w->ew.p : nullptr, st);
     if (rc) return rc;
     std::vector<float> o((size_t)N * 16);
     double l = 0.0;
@@ -398,13 +406,36 @@ int pdg_warmstart_attach(pdg_warmstart* w, pdg_solver* s)
         for (auto& q : nbr[i]) { adj.push_back(q.first); rest.push_back(q.second); }
         ptr[i + 1] = (int)adj.size();
     }
+    // Energy-norm weights of the loss's edge term: the PD system matrix
+    // M + K approximated by M plus a graph Laplacian whose diagonal is K's
+    // own (the Jacobi diagonal minus the mass), per unit mass: vertex i
+    // spreads sigma_i = (D_i - m_i) / m_i evenly over its deg_i edges, and
+    // an edge takes the mean of its two ends.  Pinned vertices contribute 0.
+    std::vector<float> sig(N, 0.f), ew(adj.size(), 0.f);
+    for (int i = 0; i < N; ++i) {
+        const float4 a = Lh.aux[i];
+        const float m = Lh.mass[i];
+        const int deg = ptr[i + 1] - ptr[i];
+        if (a.w > 0.f && m > 0.f && deg > 0) sig[i] = std::max(0.f, (1.f / (a.w * m) - 1.f) / (float)deg);
+    }
+    for (int i = 0; i < N; ++i)
+        for (int e = ptr[i]; e < ptr[i + 1]; ++e) ew[e] = 0.5f * (sig[i] + sig[adj[e]]);
     cudaStream_t st = s->stream;
     int rc = upload_graph(w, ptr, adj, st);
     if (rc) return rc;
     if (!rest.empty()) GK(cudaMemcpyAsync(w->rest.p, rest.data(), sizeof(float) * rest.size(), cudaMemcpyHostToDevice, st));
+    if (!ew.empty()) GK(cudaMemcpyAsync(w->ew.p, ew.data(), sizeof(float) * ew.size(), cudaMemcpyHostToDevice, st));
     GK(cudaMemcpyAsync(w->stat.p, stat.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, st));
     GK(s->warm.alloc(N));
     GK(cudaMemsetAsync(s->warm.p, 0, sizeof(float4) * N, st));
+    // the solver's learned-start state: previous offsets (none valid yet)
+    // and the learned chain of the judge
+    if (s->dprev.n != (size_t)N) GK(s->dprev.alloc(N));
+    GK(cudaMemsetAsync(s->dprev.p, 0, sizeof(float4) * N, st));
+    GK(s->A2.alloc(N)); GK(s->B2.alloc(N));
+    GK(s->crt2.alloc(Lh.ncloth));
+    GK(s->acc2.alloc((size_t)Lh.ncloth * s->acc_stride));
+    GK(cudaMemsetAsync(s->acc2.p, 0, sizeof(double) * (size_t)Lh.ncloth * s->acc_stride, st));
     GK(cudaStreamSynchronize(st));
     w->solver = s;
     s->ws = w;
@@ -419,24 +450,74 @@ int pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* 
     const int N = w->N;
     GK(cudaMemcpyAsync(w->Xn.p, s->X.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
     GK(cudaMemcpyAsync(w->Vn.p, s->V.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    GK(cudaMemcpyAsync(w->Dn.p, s->dprev.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
     int rc = pdg_solver_step(s, 1, nullptr);
     if (rc) return rc;
-    // inputs from (x_n, v_n, y), target (x* - y)/s from the solve
+    // inputs from (x_n, v_n, y, d_prev), target (x* - y - d_prev)/s from the solve
     k_node_feat<<<nb(N, 256), 256, 0, st>>>(N, w->Xn.p, w->Vn.p, s->Y.p, s->aux.p, w->stat.p, s->vcloth.p, s->cinfo.p,
-                                            w->xin.p);
+                                            w->Dn.p, w->xin.p);
     k_edge_feat<<<nb(N, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rest.p, s->Y.p, w->ef.p);
-    k_target<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->Y.p, s->aux.p, w->target.p, w->freew.p);
+    k_target<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->Y.p, s->aux.p, w->Dn.p, w->target.p, w->freew.p);
     int nfree = 0;
     for (const auto& a : s->L.aux) nfree += a.w >= 0.f ? 1 : 0;
     rc = forward(w, st);
     if (rc) return rc;
-    rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), st);
+    rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), w->energy ? w->ew.p : nullptr, st);
     if (rc) return rc;
     if (lr > 0.f) {
         rc = adam_step(w, lr, st);
         if (rc) return rc;
     }
-    s->launches += 8 + 3 * L + 6 * L + 4;
+    // features and target 3, forward 2 + 3L, loss and backward 5 + 7L, Adam
+    // and the bf16 refresh 3 + 3L
+    s->launches += 3 + (2 + 3 * L) + (5 + 7 * L) + (lr > 0.f ? 3 + 3 * L : 0);
+    double l = 0.0;
+    GK(cudaMemcpyAsync(&l, w->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    GK(cudaStreamSynchronize(st));
+    if (loss) *loss = (float)l;
+    return PDG_OK;
+}
+
+int pdg_warmstart_train_pair(pdg_warmstart* w, pdg_solver* traj, pdg_solver* deep, float lr, float* loss)
+{
+    if (!w || !traj || !deep || w->solver != traj)
+        return set_error(PDG_ERR_STATE, "pdg_warmstart_train_pair: the network must be attached to `traj`");
+    if (deep == traj || deep->L.ntot != traj->L.ntot || deep->L.ncloth != traj->L.ncloth ||
+        deep->L.perm_global != traj->L.perm_global || deep->kernel == PDG_KERNEL_PERSISTENT ||
+        deep->kernel == PDG_KERNEL_RESIDENT)
+        return set_error(PDG_ERR_ARG, "pdg_warmstart_train_pair: `deep` must solve the same cloths with the same "
+                                      "vertex layout (same patch plan, per-sweep kernels)");
+    cudaStream_t st = traj->stream;
+    const int N = w->N;
+    GK(cudaStreamSynchronize(deep->stream));
+    // inputs (x_n, v_n, d_prev) of the trajectory; the deep solve starts from the same state
+    GK(cudaMemcpyAsync(w->Xn.p, traj->X.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    GK(cudaMemcpyAsync(w->Vn.p, traj->V.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    GK(cudaMemcpyAsync(w->Dn.p, traj->dprev.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    GK(cudaMemcpyAsync(deep->X.p, traj->X.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    GK(cudaMemcpyAsync(deep->V.p, traj->V.p, sizeof(float4) * N, cudaMemcpyDeviceToDevice, st));
+    GK(cudaStreamSynchronize(st));
+    int rc = pdg_solver_step(deep, 1, nullptr);   // the target: x* of this frame
+    if (rc) return rc;
+    GK(cudaStreamSynchronize(deep->stream));
+    rc = pdg_solver_step(traj, 1, nullptr);       // the trajectory and its kept offsets advance
+    if (rc) return rc;
+    // y of both solvers is the same prediction from the same state
+    k_node_feat<<<nb(N, 256), 256, 0, st>>>(N, w->Xn.p, w->Vn.p, traj->Y.p, traj->aux.p, w->stat.p, traj->vcloth.p,
+                                            traj->cinfo.p, w->Dn.p, w->xin.p);
+    k_edge_feat<<<nb(N, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rest.p, traj->Y.p, w->ef.p);
+    k_target<<<nb(N, 256), 256, 0, st>>>(N, deep->X.p, traj->Y.p, traj->aux.p, w->Dn.p, w->target.p, w->freew.p);
+    int nfree = 0;
+    for (const auto& a : traj->L.aux) nfree += a.w >= 0.f ? 1 : 0;
+    rc = forward(w, st);
+    if (rc) return rc;
+    rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), w->energy ? w->ew.p : nullptr, st);
+    if (rc) return rc;
+    if (lr > 0.f) {
+        rc = adam_step(w, lr, st);
+        if (rc) return rc;
+    }
+    traj->launches += 3 + (2 + 3 * L) + (5 + 7 * L) + (lr > 0.f ? 3 + 3 * L : 0);
     double l = 0.0;
     GK(cudaMemcpyAsync(&l, w->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     GK(cudaStreamSynchronize(st));
@@ -449,6 +530,53 @@ int pdg_warmstart_set_smoothness(pdg_warmstart* w, float lambda)
     if (!w || !(lambda >= 0.f) || !std::isfinite(lambda))
         return set_error(PDG_ERR_ARG, "pdg_warmstart_set_smoothness: lambda must be finite and >= 0");
     w->smooth = lambda;
+    return PDG_OK;
+}
+
+int pdg_warmstart_time_inference(pdg_warmstart* w, int reps, float* ms)
+{
+    if (!w || reps <= 0 || !ms) return set_error(PDG_ERR_ARG, "pdg_warmstart_time_inference: bad arguments");
+    pdg_solver* s = w->solver;
+    if (!s) return set_error(PDG_ERR_STATE, "pdg_warmstart_time_inference: not attached to a solver");
+    cudaEvent_t e0, e1;
+    GK(cudaEventCreate(&e0));
+    GK(cudaEventCreate(&e1));
+    int rc = warm_infer_enqueue(w, s);   // untimed first run
+    GK(cudaEventRecord(e0, s->stream));
+    for (int r = 0; r < reps && rc == PDG_OK; ++r) rc = warm_infer_enqueue(w, s);
+    GK(cudaEventRecord(e1, s->stream));
+    GK(cudaEventSynchronize(e1));
+    float t = 0.f;
+    GK(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    s->launches += (long long)(reps + 1) * warm_kernel_count();
+    *ms = t / (float)reps;
+    return PDG_OK;
+}
+
+int pdg_warmstart_set_energy_norm(pdg_warmstart* w, int enable)
+{
+    if (!w) return set_error(PDG_ERR_ARG, "pdg_warmstart_set_energy_norm: null argument");
+    w->energy = enable ? 1 : 0;
+    return PDG_OK;
+}
+
+int pdg_warmstart_set_judge_sweeps(pdg_warmstart* w, int sweeps)
+{
+    if (!w || sweeps < 0 || sweeps > 1000)
+        return set_error(PDG_ERR_ARG, "pdg_warmstart_set_judge_sweeps: sweeps must be in [0, 1000]");
+    w->judge = sweeps;
+    // the frame graph of an attached solver holds the judge's launches
+    if (w->solver && w->solver->graph) { cudaGraphExecDestroy(w->solver->graph); w->solver->graph = nullptr; }
+    return PDG_OK;
+}
+
+int pdg_warmstart_get_judge_sweeps(const pdg_warmstart* w, int* sweeps)
+{
+    if (!w || !sweeps) return set_error(PDG_ERR_ARG, "pdg_warmstart_get_judge_sweeps: null argument");
+    *sweeps = w->judge;
     return PDG_OK;
 }
 

@@ -10,14 +10,16 @@ namespace pdg {
 namespace gnn {
 
 constexpr int H = 64;      // hidden width
-constexpr int NF = 10;     // node features
+constexpr int NF = 14;     // node features
 constexpr int NFP = 16;    // node features padded to one mma k-step
 constexpr int EF = 4;      // edge features
 constexpr int NO = 3;      // outputs
 constexpr int NOP = 8;     // outputs padded to one mma n-tile
 constexpr int L = 2;       // message-passing layers
 // length scales of the features: offsets and velocities in units of one
-// frame's gravity drop h^2 g at h = 1/60; rest lengths relative to 1 cm
+// frame's gravity drop h^2 g at h = 1/60; rest lengths relative to 1 cm.
+// Node features: (y - x_n)/s, h v_n/s, pinned flag, log mass, log stretch k,
+// log bend k, the previous frame's offset d_prev/s and its validity flag.
 constexpr float kOffsetScale = 2.725e-3f;
 constexpr float kLenScale = 0.01f;
 

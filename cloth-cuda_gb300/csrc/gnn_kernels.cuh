@@ -8,11 +8,11 @@
 // gradients are fp32 block reductions; Adam keeps fp32 master weights and
 // refreshes their bf16 copies after each step.
 //
-// Network (x: 10 node features, e_ij: 4 edge features):
+// Network (x: 14 node features, e_ij: 4 edge features):
 //   h0 = relu(We x + be)
 //   per layer: P = A h, Q = B h;  m_ij = relu(P_i + Q_j + C e_ij + c);
 //              a_i = mean_j m_ij;  h <- h + relu(U [h; a] + u)
-//   out = Wd h + bd     (offset / kOffsetScale)
+//   out = Wd h + bd     ((offset - previous offset) / kOffsetScale)
 #include "gnn.cuh"
 #include "pdg_solver.h"
 
@@ -251,14 +251,18 @@ __global__ void __launch_bounds__(256) k_msg_bwd(int N, const int* __restrict__ 
 }
 
 // Error d_i = (out_i[0:3] - target_i) w_i over free vertices (w in {0, 1}):
-//   loss = inv_cnt [ sum_i |d_i|^2 + lam/2 sum_(i,j) w_i w_j |d_i - d_j|^2 ]
-// over the directed edges (i, j) of the symmetric adjacency; the second
-// term weighs the error's differences between neighbours (its high-frequency
-// part).  dout_i = inv_cnt [2 d_i + 2 lam sum_j w_j (d_i - d_j)] w_i, one
-// thread per vertex, no atomics.
+//   loss = inv_cnt [ sum_i |d_i|^2 + lam/2 sum_(i,j) k_ij w_i w_j |d_i - d_j|^2 ]
+// over the directed edges (i, j) of the symmetric adjacency, with edge
+// weights k_ij (ew; null: 1).  The second term weighs the error's
+// differences between neighbours (its high-frequency part); with k_ij from
+// the PD system's diagonal it is the energy norm e^T (M + K) e / m of the
+// error, K approximated by a graph Laplacian with K's own diagonal.
+// dout_i = inv_cnt [2 d_i + 2 lam sum_j k_ij w_j (d_i - d_j)] w_i, one thread
+// per vertex, no atomics.
 __global__ void k_loss(int N, const float* __restrict__ out, const float* __restrict__ target,
                        const float* __restrict__ freew, const int* __restrict__ ptr, const int* __restrict__ adj,
-                       float lam, float inv_cnt, float* __restrict__ dout, double* __restrict__ loss)
+                       const float* __restrict__ ew, float lam, float inv_cnt, float* __restrict__ dout,
+                       double* __restrict__ loss)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float s = 0.f;
@@ -274,12 +278,12 @@ __global__ void k_loss(int N, const float* __restrict__ out, const float* __rest
         if (lam != 0.f && w > 0.f) {
             for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
                 const int j = adj[q];
-                const float wj = freew[j];
+                const float wj = freew[j] * (ew ? ew[q] : 1.f);
                 if (wj == 0.f) continue;
                 float e2 = 0.f;
                 #pragma unroll
                 for (int c = 0; c < NO; ++c) {
-                    const float e = d[c] - (out[(size_t)j * 16 + c] - target[(size_t)j * 3 + c]) * wj;
+                    const float e = d[c] - (out[(size_t)j * 16 + c] - target[(size_t)j * 3 + c]) * freew[j];
                     e2 += e * e;
                     gsum[c] += lam * wj * e;
                 }
@@ -338,21 +342,29 @@ __global__ void k_to_bf16(const float* __restrict__ src, int rows, int cols, bf1
 }
 
 // ---- solver-side feature kernels -----------------------------------------
-// node features: (y - x)/s, h v / s, pinned, scaled log mass / log stretch k / log bend k
+// Node features: (y - x)/s, h v / s, pinned, scaled log mass / log stretch k /
+// log bend k, then the previous frame's offset d_prev / s and its validity
+// (Dp.w: 1 when the vertex's state entering the frame is the one the solver
+// left after its previous frame, else 0 and d_prev = 0).
 __global__ void k_node_feat(int N, const float4* __restrict__ X, const float4* __restrict__ V,
                             const float4* __restrict__ Y, const float4* __restrict__ aux,
                             const float4* __restrict__ stat, const int* __restrict__ vcloth,
-                            const ClothInfo* __restrict__ cinfo, bf16* __restrict__ xin)
+                            const ClothInfo* __restrict__ cinfo, const float4* __restrict__ Dp,
+                            bf16* __restrict__ xin)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float4 x = X[i], v = V[i], y = Y[i], s = stat[i];
+    const float4 dp = Dp ? Dp[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float ok = dp.w > 0.f ? 1.f : 0.f;
     const float h = cinfo[vcloth[i]].h, is = 1.f / kOffsetScale;
     float f[NFP];
     f[0] = (y.x - x.x) * is; f[1] = (y.y - x.y) * is; f[2] = (y.z - x.z) * is;
     f[3] = h * v.x * is; f[4] = h * v.y * is; f[5] = h * v.z * is;
     f[6] = aux[i].w < 0.f ? 1.f : 0.f;
     f[7] = s.x; f[8] = s.y; f[9] = s.z;
+    f[10] = ok * dp.x * is; f[11] = ok * dp.y * is; f[12] = ok * dp.z * is;
+    f[13] = ok;
     for (int k = NF; k < NFP; ++k) f[k] = 0.f;
     for (int k = 0; k < NFP; k += 2)
         *reinterpret_cast<__nv_bfloat162*>(xin + (size_t)i * NFP + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
@@ -372,27 +384,39 @@ __global__ void k_edge_feat(int N, const int* __restrict__ ptr, const int* __res
     }
 }
 
-// target (x* - y)/s and free weight from the solver's result
+// Target of the network: (x* - y - d_prev)/s, i.e. the change of the
+// converged offset since the previous frame where d_prev is valid (the
+// prediction adds d_prev back, a skip connection in fp32), and the free weight.
 __global__ void k_target(int N, const float4* __restrict__ Xs, const float4* __restrict__ Y,
-                         const float4* __restrict__ aux, float* __restrict__ target, float* __restrict__ freew)
+                         const float4* __restrict__ aux, const float4* __restrict__ Dp, float* __restrict__ target,
+                         float* __restrict__ freew)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float4 x = Xs[i], y = Y[i];
+    const float4 dp = Dp ? Dp[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float ok = dp.w > 0.f ? 1.f : 0.f;
     const float is = 1.f / kOffsetScale;
-    target[3 * i] = (x.x - y.x) * is; target[3 * i + 1] = (x.y - y.y) * is; target[3 * i + 2] = (x.z - y.z) * is;
+    target[3 * i] = (x.x - y.x - ok * dp.x) * is;
+    target[3 * i + 1] = (x.y - y.y - ok * dp.y) * is;
+    target[3 * i + 2] = (x.z - y.z - ok * dp.z) * is;
     freew[i] = aux[i].w < 0.f ? 0.f : 1.f;
 }
 
-// predicted start offsets (pinned vertices keep the inertial start's target offset)
-__global__ void k_warm_out(int N, const float* __restrict__ out, const float4* __restrict__ A, float4* __restrict__ warm)
+// predicted start offsets d_prev + s out (pinned vertices keep the inertial
+// start's target offset)
+__global__ void k_warm_out(int N, const float* __restrict__ out, const float4* __restrict__ A,
+                           const float4* __restrict__ Dp, float4* __restrict__ warm)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float4 a = A[i];
+    const float4 dp = Dp ? Dp[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float ok = dp.w > 0.f ? 1.f : 0.f;
     warm[i] = a.w < 0.f ? a
-                        : make_float4(out[(size_t)i * 16] * kOffsetScale, out[(size_t)i * 16 + 1] * kOffsetScale,
-                                      out[(size_t)i * 16 + 2] * kOffsetScale, a.w);
+                        : make_float4(fmaf(out[(size_t)i * 16], kOffsetScale, ok * dp.x),
+                                      fmaf(out[(size_t)i * 16 + 1], kOffsetScale, ok * dp.y),
+                                      fmaf(out[(size_t)i * 16 + 2], kOffsetScale, ok * dp.z), a.w);
 }
 
 }  // namespace gnn

@@ -86,6 +86,82 @@ __global__ void k_select_vertex(int n, const int* __restrict__ vcloth, const Clo
     B[i] = w;
 }
 
+// Learned start judged after K sweeps: the inertial chain (buf, crt, acc)
+// and the learned chain (b) run K sweeps each from their own start; then
+// every cloth continues from the chain with the lower residual.
+// Start of the learned chain: per cloth its record (normaliser r(y)^2 from
+// the inertial start's evaluation in acc[slot_y], also given to the
+// inertial chain) and cleared per-sweep sums; one block per cloth.
+__global__ void k_warm_init_cloth(IterArgs a, IterArgs b, int slot_y)
+{
+    const int c = blockIdx.x;
+    const double r2y = a.acc[(size_t)c * a.acc_stride + slot_y];
+    if (threadIdx.x == 0) {
+        a.crt[c].res_y2 = r2y;
+        if (a.cinfo[c].init == 3) a.crt[c].warm = 1;
+        ClothRT r;
+        r.active = 1; r.used = 0; r.status = 0; r.warm = 1;
+        r.res_y2 = r2y; r.res0_2 = 0.0; r.resf_2 = -1.0;
+        b.crt[c] = r;
+    }
+    for (int k = threadIdx.x; k < b.acc_stride; k += blockDim.x) b.acc[(size_t)c * b.acc_stride + k] = 0.0;
+}
+
+// Start iterates of both chains: the learned chain starts from the
+// prediction (cloths asking for the judged learned start) or the inertial
+// start (others); cloths that always keep the prediction start from it on
+// the inertial chain too.
+__global__ void k_warm_init_vertex(int n, const int* __restrict__ vcloth, const ClothInfo* __restrict__ cinfo,
+                                   const float4* __restrict__ warm, float4* __restrict__ A, float4* __restrict__ B,
+                                   float4* __restrict__ A2, float4* __restrict__ B2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int init = cinfo[vcloth[i]].init;
+    const float4 s = init >= 2 ? warm[i] : A[i];
+    if (init == 3) { A[i] = s; B[i] = s; }
+    A2[i] = s;
+    B2[i] = s;
+}
+
+// The judge after K sweeps, one thread per cloth asking for the judged
+// learned start: each chain's last evaluated residual (that of x^(K-1) while
+// the chain iterates, its final one if it stopped; +inf after a failure or
+// without one) decides, ties to the inertial chain.  The learned chain's
+// record and per-sweep sums replace the inertial chain's when it wins.
+__global__ void k_judge_cloth(IterArgs a, IterArgs b, int K)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncloth || a.cinfo[c].init != 2) return;
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    auto eff = [&](const ClothRT& r, const double* acc) {
+        double v = r.status != 0 ? inf : (r.active ? acc[K - 1] : (r.resf_2 >= 0.0 ? r.resf_2 : inf));
+        return isfinite(v) ? v : inf;
+    };
+    double* am = a.acc + (size_t)c * a.acc_stride;
+    const double* al = b.acc + (size_t)c * b.acc_stride;
+    const ClothRT rm = a.crt[c], rl = b.crt[c];
+    if (!(eff(rl, al) < eff(rm, am))) return;
+    ClothRT r = rl;
+    r.warm = 1;
+    r.res_y2 = rm.res_y2;
+    a.crt[c] = r;
+    for (int k = 0; k < a.acc_stride - 2; ++k) am[k] = al[k];
+}
+
+// Vertices of cloths whose learned chain won take its iterates d^K, d^(K-1).
+__global__ void k_judge_vertex(int n, const int* __restrict__ vcloth, const ClothInfo* __restrict__ cinfo,
+                               const ClothRT* __restrict__ crt, float4* __restrict__ A, float4* __restrict__ B,
+                               const float4* __restrict__ A2, const float4* __restrict__ B2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = vcloth[i];
+    if (cinfo[c].init != 2 || !crt[c].warm) return;
+    A[i] = A2[i];
+    B[i] = B2[i];
+}
+
 __global__ void k_predict(const float4* __restrict__ X, const float4* __restrict__ V,
                           const float4* __restrict__ aux, const float* __restrict__ mass,
                           const int* __restrict__ vcloth, const ClothInfo* __restrict__ cinfo,
@@ -120,15 +196,35 @@ __global__ void k_finalize(float4* __restrict__ X, float4* __restrict__ V, const
 // AoS xyz (caller order, cloth by cloth) <-> float4 reordered.
 // Caller-order AoS xyz -> solver-order float4 (w = 0), for one or two
 // arrays per launch (x and v of a state copy).
+// The state a caller writes replaces the solver's; where it differs from the
+// solver's own (bitwise), the vertex's previous-frame offset kept for the
+// learned start (dprev, may be null) no longer belongs to its trajectory
+// and is marked invalid.
+__device__ __forceinline__ bool put_differs(float4 old, float x, float y, float z)
+{
+    return __float_as_uint(old.x) != __float_as_uint(x) || __float_as_uint(old.y) != __float_as_uint(y) ||
+           __float_as_uint(old.z) != __float_as_uint(z);
+}
+
 __global__ void k_scatter_state(const float* __restrict__ src0, float4* __restrict__ dst0,
                                 const float* __restrict__ src1, float4* __restrict__ dst1,
-                                const int* __restrict__ perm_global, int n)
+                                const int* __restrict__ perm_global, int n, float4* __restrict__ dprev)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int o = perm_global[i];
-    if (src0) dst0[i] = make_float4(src0[3 * o], src0[3 * o + 1], src0[3 * o + 2], 0.f);
-    if (src1) dst1[i] = make_float4(src1[3 * o], src1[3 * o + 1], src1[3 * o + 2], 0.f);
+    bool moved = false;
+    if (src0) {
+        const float4 a = make_float4(src0[3 * o], src0[3 * o + 1], src0[3 * o + 2], 0.f);
+        if (dprev) moved = put_differs(dst0[i], a.x, a.y, a.z);
+        dst0[i] = a;
+    }
+    if (src1) {
+        const float4 a = make_float4(src1[3 * o], src1[3 * o + 1], src1[3 * o + 2], 0.f);
+        if (dprev) moved = moved || put_differs(dst1[i], a.x, a.y, a.z);
+        dst1[i] = a;
+    }
+    if (moved) dprev[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __global__ void k_gather_state(const float4* __restrict__ src0, float* __restrict__ dst0,
@@ -146,13 +242,23 @@ __global__ void k_gather_state(const float4* __restrict__ src0, float* __restric
 // so the caller-side buffers (page-locked host memory accessed in place)
 // are read and written contiguously.
 __global__ void k_put_state(const float* __restrict__ x, const float* __restrict__ v, float4* __restrict__ X,
-                            float4* __restrict__ V, const int* __restrict__ inv, int n)
+                            float4* __restrict__ V, const int* __restrict__ inv, int n, float4* __restrict__ dprev)
 {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= n) return;
     const int i = inv[o];
-    if (x) X[i] = make_float4(x[3 * o], x[3 * o + 1], x[3 * o + 2], 0.f);
-    if (v) V[i] = make_float4(v[3 * o], v[3 * o + 1], v[3 * o + 2], 0.f);
+    bool moved = false;
+    if (x) {
+        const float4 a = make_float4(x[3 * o], x[3 * o + 1], x[3 * o + 2], 0.f);
+        if (dprev) moved = put_differs(X[i], a.x, a.y, a.z);
+        X[i] = a;
+    }
+    if (v) {
+        const float4 a = make_float4(v[3 * o], v[3 * o + 1], v[3 * o + 2], 0.f);
+        if (dprev) moved = moved || put_differs(V[i], a.x, a.y, a.z);
+        V[i] = a;
+    }
+    if (moved) dprev[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __global__ void k_take_state(const float4* __restrict__ X, const float4* __restrict__ V, float* __restrict__ x,
@@ -265,11 +371,59 @@ cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t sme
     return cudaGetLastError();
 }
 
+cudaError_t launch_warm_chain_init(const IterArgs& a, const IterArgs& b, int nt, int npatch, size_t smem,
+                                   const float4* warm, const int* vcloth, int n, cudaStream_t s)
+{
+    const int slot_y = a.acc_stride - 2;
+    static bool attr_set[3] = {false, false, false};
+    const int ti = nt == 128 ? 0 : (nt == 256 ? 1 : 2);
+    void* f = nt == 128 ? (void*)k_res_eval<128> : (nt == 256 ? (void*)k_res_eval<256> : (void*)k_res_eval<512>);
+    if (!attr_set[ti]) {
+        const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+        attr_set[ti] = true;
+    }
+    if (nt == 128) k_res_eval<128><<<npatch, 128, smem, s>>>(a, a.buf[0], slot_y);
+    else if (nt == 256) k_res_eval<256><<<npatch, 256, smem, s>>>(a, a.buf[0], slot_y);
+    else k_res_eval<512><<<npatch, 512, smem, s>>>(a, a.buf[0], slot_y);
+    k_warm_init_cloth<<<a.ncloth, 64, 0, s>>>(a, b, slot_y);
+    k_warm_init_vertex<<<nblk(n, 256), 256, 0, s>>>(n, vcloth, a.cinfo, warm, a.buf[0], a.buf[1], b.buf[0], b.buf[1]);
+    return cudaGetLastError();
+}
+
+// After a frame: the offset x_{n+1} - y_n of each vertex, valid (w = 1) for
+// free vertices of cloths whose solve succeeded; the learned start's feature
+// of the next frame.
+__global__ void k_keep_offset(int n, const float4* __restrict__ X, const float4* __restrict__ Y,
+                              const float4* __restrict__ aux, const int* __restrict__ vcloth,
+                              const ClothRT* __restrict__ crt, float4* __restrict__ Dp)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 x = X[i], y = Y[i];
+    const bool ok = aux[i].w >= 0.f && crt[vcloth[i]].status == 0;
+    Dp[i] = ok ? make_float4(x.x - y.x, x.y - y.y, x.z - y.z, 1.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+cudaError_t launch_keep_offset(const IterArgs& a, const float4* X, const float4* aux, const int* vcloth, float4* dprev,
+                               int n, cudaStream_t s)
+{
+    k_keep_offset<<<nblk(n, 256), 256, 0, s>>>(n, X, a.Y, aux, vcloth, a.crt, dprev);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warm_judge(const IterArgs& a, const IterArgs& b, int K, const int* vcloth, int n, cudaStream_t s)
+{
+    k_judge_cloth<<<nblk(a.ncloth, 128), 128, 0, s>>>(a, b, K);
+    k_judge_vertex<<<nblk(n, 256), 256, 0, s>>>(n, vcloth, a.cinfo, a.crt, a.buf[0], a.buf[1], b.buf[0], b.buf[1]);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s,
-                                 const float* src1, float4* dst1)
+                                 const float* src1, float4* dst1, float4* dprev)
 {
     if (n == 0 || (!src && !src1)) return cudaSuccess;
-    k_scatter_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, src1, dst1, perm, n);
+    k_scatter_state<<<nblk(n, 256), 256, 0, s>>>(src, dst, src1, dst1, perm, n, dprev);
     return cudaGetLastError();
 }
 
@@ -282,10 +436,10 @@ cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, 
 }
 
 cudaError_t launch_put_state(const float* x, const float* v, float4* X, float4* V, const int* inv, int n,
-                             cudaStream_t s)
+                             cudaStream_t s, float4* dprev)
 {
     if (n == 0 || (!x && !v)) return cudaSuccess;
-    k_put_state<<<nblk(n, 256), 256, 0, s>>>(x, v, X, V, inv, n);
+    k_put_state<<<nblk(n, 256), 256, 0, s>>>(x, v, X, V, inv, n, dprev);
     return cudaGetLastError();
 }
 

@@ -17,15 +17,29 @@ cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float
 // then the per-cloth choice between them (slots acc_stride-2 / -1).
 cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t smem, const float4* warm,
                                const int* vcloth, int n, cudaStream_t s);
+// Learned start judged after K sweeps: r(y) of the inertial start, then the
+// start records and iterates of the inertial chain `a` and the learned chain
+// `b` (same layout, own iterates, records and per-sweep sums).
+cudaError_t launch_warm_chain_init(const IterArgs& a, const IterArgs& b, int nt, int npatch, size_t smem,
+                                   const float4* warm, const int* vcloth, int n, cudaStream_t s);
+// After K sweeps of both chains: per cloth the chain with the lower residual
+// continues on `a`.
+cudaError_t launch_warm_judge(const IterArgs& a, const IterArgs& b, int K, const int* vcloth, int n, cudaStream_t s);
+// After a frame: each vertex's offset x - y into dprev (w = 1 valid), the
+// learned start's previous-offset feature of the next frame.
+cudaError_t launch_keep_offset(const IterArgs& a, const float4* X, const float4* aux, const int* vcloth, float4* dprev,
+                               int n, cudaStream_t s);
 // Caller order <-> solver order for one array, or two in one launch (src1/dst1).
+// dprev (may be null): vertices whose state changes lose their kept
+// previous-frame offset (the learned start's feature).
 cudaError_t launch_scatter_state(const float* src, float4* dst, const int* perm, int n, cudaStream_t s,
-                                 const float* src1 = nullptr, float4* dst1 = nullptr);
+                                 const float* src1 = nullptr, float4* dst1 = nullptr, float4* dprev = nullptr);
 cudaError_t launch_gather_state(const float4* src, float* dst, const int* perm, int n, cudaStream_t s,
                                 const float4* src1 = nullptr, float* dst1 = nullptr);
 // Whole-batch copies in caller order (inv: caller index -> reordered vertex);
 // x / v may be device pointers or mapped page-locked host memory.
 cudaError_t launch_put_state(const float* x, const float* v, float4* X, float4* V, const int* inv, int n,
-                             cudaStream_t s);
+                             cudaStream_t s, float4* dprev = nullptr);
 cudaError_t launch_take_state(const float4* X, const float4* V, float* x, float* v, const int* inv, int n,
                               cudaStream_t s);
 cudaError_t launch_apply_pins(float* pos, float* vel, const int* idx, const float* target, int P,

@@ -96,6 +96,12 @@ struct pdg_solver {
     int kernels_per_frame = 0;
 
     pdg::DevBuf<float4> X, V, Y, A, B, aux, warm;
+    // learned start (allocated when a network is attached): the previous
+    // frame's offset per vertex (w = 1 valid), and the learned chain's
+    // iterates, records and per-sweep sums for the judge after K sweeps
+    pdg::DevBuf<float4> dprev, A2, B2;
+    pdg::DevBuf<pdg::ClothRT> crt2;
+    pdg::DevBuf<double> acc2;
     pdg::DevBuf<float> mass, omega, stage_x, stage_v;
     pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, nbr_ptr, nbr;
     pdg::DevBuf<int> inv_global;   // caller-order index in the batch -> reordered vertex
@@ -132,5 +138,8 @@ int autotune_create(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes
 // learned warm start hooks (gnn.cu): features + forward into s->warm
 int warm_infer_enqueue(pdg_warmstart* w, pdg_solver* s);
 int warm_kernel_count();
+// sweeps each start runs before the judge compares them (0: compare the
+// start residuals)
+int warm_judge_sweeps(const pdg_warmstart* w);
 void warm_detach(pdg_warmstart* w);
 }  // namespace pdg

@@ -126,32 +126,93 @@ PersistArgs persist_args(pdg_solver* s)
     return p;
 }
 
-// Sweep k of the per-sweep launch structures.
-cudaError_t launch_sweep(pdg_solver* s, const IterArgs& a, int k, int res_only, cudaStream_t st)
+// Sweep k of the per-sweep launch structures.  after_sweep: the previous
+// launch on the stream is a sweep (the streaming kernel then overlaps it).
+cudaError_t launch_sweep(pdg_solver* s, const IterArgs& a, int k, int res_only, cudaStream_t st, bool after_sweep)
 {
     if (s->kernel == PDG_KERNEL_STREAM) {
         s->sargs.spin_budget = s->wait_budget;
-        return launch_stream(a, s->sargs, s->mode, s->nt, s->persist_grid, s->stream_smem, k, res_only, st, k >= 1);
+        return launch_stream(a, s->sargs, s->mode, s->nt, s->persist_grid, s->stream_smem, k, res_only, st,
+                             after_sweep);
     }
     return launch_iter(a, s->mode, s->nt, s->L.npatch, s->L.smem_bytes, k, res_only, st, s->carveout);
+}
+
+// Arguments of the learned chain: the inertial chain's, with its own
+// iterates, records and per-sweep sums.
+IterArgs learned_chain(pdg_solver* s, const IterArgs& a)
+{
+    IterArgs b = a;
+    b.buf[0] = s->A2.p; b.buf[1] = s->B2.p;
+    b.crt = s->crt2.p; b.acc = s->acc2.p;
+    return b;
+}
+
+// Sweeps each start runs before the learned start is judged (0: the start
+// residuals are compared), at most the sweep cap.
+int judge_sweeps(const pdg_solver* s)
+{
+    return (s->ws && s->any_warm) ? std::min(warm_judge_sweeps(s->ws), s->L.cap) : 0;
+}
+
+// Launches of one frame as a sequence of stream-ordered launches; the events
+// (may be null) bracket the sweeps of the iteration loop.
+cudaError_t enqueue_frame_launches(pdg_solver* s, cudaStream_t st, cudaEvent_t ev_sweeps0, cudaEvent_t ev_sweeps1,
+                                   int* warm_rc)
+{
+    const HostLayout& L = s->L;
+    const IterArgs a = iter_args(s);
+    cudaError_t e = launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, nullptr, L.ntot, st);
+    if (e != cudaSuccess) return e;
+    const int K = judge_sweeps(s);
+    int k0 = 0;
+    if (a.warm_active) {   // learned start: predict, then judge it against the inertial start
+        *warm_rc = warm_infer_enqueue(s->ws, s);
+        if (*warm_rc) return cudaSuccess;
+        if (K == 0) {
+            e = launch_warm_select(a, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st);
+        } else {
+            // both starts run K sweeps on their own chains; every cloth then
+            // continues from the chain with the lower residual
+            const IterArgs b = learned_chain(s, a);
+            e = launch_warm_chain_init(a, b, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st);
+            if (ev_sweeps0) cudaEventRecord(ev_sweeps0, st);
+            for (int k = 0; k < K && e == cudaSuccess; ++k) e = launch_sweep(s, a, k, 0, st, k >= 1);
+            for (int k = 0; k < K && e == cudaSuccess; ++k) e = launch_sweep(s, b, k, 0, st, true);
+            if (e == cudaSuccess) e = launch_warm_judge(a, b, K, s->vcloth.p, L.ntot, st);
+            k0 = K;
+        }
+        if (e != cudaSuccess) return e;
+    }
+    if (ev_sweeps0 && k0 == 0) cudaEventRecord(ev_sweeps0, st);
+    for (int k = k0; k < L.cap && e == cudaSuccess; ++k) e = launch_sweep(s, a, k, 0, st, k > k0);
+    if (ev_sweeps1) cudaEventRecord(ev_sweeps1, st);
+    if (e == cudaSuccess && s->have_final) e = launch_sweep(s, a, L.cap, 1, st, L.cap > k0);
+    if (e == cudaSuccess) e = launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st);
+    if (e == cudaSuccess && s->ws) e = launch_keep_offset(a, s->X.p, s->aux.p, s->vcloth.p, s->dprev.p, L.ntot, st);
+    return e;
 }
 
 // One frame as a sequence of stream-ordered launches.
 int enqueue_frame(pdg_solver* s)
 {
-    const HostLayout& L = s->L;
-    cudaStream_t st = s->stream;
-    const IterArgs a = iter_args(s);
-    CK(launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, nullptr, L.ntot, st));
-    if (a.warm_active) {   // learned start: predict, measure both starts, keep the better per cloth
-        const int rc = warm_infer_enqueue(s->ws, s);
-        if (rc) return rc;
-        CK(launch_warm_select(a, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st));
-    }
-    for (int k = 0; k < L.cap; ++k) CK(launch_sweep(s, a, k, 0, st));
-    if (s->have_final) CK(launch_sweep(s, a, L.cap, 1, st));
-    CK(launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st));
+    int wrc = PDG_OK;
+    const cudaError_t e = enqueue_frame_launches(s, s->stream, nullptr, nullptr, &wrc);
+    if (wrc) return wrc;
+    CK(e);
     return PDG_OK;
+}
+
+// Launches of one frame beyond the solver's own (learned start).
+long long warm_launches(const pdg_solver* s)
+{
+    if (!s->ws) return 0;
+    long long n = 1;   // the kept offset
+    if (s->any_warm) {
+        const int K = judge_sweeps(s);
+        n += warm_kernel_count() + (K == 0 ? 4 : 3 + K + 2);
+    }
+    return n;
 }
 
 int build_graph(pdg_solver* s)
@@ -343,8 +404,80 @@ int pdg_solver_create_batch(int n, const pdg_config* cfgs, const pdg_mesh* const
     }
 }
 
-int pdg_layout_check(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
-                     int patch_verts, pdg_layout_info* info)
+// One mistake planted in a built layout (for the checker's own tests): false
+// if the layout offers no place for it.
+static bool plant_mistake(HostLayout& L, int mistake)
+{
+    auto patch_with = [&](auto pred) -> int {
+        for (int p = 0; p < L.npatch; ++p)
+            if (pred(L.patches[p])) return p;
+        return -1;
+    };
+    switch (mistake) {
+        case 1: {   // two vertices' caller indices swapped
+            const ClothInfo& c = L.cinfo[0];
+            if (c.nverts < 2) return false;
+            std::swap(L.perm_global[c.vbegin], L.perm_global[c.vbegin + 1]);
+            return true;
+        }
+        case 2: {   // a halo entry repeated
+            const int p = patch_with([](const PatchHdr& h) { return h.nlocal - h.nown >= 2; });
+            if (p < 0) return false;
+            L.halo[L.patches[p].halo_off + 1] = L.halo[L.patches[p].halo_off];
+            return true;
+        }
+        case 3: {   // a boundary vertex moved past the published prefix
+            const int p = patch_with([](const PatchHdr& h) { return h.nbnd >= 1; });
+            if (p < 0) return false;
+            L.patches[p].nbnd -= 1;
+            return true;
+        }
+        case 4: {   // two records pointed at one contribution slot of a vertex they share
+            auto corner = [](const CellRec& r, int k) {
+                const uint32_t w = k < 2 ? r.c01 : (k < 4 ? r.c23 : r.x12);
+                return (k & 1) ? w >> 16 : w & 0xffffu;
+            };
+            auto slot_ref = [](CellRec& r, int k) -> uint32_t& { return k < 2 ? r.vm01 : (k < 4 ? r.vm23 : r.vm45); };
+            auto slot_of = [&](CellRec& r, int k) { return (k & 1) ? slot_ref(r, k) >> 16 : slot_ref(r, k) & 0xffffu; };
+            for (int p = 0; p < L.npatch; ++p) {
+                const PatchHdr& h = L.patches[p];
+                for (int q = 0; q + 1 < h.ncell; ++q)
+                    for (int q2 = q + 1; q2 < h.ncell; ++q2) {
+                        CellRec& a = L.cells[h.cell_off + q];
+                        CellRec& b = L.cells[h.cell_off + q2];
+                        for (int ka = 0; ka < 6; ++ka)
+                            for (int kb = 0; kb < 6; ++kb) {
+                                if (corner(a, ka) != corner(b, kb) || slot_of(a, ka) == 0xffffu ||
+                                    slot_of(b, kb) == 0xffffu)
+                                    continue;
+                                const uint32_t sb = slot_of(b, kb);
+                                uint32_t& w = slot_ref(a, ka);
+                                w = (ka & 1) ? ((w & 0xffffu) | (sb << 16)) : ((w & 0xffff0000u) | sb);
+                                return true;
+                            }
+                    }
+            }
+            return false;
+        }
+        case 5: {   // a cell dropped
+            const int p = patch_with([](const PatchHdr& h) { return h.ncell >= 2; });
+            if (p < 0) return false;
+            L.patches[p].ncell -= 1;
+            if (L.patches[p].ncell_a > L.patches[p].ncell) L.patches[p].ncell_a = L.patches[p].ncell;
+            return true;
+        }
+        case 6: {   // a halo entry out of range
+            const int p = patch_with([](const PatchHdr& h) { return h.nlocal - h.nown >= 1; });
+            if (p < 0) return false;
+            L.halo[L.patches[p].halo_off] = L.ntot + 5;
+            return true;
+        }
+    }
+    return false;
+}
+
+static int layout_check_impl(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes,
+                             const pdg_constraints* const* cons, int patch_verts, int mistake, pdg_layout_info* info)
 {
     try {
         if (n <= 0 || !cfgs || !meshes || !cons || !info) return set_error(PDG_ERR_ARG, "pdg_layout_check: bad arguments");
@@ -368,12 +501,27 @@ int pdg_layout_check(int n, const pdg_config* cfgs, const pdg_mesh* const* meshe
         info->cells = (long long)L.cells.size();
         info->lone_hinges = (long long)L.hinges.size();
         info->smem_resident = (long long)L.smem_resident;
+        if (mistake && !plant_mistake(L, mistake))
+            return set_error(PDG_ERR_ARG, "pdg_layout_check_planted: no place for mistake %d in this layout", mistake);
         err = check_layout(cl, L);
         if (!err.empty()) return set_error(PDG_ERR_STATE, "layout check: %s", err.c_str());
         return PDG_OK;
     } catch (const std::bad_alloc&) {
         return set_error(PDG_ERR_ALLOC, "host allocation failed");
     }
+}
+
+int pdg_layout_check(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes, const pdg_constraints* const* cons,
+                     int patch_verts, pdg_layout_info* info)
+{
+    return layout_check_impl(n, cfgs, meshes, cons, patch_verts, 0, info);
+}
+
+int pdg_layout_check_planted(int n, const pdg_config* cfgs, const pdg_mesh* const* meshes,
+                             const pdg_constraints* const* cons, int patch_verts, int mistake, pdg_layout_info* info)
+{
+    if (mistake < 1 || mistake > 6) return set_error(PDG_ERR_ARG, "pdg_layout_check_planted: mistake must be 1..6");
+    return layout_check_impl(n, cfgs, meshes, cons, patch_verts, mistake, info);
 }
 
 int pdg_solver_num_cloths(const pdg_solver* s, int* n)
@@ -438,7 +586,7 @@ static int enqueue_frames(pdg_solver* s, int nframes, const FrameIO* io)
                 if (rc) return rc;
             }
             CK(cudaGraphLaunch(s->graph, s->stream));
-            s->launches += s->kernels_per_frame + ((s->ws && s->any_warm) ? warm_kernel_count() + 4 : 0);
+            s->launches += s->kernels_per_frame + warm_launches(s);
         }
     }
     return PDG_OK;
@@ -496,7 +644,7 @@ static int put_state(pdg_solver* s, int vb, int n, const float* x, const float* 
         x = x ? s->stage_x.p : nullptr;
         v = v ? s->stage_v.p : nullptr;
     }
-    CK(launch_scatter_state(x, s->X.p + vb, perm, n, s->stream, v, s->V.p + vb));
+    CK(launch_scatter_state(x, s->X.p + vb, perm, n, s->stream, v, s->V.p + vb, s->dprev.p ? s->dprev.p + vb : nullptr));
     return PDG_OK;
 }
 
@@ -618,7 +766,7 @@ int pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const fl
             CK(cudaMemcpyAsync(s->stage_v.p, v_in, bytes, cudaMemcpyHostToDevice, s->stream));
             dv = s->stage_v.p;
         }
-        CK(launch_put_state(dx, dv, s->X.p, s->V.p, s->inv_global.p, n, s->stream));
+        CK(launch_put_state(dx, dv, s->X.p, s->V.p, s->inv_global.p, n, s->stream, s->dprev.p));
     }
     // the frames, then the download: all stream-ordered behind the upload
     int rc = pdg_solver_step(s, nframes, nullptr);
@@ -634,6 +782,35 @@ int pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const fl
     }
     if (stats) return pdg_solver_step(s, 0, stats);   // reads the last frame's records (synchronises)
     CK(cudaStreamSynchronize(s->stream));
+    return PDG_OK;
+}
+
+int pdg_solver_set_tolerance(pdg_solver* s, int cloth, float tolerance)
+{
+    if (!s || !(tolerance >= 0.f) || !std::isfinite(tolerance))
+        return set_error(PDG_ERR_ARG, "pdg_solver_set_tolerance: tolerance must be finite and >= 0");
+    if (cloth < -1 || cloth >= s->L.ncloth) return set_error(PDG_ERR_ARG, "pdg_solver_set_tolerance: bad cloth");
+    const int c0 = cloth < 0 ? 0 : cloth, c1 = cloth < 0 ? s->L.ncloth : cloth + 1;
+    for (int c = c0; c < c1; ++c) {
+        s->L.cinfo[c].tol = tolerance;
+        s->cloths[c].cfg.tolerance = tolerance;
+    }
+    CK(cudaMemcpyAsync(s->cinfo.p, s->L.cinfo.data(), sizeof(ClothInfo) * s->L.cinfo.size(), cudaMemcpyHostToDevice,
+                       s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    // the launch plan's choices that depend on the tolerance (as at creation)
+    if (s->kernel == PDG_KERNEL_RESIDENT) {
+        s->nbr_sync = 1;
+        for (const auto& c : s->cloths)
+            if (c.cfg.tolerance > 0.f) s->nbr_sync = 0;
+    }
+    const pdg_config& f = s->cloths[0].cfg;
+    const int hf = (s->mode == PDG_MODE_CONSISTENT) && (f.compute_final_residual || f.tolerance > 0.f);
+    if (hf != s->have_final) {
+        s->have_final = hf;
+        s->kernels_per_frame = 4 + s->L.cap + (hf ? 1 : 0);
+        if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    }
     return PDG_OK;
 }
 
@@ -694,20 +871,11 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
             s->launches += 1;
             cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
         } else {
-            const IterArgs a = iter_args(s);
-            cudaError_t err = launch_predict(a, s->X.p, s->V.p, s->aux.p, s->mass.p, s->vcloth.p, nullptr, L.ntot, st);
-            if (err == cudaSuccess && a.warm_active) {
-                const int wrc = warm_infer_enqueue(s->ws, s);
-                if (wrc) { rc = wrc; break; }
-                err = launch_warm_select(a, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st);
-            }
-            cudaEventRecord(e[1], st);
-            for (int k = 0; k < L.cap && err == cudaSuccess; ++k) err = launch_sweep(s, a, k, 0, st);
-            cudaEventRecord(e[2], st);
-            if (err == cudaSuccess && s->have_final) err = launch_sweep(s, a, L.cap, 1, st);
-            if (err == cudaSuccess) err = launch_finalize(a, s->X.p, s->V.p, s->aux.p, s->vcloth.p, L.ntot, st);
+            int wrc = PDG_OK;
+            const cudaError_t err = enqueue_frame_launches(s, st, e[1], e[2], &wrc);
+            if (wrc) { rc = wrc; break; }
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "frame launch: %s", cudaGetErrorString(err));
-            s->launches += s->kernels_per_frame + ((s->ws && s->any_warm) ? warm_kernel_count() + 4 : 0);
+            s->launches += s->kernels_per_frame + warm_launches(s);
         }
         cudaEventRecord(e[3], st);
         cudaError_t se = cudaEventSynchronize(e[3]);

@@ -21,6 +21,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_ALLOC, ERR_STATE, ERR_TIMEOUT, ERR_NUMERIC, ERR_IO = 
 MODE_CONSISTENT, MODE_REFERENCE_LITERAL = 0, 1
 INIT_INERTIAL, INIT_PREVIOUS, INIT_WARMSTART, INIT_WARMSTART_KEEP = 0, 1, 2, 3
 KERNEL_AUTO, KERNEL_GRAPH, KERNEL_PERSISTENT, KERNEL_RESIDENT, KERNEL_AUTOTUNE, KERNEL_STREAM = 0, 1, 2, 3, 4, 5
+NODE_FEATURES = 14   # node features of the learned warm start
 
 
 class PDGError(RuntimeError):
@@ -97,6 +98,21 @@ def layout_check(cfg, meshes, cons, patch_verts):
     info = LayoutInfo()
     _check(lib().pdg_layout_check(n, (Config * n)(*cfgs), (C.c_void_p * n)(*[m.h.value for m in meshes]),
                                   (C.c_void_p * n)(*[c.h.value for c in cons]), patch_verts, C.byref(info)))
+    return info.as_dict()
+
+
+def layout_check_planted(cfg, meshes, cons, patch_verts, mistake):
+    """pdg_layout_check_planted: the layout check after planting mistake
+    1..6 (see include/pdg.h); raises PDGError with the checker's finding."""
+    single = isinstance(meshes, Mesh)
+    meshes = [meshes] if single else list(meshes)
+    cons = [cons] if single else list(cons)
+    cfgs = [cfg] * len(meshes) if isinstance(cfg, Config) else list(cfg)
+    n = len(meshes)
+    info = LayoutInfo()
+    _check(lib().pdg_layout_check_planted(n, (Config * n)(*cfgs), (C.c_void_p * n)(*[m.h.value for m in meshes]),
+                                          (C.c_void_p * n)(*[c.h.value for c in cons]), patch_verts, mistake,
+                                          C.byref(info)))
     return info.as_dict()
 
 
@@ -348,6 +364,10 @@ class Solver:
                                           C.cast(st, C.c_void_p) if stats else None))
         return [s.as_dict() for s in st] if stats else None
 
+    def set_tolerance(self, tol, cloth=-1):
+        """Relative-residual target of one cloth (-1: all); 0 runs the cap."""
+        _check(lib().pdg_solver_set_tolerance(self.h, cloth, C.c_float(tol)))
+
     def set_pin_targets(self, targets, cloth=0):
         t = _f32(targets).reshape(-1, 3)
         _check(lib().pdg_solver_set_pin_targets(self.h, cloth, _p(t)))
@@ -423,13 +443,15 @@ class WarmStart:
         assert p.size == self.count
         _check(lib().pdg_warmstart_set_params(self.h, _p(p)))
 
-    def eval(self, x, ptr, adj, ef, target, freew):
-        x = _f32(x).reshape(-1, 10); ptr = _i32(ptr); adj = _i32(adj); ef = _f32(ef).reshape(-1, 4)
+    def eval(self, x, ptr, adj, ef, target, freew, ew=None):
+        x = _f32(x).reshape(-1, NODE_FEATURES); ptr = _i32(ptr); adj = _i32(adj); ef = _f32(ef).reshape(-1, 4)
         target = _f32(target).reshape(-1, 3); freew = _f32(freew)
+        ewa = None if ew is None else _f32(ew).reshape(-1)
         N = len(x)
         out = np.zeros((N, 3), np.float32); grads = np.zeros(self.count, np.float32); loss = C.c_float()
         _check(lib().pdg_warmstart_eval(self.h, N, _p(x), _p(ptr), _p(adj) if adj.size else None,
-                                        _p(ef) if ef.size else None, _p(target), _p(freew), _p(out),
+                                        _p(ef) if ef.size else None, _p(target), _p(freew),
+                                        _p(ewa) if ewa is not None and ewa.size else None, _p(out),
                                         C.byref(loss), _p(grads)))
         return out, loss.value, grads
 
@@ -444,6 +466,35 @@ class WarmStart:
         """Weight of the neighbour-difference term of the loss (0: plain MSE)."""
         _check(lib().pdg_warmstart_set_smoothness(self.h, C.c_float(lam)))
         return self
+
+    def set_energy_norm(self, enable=True):
+        """Weigh the neighbour-difference term by the PD system's stiffness
+        (the error's energy norm) when training on an attached solver."""
+        _check(lib().pdg_warmstart_set_energy_norm(self.h, 1 if enable else 0))
+        return self
+
+    def set_judge_sweeps(self, k):
+        """Sweeps each start runs before the judge compares them (0: start residuals)."""
+        _check(lib().pdg_warmstart_set_judge_sweeps(self.h, int(k)))
+        return self
+
+    def time_inference(self, reps=5):
+        """Mean device ms of one prediction on the attached solver's state."""
+        ms = C.c_float()
+        _check(lib().pdg_warmstart_time_inference(self.h, int(reps), C.byref(ms)))
+        return ms.value
+
+    @property
+    def judge_sweeps(self):
+        k = C.c_int()
+        _check(lib().pdg_warmstart_get_judge_sweeps(self.h, C.byref(k)))
+        return k.value
+
+    def train_pair(self, traj, deep, lr):
+        """One training step on traj's trajectory with deep's solve as target."""
+        loss = C.c_float()
+        _check(lib().pdg_warmstart_train_pair(self.h, traj.h, deep.h, C.c_float(lr), C.byref(loss)))
+        return loss.value
 
     def train_frame(self, solver, lr):
         loss = C.c_float()

@@ -1,20 +1,31 @@
 """Train and evaluate the learned warm start on data the PD solver generates.
 
-    python cloth-cuda_gb300/train_warmstart.py [--trajectories 256] [--frames 64]
-        [--batch 32] [--lr 1e-3] [--smoothness 0] [--eval-seeds 128] [--out params.npy] [--json result.json]
+    python cloth-cuda_gb300/train_warmstart.py [--trajectories 2000] [--frames 64]
+        [--batch 32] [--lr 1e-3] [--smoothness 0] [--energy-norm] [--eval-seeds 128]
+        [--eval-frames 16] [--judge 0,4] [--out params.npy] [--json result.json]
 
-Training data: trajectories of cloths drawn from the batched-workload
-distribution (scenes.batch), `batch` cloths per solver; every frame of every
-trajectory is one training batch: inputs (x_n, v_n, y), target the solver's
-frame result x_{n+1} - y, computed with a deep solve (cap 400 sweeps, relative
-residual 1e-6) so the target is close to the converged positions.  Loss: MSE
-plus --smoothness times the squared error differences over the mesh edges;
-Adam.  Evaluation on `eval_seeds` held-out cloths: for each, the same frames
-are solved from the inertial start, from the learned start kept only where
-its residual is lower, and from the learned start always kept, to relative
-residual --eval-tol (1e-5) with cap 200; the script reports the
-start-residual ratio, iterations, convergence and the vertex-steps/s of
-each, and the sweeps saved on the frames both starts solve.
+The committed parameters (cloth-cuda_gb300/warmstart_params.npy) were made by
+
+    python cloth-cuda_gb300/train_warmstart.py --trajectories 2000 --frames 64 --batch 32 \\
+        --out cloth-cuda_gb300/warmstart_params.npy --json gpurun_out/train.json
+
+Training data: 2,000 trajectories of 64 frames of cloths drawn from the
+batched-workload distribution (scenes.batch: grid side 17..129, 0.5-2 m,
+1-4 boundary pins, stretch k 1e2..1e4, bend k 1e-3..1e-1, wind N(0, 2)),
+`batch` cloths per solver and per Adam step; every frame of every trajectory
+is one training batch: inputs (x_n, v_n, y, d_prev) of the trajectory, which
+is solved as in use (cap --traj-cap sweeps, tolerance --traj-tol), target
+x* - y - d_prev from a deep solve of the same frame from the same state (cap
+--target-cap sweeps, relative residual --target-tol) so the target is close
+to the converged positions (pdg_warmstart_train_pair).
+Loss: MSE, plus --smoothness times the squared error differences over the
+mesh edges (weighted by the PD system's stiffness with --energy-norm); Adam,
+lr 1e-3.  Evaluation on --eval-seeds held-out cloths (seeds disjoint from
+training): the same frames are solved from the inertial start and from the
+judged learned start (judge after K sweeps for each K of --judge) to each
+relative residual of --eval-tols with cap 200; the script reports sweeps,
+convergence, the fraction of cloth-frames where the learned start was kept,
+and the sweeps saved on the frames both starts solve.
 """
 from __future__ import annotations
 
@@ -32,120 +43,168 @@ sys.path.insert(0, HERE)
 import pdg  # noqa: E402
 import scenes  # noqa: E402
 
+PARAMS = os.path.join(HERE, "warmstart_params.npy")
+TRAIN_SEED0 = 1000          # training batches: seeds 1000, 1001, ...
+EVAL_SEED0 = 900000         # held-out evaluation batches
+
+
+def load_params(path=PARAMS):
+    """The committed network parameters (float32, pdg_warmstart layout)."""
+    return np.load(path).astype(np.float32)
+
+
+def _pair(args, seed):
+    """The trajectory solver (solved as in use: cap --traj-cap, tolerance
+    --traj-tol) and the deep solver of the targets, over the same cloths."""
+    out = []
+    for cap, tol in ((args.traj_cap, args.traj_tol), (args.target_cap, args.target_tol)):
+        ms, cs, cfgs, _ = scenes.batch(args.batch, seed=seed, max_iterations=cap, tolerance=tol,
+                                       kernel=pdg.KERNEL_STREAM, patch_verts=128, block_threads=128,
+                                       n_range=args.n_range)
+        out.append(pdg.Solver(cfgs, ms, cs))
+    return out
+
 
 def train(args, log=print):
-    w = pdg.WarmStart(seed=args.seed).set_smoothness(args.smoothness)
+    w = pdg.WarmStart(seed=args.seed).set_smoothness(args.smoothness).set_energy_norm(args.energy_norm)
     nbatches = max(1, args.trajectories // args.batch)
     losses = []
     t0 = time.time()
     for b in range(nbatches):
-        ms, cs, cfgs, _ = scenes.batch(args.batch, seed=1000 + b, max_iterations=args.target_cap,
-                                       tolerance=args.target_tol, kernel=pdg.KERNEL_GRAPH, n_range=args.n_range)
-        s = pdg.Solver(cfgs, ms, cs)
-        w.attach(s)
-        bl = [w.train_frame(s, args.lr) for _ in range(args.frames)]
+        traj, deep = _pair(args, TRAIN_SEED0 + b)
+        w.attach(traj)
+        bl = [w.train_pair(traj, deep, args.lr) for _ in range(args.frames)]
         losses.append(float(np.mean(bl)))
-        log("batch %d/%d  mean loss %.4f  (%.1f s)" % (b + 1, nbatches, losses[-1], time.time() - t0))
-        s.close()
+        if b % 8 == 0 or b == nbatches - 1:
+            log("batch %d/%d  mean loss %.4f  (%.1f s)" % (b + 1, nbatches, losses[-1], time.time() - t0))
+        traj.close(); deep.close()
         w.solver = None
     return w, losses
 
 
 def score(params, args, seeds=2, frames=32, base_seed=500000):
-    """Mean squared offset error (lr = 0, no smoothness term) of `params` on
-    held-out trajectories."""
+    """Mean squared error (lr = 0, no smoothness term) of the prediction of
+    `params` on held-out trajectories: the target is the change of the
+    converged offset since the previous frame, so zero parameters score the
+    previous frame's offset as the prediction."""
     out = []
     for b in range(seeds):
-        ms, cs, cfgs, _ = scenes.batch(args.batch, seed=base_seed + b, max_iterations=args.target_cap,
-                                       tolerance=args.target_tol, kernel=pdg.KERNEL_GRAPH, n_range=args.n_range)
-        s = pdg.Solver(cfgs, ms, cs)
+        traj, deep = _pair(args, base_seed + b)
         w = pdg.WarmStart(seed=0)
         w.set_params(params)
-        w.attach(s)
-        out += [w.train_frame(s, 0.0) for _ in range(frames)]
-        s.close(); w.close()
+        w.attach(traj)
+        out += [w.train_pair(traj, deep, 0.0) for _ in range(frames)]
+        traj.close(); deep.close(); w.close()
     return float(np.mean(out))
 
 
+def solve_frames(params, cfg_kw, seed, count, frames, n_range, judge=4):
+    """Per-cloth frame stats of `frames` frames of one held-out batch, and
+    the host time of the frames (each step call synchronises)."""
+    ms, cs, cfgs, _ = scenes.batch(count, seed=seed, n_range=n_range, **cfg_kw)
+    s = pdg.Solver(cfgs, ms, cs)
+    w = None
+    if params is not None:
+        w = pdg.WarmStart(seed=0)
+        w.set_params(params)
+        w.set_judge_sweeps(judge)
+        w.attach(s)
+    st_all, t = [], 0.0
+    for f in range(frames):
+        t0 = time.perf_counter()
+        st = s.step(1)
+        t += time.perf_counter() - t0
+        st_all += [dict(frame=f, **x) for x in st]
+    N = sum(m.N for m in ms)
+    s.close()
+    if w is not None:
+        w.close()
+    return st_all, N * frames, t
+
+
+def summarize(rows):
+    return dict(iterations_mean=float(np.mean([x["iterations"] for x in rows])),
+                converged_fraction=float(np.mean([x["converged"] for x in rows])),
+                rel_residual_median=float(np.median([x["rel_residual"] for x in rows])),
+                learned_start_kept=float(np.mean([x["warm_start_used"] for x in rows])))
+
+
 def evaluate(params, args, log=print):
-    res = {"inertial": [], "learned": [], "learned_kept": []}
-    times = {"inertial": 0.0, "learned": 0.0, "learned_kept": 0.0}
-    verts = {"inertial": 0, "learned": 0, "learned_kept": 0}
+    """Inertial vs judged learned start on held-out cloths, per tolerance and
+    judge sweep count."""
     nb = max(1, args.eval_seeds // args.batch)
-    for b in range(nb):
-        for mode in ("inertial", "learned", "learned_kept"):
-            init = {"inertial": pdg.INIT_INERTIAL, "learned": pdg.INIT_WARMSTART,
-                    "learned_kept": pdg.INIT_WARMSTART_KEEP}[mode]
-            ms, cs, cfgs, _ = scenes.batch(args.batch, seed=900000 + b, max_iterations=200,
-                                           tolerance=args.eval_tol, kernel=pdg.KERNEL_GRAPH, init=init,
-                                           n_range=args.n_range)
-            s = pdg.Solver(cfgs, ms, cs)
-            w = None
-            if mode != "inertial":
-                w = pdg.WarmStart(seed=0)
-                w.set_params(params)
-                w.attach(s)
-            N = sum(m.N for m in ms)
-            for f in range(args.eval_frames):
-                t0 = time.perf_counter()
-                st = s.step(1)
-                times[mode] += time.perf_counter() - t0
-                verts[mode] += N
-                res[mode] += [dict(frame=f, **x) for x in st]
-            s.close()
-            if w is not None:
-                w.close()
     out = {}
-    for mode in res:
-        r = res[mode]
-        out[mode] = dict(
-            iterations_mean=float(np.mean([x["iterations"] for x in r])),
-            converged_fraction=float(np.mean([x["converged"] for x in r])),
-            start_ratio_mean=float(np.mean([x["res_initial"] / max(x["res_inertial"], 1e-30) for x in r])),
-            rel_residual_median=float(np.median([x["rel_residual"] for x in r])),
-            learned_start_kept=float(np.mean([x["warm_start_used"] for x in r])),
-            vertex_steps_per_s_host_timed=verts[mode] / max(times[mode], 1e-9))
-        log(mode, json.dumps(out[mode]))
-    # sweeps to the tolerance on the frames both starts reach it
-    for mode in ("learned", "learned_kept"):
-        both = [(xi["iterations"], xl["iterations"]) for xi, xl in zip(res["inertial"], res[mode])
-                if xi["converged"] and xl["converged"]]
-        out["%s_iterations_saved_on_frames_both_converge" % mode] = (
-            float(1 - np.sum([b for _, b in both]) / max(np.sum([a for a, _ in both]), 1)) if both else None)
-        out["%s_frames_both_converge" % mode] = len(both)
+    for tol in args.eval_tols:
+        common = dict(max_iterations=200, tolerance=tol, kernel=pdg.KERNEL_STREAM, patch_verts=128,
+                      block_threads=128)
+        arms = {"inertial": dict(params=None, init=pdg.INIT_INERTIAL, judge=0)}
+        for K in args.judge:
+            arms["learned_judge%d" % K] = dict(params=params, init=pdg.INIT_WARMSTART, judge=K)
+        res = {}
+        for name, arm in arms.items():
+            rows, vs, t = [], 0, 0.0
+            for b in range(nb):
+                r, v_, t_ = solve_frames(arm["params"], dict(common, init=arm["init"]), EVAL_SEED0 + b, args.batch,
+                                         args.eval_frames, args.n_range, judge=arm["judge"])
+                rows += r; vs += v_; t += t_
+            res[name] = rows
+            out.setdefault("tol_%g" % tol, {})[name] = dict(summarize(rows), vertex_steps_per_s_host_timed=vs / t)
+            log("tol %g %s %s" % (tol, name, json.dumps(out["tol_%g" % tol][name])))
+        for name in res:
+            if name == "inertial":
+                continue
+            both = [(a["iterations"], b["iterations"]) for a, b in zip(res["inertial"], res[name])
+                    if a["converged"] and b["converged"]]
+            out["tol_%g" % tol][name]["sweeps_saved_on_frames_both_converge"] = (
+                float(1 - sum(b for _, b in both) / max(sum(a for a, _ in both), 1)) if both else None)
+            out["tol_%g" % tol][name]["frames_both_converge"] = len(both)
     return out
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--trajectories", type=int, default=256)
+    ap.add_argument("--trajectories", type=int, default=2000)
     ap.add_argument("--frames", type=int, default=64)
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--smoothness", type=float, default=0.0,
                     help="weight of the neighbour-difference term of the training loss")
+    ap.add_argument("--energy-norm", action="store_true",
+                    help="weigh that term by the PD system's stiffness (energy norm of the error)")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--target-cap", type=int, default=400)
-    ap.add_argument("--target-tol", type=float, default=1e-6)
+    ap.add_argument("--target-cap", type=int, default=1000)
+    ap.add_argument("--target-tol", type=float, default=1e-7)
+    ap.add_argument("--traj-cap", type=int, default=200, help="sweep cap of the training trajectories' frames")
+    ap.add_argument("--traj-tol", type=float, default=1e-5, help="tolerance of the training trajectories' frames")
     ap.add_argument("--eval-seeds", type=int, default=128)
     ap.add_argument("--eval-frames", type=int, default=16)
-    ap.add_argument("--eval-tol", type=float, default=1e-5, help="relative residual the evaluation solves to")
+    ap.add_argument("--eval-tols", default="1e-2,1e-5", help="relative residuals the evaluation solves to")
+    ap.add_argument("--judge", default="0,4", help="judge sweep counts to evaluate")
     ap.add_argument("--n-min", type=int, default=17)
     ap.add_argument("--n-max", type=int, default=129)
+    ap.add_argument("--params", default="", help="evaluate these parameters instead of training")
     ap.add_argument("--out", default="")
     ap.add_argument("--json", default="")
     args = ap.parse_args()
     args.n_range = (args.n_min, args.n_max)
-    w, losses = train(args)
-    params = w.get_params()
-    if args.out:
-        np.save(args.out, params)
+    args.eval_tols = [float(x) for x in args.eval_tols.split(",") if x]
+    args.judge = [int(x) for x in args.judge.split(",") if x]
+    t0 = time.time()
+    losses = []
+    if args.params:
+        params = np.load(args.params).astype(np.float32)
+    else:
+        w, losses = train(args)
+        params = w.get_params()
+        if args.out:
+            np.save(args.out, params)
+    t_train = time.time() - t0
     held_out = score(params, args, frames=args.frames)
     zero = score(np.zeros_like(params), args, frames=args.frames)
-    print("held-out loss: trained %.4f, zero predictor (inertial start) %.4f" % (held_out, zero))
+    print("held-out loss: trained %.4f, zero parameters (previous offset) %.4f" % (held_out, zero))
     ev = evaluate(params, args)
-    result = dict(args={k: v for k, v in vars(args).items() if k != "n_range"}, train_loss=losses,
-                  held_out_loss=held_out, zero_predictor_loss=zero, eval=ev)
+    result = dict(args={k: v for k, v in vars(args).items() if k != "n_range"}, train_seconds=t_train,
+                  train_loss=losses, held_out_loss=held_out, zero_params_loss=zero, eval=ev)
     print(json.dumps(result))
     if args.json:
         json.dump(result, open(args.json, "w"), indent=1)

@@ -204,6 +204,16 @@ int  pdg_layout_check(int ncloths, const pdg_config* cfgs,
                       const pdg_mesh* const* meshes,
                       const pdg_constraints* const* cons, int patch_verts,
                       pdg_layout_info* info);
+/* The same check after planting one mistake in the built layout, so that a
+ * test can show the checker catches it: 1 two vertices' caller indices
+ * swapped, 2 a halo entry repeated, 3 a boundary vertex moved past the
+ * published prefix, 4 two records pointed at one contribution slot, 5 a
+ * cell dropped, 6 a halo entry out of range.  PDG_ERR_STATE with the
+ * violation when caught; PDG_ERR_ARG if the layout has no place for it. */
+int  pdg_layout_check_planted(int ncloths, const pdg_config* cfgs,
+                              const pdg_mesh* const* meshes,
+                              const pdg_constraints* const* cons, int patch_verts,
+                              int mistake, pdg_layout_info* info);
 int  pdg_solver_num_cloths(const pdg_solver* s, int* n);
 int  pdg_solver_cloth_counts(const pdg_solver* s, int cloth, int* N, int* T);
 /* PDSolver::step (src/pd_solver.cu:496-621): `nframes` frames.  stats: NULL
@@ -235,6 +245,9 @@ int  pdg_solver_get_state_all(pdg_solver* s, float* x, float* v, int on_device);
  * outputs undefined, like the solver state. */
 int  pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const float* v_in,
                           float* x_out, float* v_out, pdg_frame_stats* stats);
+/* Relative-residual target of one cloth (cloth = -1: every cloth), as
+ * pdg_config.tolerance at creation; 0 runs the sweep cap. */
+int  pdg_solver_set_tolerance(pdg_solver* s, int cloth, float tolerance);
 /* Move the pins of one cloth (Constraints::target_positions). */
 int  pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets);
 /* Inertial prediction y of the last frame and the residual r(x) of a given
@@ -287,37 +300,76 @@ void pdg_autotune_clear_cache(void);
 /* ---------------- learned warm start (no counterpart in the reference) ----
  * A 2-layer mesh message-passing network (hidden 64, bf16 weights and
  * activations, fp32 accumulation) predicts each vertex's offset x* - y of
- * the converged position from the inertial prediction.  Attached to a solver
- * whose cloths use cfg.init = PDG_INIT_WARMSTART, every frame evaluates the
- * prediction and the inertial start and keeps, per cloth, the one with the
- * lower residual (plain PD remains the fallback); PDG_INIT_WARMSTART_KEEP
- * always keeps the prediction.  Parameter layout: see
- * pdg_warmstart_get_params (We[64][10] be[64] {A[64][64] B[64][64] C[64][4]
- * c[64] U[64][128] u[64]} x 2 Wd[3][64] bd[3], fp32). */
+ * the converged position from the inertial prediction.  Node features (14):
+ * (y - x_n)/s, h v_n/s, pinned flag, log mass, log stretch k, log bend k, the
+ * previous frame's offset d_prev/s and its validity flag (s = 2.725e-3 m,
+ * one frame's gravity drop at h = 1/60).  The network's output is the change
+ * of the offset: the prediction is d_prev + s out (a skip connection kept in
+ * fp32).  d_prev is the offset x_n - y_(n-1) the solver kept at the end of
+ * its previous frame; it is valid for a vertex whose state entering the frame
+ * is bitwise the state the solver left (pdg_solver_set_state* and
+ * pdg_solver_step_host inputs that change a vertex invalidate it, as does
+ * attaching a network).  Edge features (4): log rest length and the current
+ * edge vector over the rest length.
+ *
+ * Attached to a solver whose cloths use cfg.init = PDG_INIT_WARMSTART,
+ * every frame judges the prediction against the inertial start and keeps,
+ * per cloth, the better one (plain PD remains both fallback and judge):
+ * with K = pdg_warmstart_set_judge_sweeps (default 4) > 0 both starts run K
+ * sweeps on their own iterates and the cloth continues from the one whose
+ * residual is lower (ties: the inertial start); with K = 0 the start
+ * residuals themselves are compared.  PDG_INIT_WARMSTART_KEEP always keeps
+ * the prediction.  Parameter layout: see pdg_warmstart_get_params
+ * (We[64][14] be[64] {A[64][64] B[64][64] C[64][4] c[64] U[64][128] u[64]}
+ * x 2 Wd[3][64] bd[3], fp32). */
 int  pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out);
 int  pdg_warmstart_param_count(const pdg_warmstart* w, int* n);
 int  pdg_warmstart_get_params(pdg_warmstart* w, float* host);
 int  pdg_warmstart_set_params(pdg_warmstart* w, const float* host);
-/* Forward + backward on a caller graph (host arrays): x N*10 node features,
+/* Forward + backward on a caller graph (host arrays): x N*14 node features,
  * symmetric CSR ptr (N+1) / adj, ef 4 features per directed edge, target
- * N*3, free weights N.  Returns out N*3, the MSE loss and the gradients
- * (param_count floats).  Not while attached to a solver. */
+ * N*3, free weights N, ew one weight per directed edge of the loss's edge
+ * term (NULL: 1).  Returns out N*3, the loss and the gradients (param_count
+ * floats).  Not while attached to a solver. */
 int  pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr, const int* adj,
-                        const float* ef, const float* target, const float* freew, float* out,
-                        float* loss, float* grads);
+                        const float* ef, const float* target, const float* freew, const float* ew,
+                        float* out, float* loss, float* grads);
 /* One Adam step (beta 0.9/0.999) with the gradients of the last eval/train. */
 int  pdg_warmstart_adam_step(pdg_warmstart* w, float lr);
 /* Bind to a solver (per-sweep kernels); its frames then use the prediction
  * for cloths with cfg.init == PDG_INIT_WARMSTART or _KEEP. */
 int  pdg_warmstart_attach(pdg_warmstart* w, pdg_solver* s);
 /* Training on data the solver generates: one frame of `s` from its current
- * state, then one Adam step (lr > 0) on (x_n, v_n, y) -> (x_{n+1} - y). */
+ * state, then one Adam step (lr > 0) on (x_n, v_n, y, d_prev) ->
+ * (x_{n+1} - y - d_prev). */
 int  pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* loss);
+/* Training on a trajectory of `traj` (the network attached to it) with the
+ * targets of a deeper solve: `deep` solves the same cloths with the same
+ * vertex layout (created from the same meshes, constraints and launch plan,
+ * with a larger cap or a lower tolerance).  One step copies traj's state
+ * into `deep`, runs one frame of `deep` (the target x*), one frame of `traj`
+ * (the trajectory and its kept offsets advance as in use), then one Adam
+ * step (lr > 0) on (x_n, v_n, y, d_prev of traj) -> (x* - y - d_prev). */
+int  pdg_warmstart_train_pair(pdg_warmstart* w, pdg_solver* traj, pdg_solver* deep, float lr, float* loss);
 /* Loss of training and evaluation: mean squared offset error plus lambda/2
- * times the squared error differences over the mesh's edges (default 0).
- * The second term weighs the high-frequency part of the error, which the
- * residual judge of the learned start amplifies. */
+ * times the weighted squared error differences over the mesh's edges
+ * (default 0).  The second term weighs the high-frequency part of the
+ * error, which the residual of a start amplifies. */
 int  pdg_warmstart_set_smoothness(pdg_warmstart* w, float lambda);
+/* Edge weights of that term when training on an attached solver: 0 (default)
+ * 1 per edge; 1 the energy norm e^T (M + K) e / m of the error, K the PD
+ * system's stiffness approximated by a graph Laplacian with K's diagonal
+ * (the Jacobi diagonal minus the mass). */
+int  pdg_warmstart_set_energy_norm(pdg_warmstart* w, int enable);
+/* Sweeps K each start runs before the judge (0..1000; default 4; at most
+ * the sweep cap is used). */
+int  pdg_warmstart_set_judge_sweeps(pdg_warmstart* w, int sweeps);
+int  pdg_warmstart_get_judge_sweeps(const pdg_warmstart* w, int* sweeps);
+/* Measurement helper: mean device time (CUDA events on the attached
+ * solver's stream) of the prediction for the solver's current state --
+ * features, network forward and start offsets -- over `reps` runs after one
+ * untimed run.  The solver's state is not changed. */
+int  pdg_warmstart_time_inference(pdg_warmstart* w, int reps, float* ms);
 void pdg_warmstart_destroy(pdg_warmstart* w);
 
 /* ---------------- allocation-free frame ----------------------------------
@@ -329,15 +381,21 @@ void pdg_warmstart_destroy(pdg_warmstart* w);
  * Inputs are the cloth in the reference's own device layout -- the arrays of
  * ClothMesh (pos, vel, mass, tris, Dm_inv, rest area), SimConstraints
  * (stretch k, Jacobi diagonal for cfg->dt, bend quads/w/n/k) and Constraints
- * (pin indices and targets); d_pos and d_vel are updated in place.  It
- * allocates nothing: its work arrays live in one static device array of about
- * 8.4 MB that every GPU loading the library keeps until exit, so N is limited
- * to PDG_NOALLOC_MAX_VERTS and the sweep count to PDG_NOALLOC_MAX_ITERS
- * (larger sizes return PDG_ERR_ARG).  The first call on a device looks up the
- * array's device address; make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU (other streams or host threads)
- * race.  Only PDG_MODE_CONSISTENT with PDG_INIT_INERTIAL.  stats: NULL or one
- * host struct (filling it synchronises the stream). */
+ * (pin indices and targets); d_pos and d_vel are updated in place.  Every
+ * vertex index (tris, quads, pins) must be < N, as in the reference's
+ * arrays; indices are not checked on the device.  It allocates nothing: its
+ * work arrays live in one static device array of about 8.4 MB that every GPU
+ * loading the library keeps until exit, so N is limited to
+ * PDG_NOALLOC_MAX_VERTS and the sweep count to PDG_NOALLOC_MAX_ITERS (larger
+ * sizes return PDG_ERR_ARG).  The first call on a device looks up the
+ * array's device address; make it before any stream capture.  The calling
+ * thread's current device must own `stream` (checked) and the arrays.  All
+ * calls share the array: calls that overlap on the GPU (other streams or host
+ * threads) race.  Only PDG_MODE_CONSISTENT with PDG_INIT_INERTIAL.  stats:
+ * NULL or one host struct (filling it synchronises the stream).  A frame
+ * whose solve produced NaN/Inf keeps x, zeroes v and re-applies the pins;
+ * it is reported only through stats->status (PDG_ERR_NUMERIC): the call
+ * itself returns PDG_OK, since without stats it does not wait for the GPU. */
 #define PDG_NOALLOC_MAX_VERTS 131072
 #define PDG_NOALLOC_MAX_ITERS 4096
 int  pdg_step_noalloc(const pdg_config* cfg, int N, float* d_pos, float* d_vel, const float* d_mass,

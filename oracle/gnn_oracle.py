@@ -4,16 +4,17 @@ The network has no counterpart in the reference; the tests compare the
 library's hand-written CUDA forward/backward/Adam kernels with this module.
 
 Network (hidden H = 64), on the mesh graph (both directions of every edge):
-    h0    = relu(We x + be)                          x: 10 node features
+    h0    = relu(We x + be)                          x: 14 node features
     for l = 1, 2:
       P, Q  = A_l h, B_l h
       m_ij  = relu(P_i + Q_j + C_l e_ij + c_l)         e_ij: 4 edge features
       a_i   = mean_{j in N(i)} m_ij
       h     = h + relu(U_l [h; a] + u_l)
-    out   = Wd h + bd                                 3 outputs (offset / scale)
-Loss: mean over free vertices and the 3 components of (out - target)^2.
+    out   = Wd h + bd                                 3 outputs (offset change / scale)
+Loss: mean over free vertices and the 3 components of (out - target)^2, plus
+an optional weighted edge term (loss_and_grad).
 Parameter shapes follow the library's layout (pdg_warmstart_get_params):
-    We (64, 10), be (64), then per layer A (64, 64), B (64, 64), C (64, 4),
+    We (64, 14), be (64), then per layer A (64, 64), B (64, 64), C (64, 4),
     c (64), U (64, 128), u (64), then Wd (3, 64), bd (3).
 """
 from __future__ import annotations
@@ -21,7 +22,7 @@ from __future__ import annotations
 import numpy as np
 
 H = 64
-NF = 10
+NF = 14
 EF = 4
 NO = 3
 
@@ -76,14 +77,16 @@ def forward(p, x, e, src, dst, deg):
     return out, cache
 
 
-def loss_and_grad(p, x, e, src, dst, deg, target, free, lam=0.0):
-    """Loss = [sum_i |d_i|^2 + lam/2 sum_(a->b) w_a w_b |d_a - d_b|^2] / cnt with
-    d = (out - target) * free over the directed edges (both directions of
-    every mesh edge), and its gradient with respect to every parameter."""
+def loss_and_grad(p, x, e, src, dst, deg, target, free, lam=0.0, ew=None):
+    """Loss = [sum_i |d_i|^2 + lam/2 sum_(a->b) k_ab w_a w_b |d_a - d_b|^2] / cnt
+    with d = (out - target) * free over the directed edges (both directions
+    of every mesh edge), edge weights k (ew, one per directed edge; None: 1),
+    and its gradient with respect to every parameter."""
     out, c = forward(p, x, e, src, dst, deg)
     cnt = max(int(free.sum()) * NO, 1)
     diff = (out - target) * free[:, None]
-    wab = (free[src] * free[dst])[:, None]
+    kab = np.ones(len(src)) if ew is None else np.asarray(ew, np.float64)
+    wab = (free[src] * free[dst] * kab)[:, None]
     de = (diff[src] - diff[dst]) * wab
     loss = float(((diff ** 2).sum() + 0.5 * lam * ((diff[src] - diff[dst]) ** 2 * wab).sum()) / cnt)
     g = {n: np.zeros(s) for n, s in shapes()}

@@ -32,22 +32,27 @@ def problem(seed=0, n=30):
     return G, p, x, e, src, dst, deg, target, free, ptr, adj
 
 
-@pytest.mark.parametrize("lam", [0.0, 0.5])
-def test_forward_backward_match_oracle(pdg, lam):
+@pytest.mark.parametrize("lam,weighted", [(0.0, False), (0.5, False), (0.5, True)])
+def test_forward_backward_match_oracle(pdg, lam, weighted):
     G, p, x, e, src, dst, deg, target, free, ptr, adj = problem(0)
     flat = G.flatten(p).astype(np.float32)
     w = pdg.WarmStart(seed=1).set_smoothness(lam)
     assert w.count == G.count()
     w.set_params(flat)
     assert np.array_equal(w.get_params(), flat)
-    out, loss, grads = w.eval(x, ptr, adj, e, target, free)
+    ew = None
+    if weighted:   # symmetric edge weights, as the energy-norm term's
+        a = np.random.default_rng(4).uniform(0.5, 3.0, len(deg))
+        ew = (0.5 * (a[src] + a[dst])).astype(np.float32)
+    out, loss, grads = w.eval(x, ptr, adj, e, target, free, ew)
     # the oracle on the GPU's bf16-rounded inputs and GEMM weights
     pb = dict(G.unflatten(flat))
     for k in pb:
         if k[0] in "WABU":
             pb[k] = bf16_round(pb[k]).astype(np.float64)
     lo, go, oo = G.loss_and_grad(pb, bf16_round(x).astype(np.float64), e.astype(np.float64), src, dst, deg,
-                                 target.astype(np.float64), free.astype(np.float64), lam)
+                                 target.astype(np.float64), free.astype(np.float64), lam,
+                                 None if ew is None else ew.astype(np.float64))
     assert abs(loss - lo) <= 2e-2 * lo
     assert np.linalg.norm(out - oo) <= 2e-2 * np.linalg.norm(oo)
     gg = G.unflatten(grads)
@@ -77,14 +82,13 @@ def test_adam_step_matches_oracle(pdg):
         cur = got
 
 
-def test_training_on_solver_data_beats_inertial_start_and_never_hurts(pdg):
+def test_training_on_solver_data_beats_previous_offset_and_never_hurts(pdg):
     import scenes
     w = pdg.WarmStart(seed=0)
     # fresh trajectories of cloths from the batched distribution; training
     # is not bit-reproducible (the blocks add their weight-gradient partial
-    # sums with float atomics), so it
-    # runs long enough to clear the bar by a wide margin (measured: held-out
-    # ratio 0.88-0.91 after 10 batches, 0.50-0.52 after 20)
+    # sums with float atomics), so it runs long enough to clear the bar by a
+    # wide margin
     for b in range(20):
         ms, cs, cfgs, _ = scenes.batch(16, seed=100 + b, max_iterations=300, tolerance=1e-6, n_range=(17, 33),
                                        kernel=pdg.KERNEL_GRAPH)
@@ -94,9 +98,10 @@ def test_training_on_solver_data_beats_inertial_start_and_never_hurts(pdg):
             w.train_frame(s, 1e-3)
         s.close()
     params = w.get_params()
-    # held-out trajectories scored (lr = 0): the trained network against the
-    # zero predictor, i.e. the inertial start (the solver's frames do not
-    # depend on the network)
+    # held-out trajectories scored (lr = 0): the trained network against zero
+    # parameters, which predict the previous frame's offset (the inertial
+    # start on a trajectory's first frame); the solver's frames do not
+    # depend on the network
     ms3, cs3, cfgs3, _ = scenes.batch(16, seed=7, max_iterations=300, tolerance=1e-6, n_range=(17, 33),
                                       kernel=pdg.KERNEL_GRAPH)
     scores = []
@@ -107,12 +112,14 @@ def test_training_on_solver_data_beats_inertial_start_and_never_hurts(pdg):
         w3.attach(s3)
         scores.append(np.mean([w3.train_frame(s3, 0.0) for _ in range(24)]))
     assert scores[1] < 0.85 * scores[0], scores
-    # held-out cloths: the learned start is kept only where it lowers the start residual
+    # held-out cloths, judge on the start residuals (K = 0): the learned start
+    # is kept only where it lowers the start residual
     ms2, cs2, cfgs2, _ = scenes.batch(6, seed=99, max_iterations=40, tolerance=0.0, n_range=(17, 25),
                                       kernel=pdg.KERNEL_GRAPH, init=pdg.INIT_WARMSTART)
     eval_s = pdg.Solver(cfgs2, ms2, cs2)
     w2 = pdg.WarmStart(seed=0)
     w2.set_params(params)
+    w2.set_judge_sweeps(0)
     w2.attach(eval_s)
     for _ in range(5):
         st = eval_s.step(1)
@@ -158,3 +165,82 @@ def test_learned_start_on_the_streaming_kernel_matches_graph(pdg, init_name):
     (xb, vb), ub = outs[1]
     assert np.array_equal(xa, xb) and np.array_equal(va, vb)
     assert ua == ub
+
+
+def _batch_solver(pdg, init, kern, seed=31, count=6, cap=24, tol=0.0):
+    import scenes
+    ms, cs, cfgs, _ = scenes.batch(count, seed=seed, max_iterations=cap, tolerance=tol, n_range=(17, 41),
+                                   kernel=kern, init=init, patch_verts=128, block_threads=128)
+    return pdg.Solver(cfgs, ms, cs)
+
+
+@pytest.mark.parametrize("kern_name", ["KERNEL_GRAPH", "KERNEL_STREAM"])
+def test_judge_after_k_sweeps_continues_one_chain_bitwise(pdg, kern_name):
+    # Zero parameters predict "no change of the offset": the prediction is
+    # the previous frame's offset (none valid on the first frame, so every
+    # start equals the inertial one).  On the second frame the judge runs K
+    # sweeps from both starts and each cloth continues from one of them:
+    # its result is bitwise the plain solve's or the always-kept solve's.
+    kern = getattr(pdg, kern_name)
+    K = 4
+    runs = {}
+    for name, init in (("inertial", pdg.INIT_INERTIAL), ("judged", pdg.INIT_WARMSTART),
+                       ("kept", pdg.INIT_WARMSTART_KEEP)):
+        s = _batch_solver(pdg, init, kern)
+        w = pdg.WarmStart(seed=0)
+        w.set_params(np.zeros(w.count, np.float32))
+        w.set_judge_sweeps(K)
+        assert w.judge_sweeps == K
+        w.attach(s)
+        st1 = s.step(1)
+        x1 = s.get_state_all()
+        st2 = s.step(1)
+        runs[name] = (st1, x1, st2, [s.get_state(c) for c in range(s.n)])
+        s.close()
+    for name in ("judged", "kept"):   # first frame: no previous offset, one start
+        assert all(np.array_equal(a, b) for a, b in zip(runs[name][1], runs["inertial"][1])), name
+    used = [x["warm_start_used"] for x in runs["judged"][2]]
+    assert 0 < sum(used) < len(used), used   # both outcomes occur on this batch
+    for c, u in enumerate(used):
+        ref = runs["kept" if u else "inertial"]
+        xj, vj = runs["judged"][3][c]
+        xr, vr = ref[3][c]
+        assert np.array_equal(xj, xr) and np.array_equal(vj, vr), (c, u)
+        assert runs["judged"][2][c]["iterations"] == ref[2][c]["iterations"]
+        # the normaliser is the inertial start's residual in every arm
+        assert np.isclose(runs["judged"][2][c]["res_inertial"], runs["inertial"][2][c]["res_inertial"], rtol=1e-9)
+
+
+def test_previous_offset_is_kept_across_an_unchanged_state_and_dropped_when_it_changes(pdg):
+    # KEEP mode starts every frame from the prediction d_prev + s out, so the
+    # result depends on the kept previous offsets.  Writing back the solver's
+    # own state keeps them; writing a changed state drops them, exactly like
+    # re-attaching the network (which clears them).
+    def run(after):
+        s = _batch_solver(pdg, pdg.INIT_WARMSTART_KEEP, pdg.KERNEL_STREAM, seed=51, count=4)
+        w = pdg.WarmStart(seed=0)
+        w.set_params(np.zeros(w.count, np.float32))
+        w.attach(s)
+        s.step(2)
+        x, v = s.get_state_all()
+        if after == "same":
+            s.set_state_all(x, v)
+        elif after == "moved":
+            s.set_state_all(x + 1e-3, v)
+        elif after == "moved_reattached":
+            s.set_state_all(x + 1e-3, v)
+            w.attach(s)
+        elif after == "reattached":
+            w.attach(s)
+        s.step(1)
+        r = s.get_state_all()
+        s.close()
+        return r
+    base = run("none")
+    same = run("same")
+    assert all(np.array_equal(a, b) for a, b in zip(base, same))
+    reatt = run("reattached")
+    assert not all(np.array_equal(a, b) for a, b in zip(base, reatt))
+    moved = run("moved")
+    moved_reatt = run("moved_reattached")
+    assert all(np.array_equal(a, b) for a, b in zip(moved, moved_reatt))

@@ -38,10 +38,15 @@ def random_problem(seed=0, n=5):
     return G, p, x, e, src, dst, deg, target, free, ptr, adj
 
 
-@pytest.mark.parametrize("lam", [0.0, 0.7])
-def test_oracle_gradients_match_finite_differences(lam):
+@pytest.mark.parametrize("lam,weighted", [(0.0, False), (0.7, False), (0.7, True)])
+def test_oracle_gradients_match_finite_differences(lam, weighted):
     G, p, x, e, src, dst, deg, target, free, _, _ = random_problem(0)
-    loss, g, _ = G.loss_and_grad(p, x, e, src, dst, deg, target, free, lam)
+    # symmetric positive edge weights (the energy-norm term's form)
+    ew = None
+    if weighted:
+        a = np.random.default_rng(5).uniform(0.5, 3.0, len(deg))
+        ew = 0.5 * (a[src] + a[dst])
+    loss, g, _ = G.loss_and_grad(p, x, e, src, dst, deg, target, free, lam, ew)
     flat = G.flatten(p)
     gflat = G.flatten(g)
     rng = np.random.default_rng(1)
@@ -50,8 +55,8 @@ def test_oracle_gradients_match_finite_differences(lam):
     for k in idx:
         fp = flat.copy(); fp[k] += eps
         fm = flat.copy(); fm[k] -= eps
-        lp = G.loss_and_grad(G.unflatten(fp), x, e, src, dst, deg, target, free, lam)[0]
-        lm = G.loss_and_grad(G.unflatten(fm), x, e, src, dst, deg, target, free, lam)[0]
+        lp = G.loss_and_grad(G.unflatten(fp), x, e, src, dst, deg, target, free, lam, ew)[0]
+        lm = G.loss_and_grad(G.unflatten(fm), x, e, src, dst, deg, target, free, lam, ew)[0]
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - gflat[k]) <= 1e-6 + 1e-4 * abs(fd), (k, fd, gflat[k])
 
