@@ -708,10 +708,19 @@ std::string check_layout(const std::vector<ClothSetup>& cl, const HostLayout& L)
         }
         if (next != ntot) return fail("patches own %d of %d vertices", next, ntot);
     }
-    // vertices that some patch reads as a halo vertex
+    // vertices that some patch reads as a halo vertex (each entry range-checked
+    // before it is used as an index)
     std::vector<char> in_halo(ntot, 0);
-    for (const PatchHdr& h : L.patches)
-        for (int q = 0; q < h.nlocal - h.nown; ++q) in_halo[L.halo[h.halo_off + q]] = 1;
+    for (int p = 0; p < L.npatch; ++p) {
+        const PatchHdr& h = L.patches[p];
+        if (h.halo_off < 0 || h.nlocal < h.nown || (size_t)h.halo_off + (size_t)(h.nlocal - h.nown) > L.halo.size())
+            return fail("patch %d: halo list outside the halo array", p);
+        for (int q = 0; q < h.nlocal - h.nown; ++q) {
+            const int g = L.halo[h.halo_off + q];
+            if (g < 0 || g >= ntot) return fail("patch %d: halo entry %d out of range (%d)", p, q, g);
+            in_halo[g] = 1;
+        }
+    }
 
     std::vector<int> stamp(ntot, -1), nslot_of;
     std::vector<char> slot_seen;

@@ -122,3 +122,34 @@ def test_bad_arguments(pdg):
     with pytest.raises(pdg.PDGError) as e:
         pdg.layout_check(pdg.Config.default(), [m, m2], [c2, c], 32)   # constraints of another mesh
     assert e.value.code == pdg.ERR_ARG
+
+
+# Each planted mistake and the checker's finding (pdg_layout_check_planted
+# builds the layout, plants one mistake, then runs the same check).
+PLANTED = {
+    1: "cloth or caller index out of place",
+    2: "is foreign, owned or repeated",
+    3: "is read by another patch but not among the first",
+    4: "written twice",
+    5: "contributions written",
+    6: "out of range",
+}
+
+
+@pytest.mark.parametrize("mistake", sorted(PLANTED))
+@pytest.mark.parametrize("mtype", [1, 3])
+def test_checker_catches_each_planted_mistake(pdg, mistake, mtype):
+    m, c = cloth(pdg, 33, mtype=mtype)
+    cfg = pdg.Config.default()
+    pdg.layout_check(cfg, m, c, 128)   # the built layout itself passes
+    with pytest.raises(pdg.PDGError) as e:
+        pdg.layout_check_planted(cfg, m, c, 128, mistake)
+    assert e.value.code == pdg.ERR_STATE, str(e.value)
+    assert PLANTED[mistake] in str(e.value), str(e.value)
+
+
+def test_planted_mistake_out_of_range_is_an_argument_error(pdg):
+    m, c = cloth(pdg, 17)
+    with pytest.raises(pdg.PDGError) as e:
+        pdg.layout_check_planted(pdg.Config.default(), m, c, 128, 7)
+    assert e.value.code == pdg.ERR_ARG
