@@ -289,6 +289,13 @@ extern "C" int pdg_step_noalloc(const pdg_config* cfg, int N, float* d_pos, floa
 
     int dev = 0;
     NA_CK(cudaGetDevice(&dev));
+    if (stream) {   // the scratch address is this device's: the stream must belong to it
+        int sdev = -1;
+        NA_CK(cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev));
+        if (sdev != dev)
+            return set_error(PDG_ERR_ARG, "pdg_step_noalloc: the stream belongs to device %d, the current device is %d",
+                             sdev, dev);
+    }
     unsigned char* base = nullptr;
     const int rc = scratch_of(dev, &base);
     if (rc) return rc;
