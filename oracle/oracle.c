@@ -392,6 +392,11 @@ void orc_step_literal_f32(const orc_problem* p, const float* diag, int iters,
 }
 
 /* ---------------- precision-generic solvers ---------------- */
+/* size of the last LDL^T factor the direct solve built (strictly lower
+ * entries of L), for the CPU-baseline report */
+static long long orc_last_nnz_L = 0;
+long long orc_last_factor_nnz(void) { return orc_last_nnz_L; }
+
 #define REAL double
 #define SFX(name) name##_f64
 #define RSQRT(a) sqrt(a)

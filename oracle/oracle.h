@@ -108,6 +108,9 @@ int  orc_step_direct_f64(const orc_problem* p, int iters, int pin_elim,
                          int with_bend, double* x, double* v);
 int  orc_step_direct_f32(const orc_problem* p, int iters, int pin_elim,
                          int with_bend, float* x, float* v);
+/* Strictly lower entries of the last LDL^T factor the direct solve built
+ * (3N x 3N, minimum-degree order). */
+long long orc_last_factor_nnz(void);
 /* Solve K z = b for the frame's global matrix (for the scipy cross-check). */
 int  orc_global_matrix_f64(const orc_problem* p, int pin_elim, int with_bend,
                            int* nnz, int* ri, int* ci, double* val);

@@ -211,6 +211,13 @@ class Scene:
             raise RuntimeError("LDL^T factorisation failed")
         return x, v
 
+    @staticmethod
+    def last_factor_nnz():
+        """Strictly lower entries of the last LDL^T factor step_direct built."""
+        f = lib().orc_last_factor_nnz
+        f.restype = C.c_longlong
+        return int(f())
+
     def global_matrix(self, with_bend=False):
         pr = self.problem()
         nnz = C.c_int()
