@@ -51,12 +51,11 @@ def shard(sizes, rank, world):
     return [i for i in range(len(sizes)) if owner[i] == rank]
 
 
-def batch(count, seed=0, *, max_iterations=200, tolerance=1e-5, rho=0.99, n_range=(17, 129),
-          size_range=(0.5, 2.0), **cfg_kw):
-    """(meshes, constraints, configs, params) of `count` cloths drawn from
-    the batched-workload distribution."""
+def batch_params(count, seed=0, *, n_range=(17, 129), size_range=(0.5, 2.0)):
+    """Per-cloth parameters of `count` cloths drawn from the batched-workload
+    distribution (numpy only; batch() builds the meshes from them)."""
     rng = np.random.default_rng(seed)
-    meshes, cons, cfgs, params = [], [], [], []
+    out = []
     for i in range(count):
         n = int(rng.integers(n_range[0], n_range[1] + 1))
         size = float(rng.uniform(*size_range))
@@ -65,10 +64,22 @@ def batch(count, seed=0, *, max_iterations=200, tolerance=1e-5, rho=0.99, n_rang
         wind = rng.normal(0.0, 2.0, 3).astype(np.float32)
         npins = int(rng.integers(1, 5))
         pins = rng.choice(boundary_vertices(n), size=npins, replace=False).astype(np.int32)
-        m = pdg.Mesh.hanging(n, size, mtype=1, jitter=1e-4, seed=int(rng.integers(1 << 31)))
-        c = pdg.Constraints(m).build_stretch(ks).build_bend(kb).set_pins(pins)
+        mesh_seed = int(rng.integers(1 << 31))
+        out.append(dict(n=n, size=size, ks=ks, kb=kb, wind=wind.tolist(), pins=pins.tolist(), mesh_seed=mesh_seed))
+    return out
+
+
+def batch(count, seed=0, *, max_iterations=200, tolerance=1e-5, rho=0.99, n_range=(17, 129),
+          size_range=(0.5, 2.0), **cfg_kw):
+    """(meshes, constraints, configs, params) of `count` cloths drawn from
+    the batched-workload distribution."""
+    meshes, cons, cfgs = [], [], []
+    params = batch_params(count, seed, n_range=n_range, size_range=size_range)
+    for p in params:
+        n = p["n"]
+        m = pdg.Mesh.hanging(n, p["size"], mtype=1, jitter=1e-4, seed=p["mesh_seed"])
+        c = pdg.Constraints(m).build_stretch(p["ks"]).build_bend(p["kb"]).set_pins(np.array(p["pins"], np.int32))
         cfg = pdg.Config.default(max_iterations=max_iterations, tolerance=tolerance, rho=rho, dt=H, gravity=G,
-                                 wind=tuple(float(w) for w in wind), **cfg_kw)
+                                 wind=tuple(float(w) for w in p["wind"]), **cfg_kw)
         meshes.append(m); cons.append(c); cfgs.append(cfg)
-        params.append(dict(n=n, size=size, ks=ks, kb=kb, wind=wind.tolist(), pins=pins.tolist()))
     return meshes, cons, cfgs, params

@@ -1,0 +1,123 @@
+"""The benchmark workloads' physics held to the float64 oracle (GPU).
+
+The batched workload draws per cloth a grid side n, a size, 1-4 random
+boundary pins, stretch k up to 1e4, bend k and a constant wind N(0, 2 m/s^2)
+per axis; the large workload is a 1025x1025 cloth with stretch k 1e4 and wind.
+Here a small batch from the same distribution (n in 17..65) is solved on the
+streaming and the resident kernel and every cloth is compared with the
+oracle's float64 Jacobi-Chebyshev run of the same sweeps: one frame within
+1e-5 relative in positions, 20 frames within 1e-4, and in tolerance mode the
+sweep count within 2 of the oracle's.  One frame of the real 1025x1025
+workload (a few sweeps) is held to 1e-5 as well.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_ONE_FRAME = 1e-5
+REL_F64 = 1e-4
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64).reshape(-1); b = np.asarray(b, np.float64).reshape(-1)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+def oracle_scene(oracle, m, c, cfg):
+    a = m.arrays(); ca = c.arrays()
+    kb = float(ca["bend_k"][0]) if len(ca["bend_k"]) else 0.0
+    sc = oracle.Scene(a["rest"], a["tris"], k_stretch=ca["k_stretch"], k_bend=kb, pins=ca["pins"], h=cfg.dt,
+                      gravity=cfg.gravity, wind=tuple(cfg.wind), damping=cfg.damping)
+    return sc, a
+
+
+def small_batch(pdg, kern, cap, tol=0.0, seed=2024, count=8):
+    import scenes
+    ms, cs, cfgs, params = scenes.batch(count, seed=seed, max_iterations=cap, tolerance=tol, n_range=(17, 65),
+                                        kernel=kern)
+    return ms, cs, cfgs, params
+
+
+def test_small_batch_draws_the_workload_physics(pdg):
+    _, _, _, params = small_batch(pdg, pdg.KERNEL_STREAM, 10)
+    assert max(p["ks"] for p in params) > 1e3                 # stiff cloths in the draw
+    assert any(len(p["pins"]) > 2 for p in params)              # more than two pins
+    assert any(abs(w) > 1.0 for p in params for w in p["wind"])  # wind of the N(0, 2) scale
+
+
+@pytest.mark.parametrize("kern_name", ["KERNEL_STREAM", "KERNEL_RESIDENT"])
+def test_batch_one_frame_every_cloth_matches_f64(pdg, oracle, kern_name):
+    kern = getattr(pdg, kern_name)
+    ms, cs, cfgs, _ = small_batch(pdg, kern, 10)
+    s = pdg.Solver(cfgs, ms, cs)
+    assert s.launch_info()["kernel"] == kern
+    st = s.step(1)
+    for i, (m, c, cfg) in enumerate(zip(ms, cs, cfgs)):
+        sc, a = oracle_scene(oracle, m, c, cfg)
+        x0 = a["rest"].astype(np.float64).reshape(-1)
+        xo, vo, info = sc.step_jacobi(x0, np.zeros_like(x0), 10, rho=cfg.rho)
+        x, v = s.get_state(i)
+        assert st[i]["status"] == 0 and st[i]["iterations"] == 10
+        assert rel(x, xo) < REL_ONE_FRAME, (i, rel(x, xo))
+        assert rel(v, vo) < 1e-3, (i, rel(v, vo))
+        assert abs(st[i]["res_inertial"] - info["res_y"]) <= 1e-3 * info["res_y"]
+
+
+@pytest.mark.parametrize("kern_name", ["KERNEL_STREAM", "KERNEL_RESIDENT"])
+def test_batch_twenty_frames_every_cloth_within_1e4_of_f64(pdg, oracle, kern_name):
+    kern = getattr(pdg, kern_name)
+    ms, cs, cfgs, _ = small_batch(pdg, kern, 32)
+    s = pdg.Solver(cfgs, ms, cs)
+    s.step(20, stats=False)
+    for i, (m, c, cfg) in enumerate(zip(ms, cs, cfgs)):
+        sc, a = oracle_scene(oracle, m, c, cfg)
+        x = a["rest"].astype(np.float64).reshape(-1); v = np.zeros_like(x)
+        for _ in range(20):
+            x, v, _ = sc.step_jacobi(x, v, 32, rho=cfg.rho)
+        xg, vg = s.get_state(i)
+        assert rel(xg, x) < REL_F64, (i, rel(xg, x))
+        assert rel(vg, v) < 1e-2, (i, rel(vg, v))
+
+
+@pytest.mark.parametrize("kern_name", ["KERNEL_STREAM", "KERNEL_RESIDENT"])
+def test_batch_tolerance_mode_sweeps_match_f64(pdg, oracle, kern_name):
+    # a tolerance every cloth of the draw reaches well within the cap, so the
+    # per-cloth stopping sweep is compared (float32 residuals near the
+    # threshold may stop a sweep or two apart)
+    kern = getattr(pdg, kern_name)
+    tol, cap = 3e-2, 400
+    ms, cs, cfgs, _ = small_batch(pdg, kern, cap, tol=tol)
+    s = pdg.Solver(cfgs, ms, cs)
+    st = s.step(1)
+    for i, (m, c, cfg) in enumerate(zip(ms, cs, cfgs)):
+        sc, a = oracle_scene(oracle, m, c, cfg)
+        x0 = a["rest"].astype(np.float64).reshape(-1)
+        xo, vo, info = sc.step_jacobi(x0, np.zeros_like(x0), cap, tol=tol, rho=cfg.rho)
+        assert info["used"] < cap
+        assert st[i]["converged"] == 1 and st[i]["rel_residual"] <= tol
+        assert abs(st[i]["iterations"] - info["used"]) <= 2, (i, st[i]["iterations"], info["used"])
+        x, _ = s.get_state(i)
+        assert rel(x, xo) < REL_ONE_FRAME
+
+
+def test_large_1025_cloth_one_frame_matches_f64(pdg, oracle):
+    # the large workload itself: 1,050,625 vertices, stretch k 1e4, bend k
+    # 1e-2, wind N(0, 1) per axis (seed 0), two top corners pinned; a few
+    # sweeps of its first frame against the float64 oracle
+    import scenes
+    n, sweeps = 1025, 4
+    m, c = scenes.hanging(n, 4.0, ks=1e4, kb=1e-2, seed=0)
+    wind = tuple(float(w) for w in np.random.default_rng(0).normal(0.0, 1.0, 3))
+    cfg = pdg.Config.default(max_iterations=sweeps, tolerance=0.0, rho=0.99, dt=scenes.H, gravity=scenes.G,
+                             wind=wind, kernel=pdg.KERNEL_STREAM)
+    s = pdg.Solver(cfg, m, c)
+    st = s.step(1)[0]
+    x, v = s.get_state()
+    sc, a = oracle_scene(oracle, m, c, cfg)
+    x0 = a["rest"].astype(np.float64).reshape(-1)
+    xo, vo, info = sc.step_jacobi(x0, np.zeros_like(x0), sweeps, rho=0.99)
+    assert st["status"] == 0 and st["iterations"] == sweeps
+    assert rel(x, xo) < REL_ONE_FRAME, rel(x, xo)
+    assert rel(v, vo) < 1e-3, rel(v, vo)
+    assert abs(st["res_inertial"] - info["res_y"]) <= 1e-3 * info["res_y"]
