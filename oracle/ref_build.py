@@ -2,11 +2,18 @@
 
 The reference GPU path (src/pd_solver.cu) compiles with nvcc without Eigen,
 because its Eigen-dependent members sit behind #ifndef __CUDACC__.  Where the
-reference sources are present (this container; not the GPU machine), this
-recipe compiles that file, as it lies under /root/reference, into a device
-image for sm_103a:
+reference sources are present (not on the GPU machine), this recipe compiles
+that file, as it lies in the reference tree, into a device image for sm_103a:
 
     oracle/_ref/pd_solver_ref.cubin
+
+The reference tree is the directory named by the environment variable
+CLOTH_CUDA_REFERENCE, or the first command-line argument:
+
+    CLOTH_CUDA_REFERENCE=/path/to/cloth-cuda python oracle/ref_build.py
+    python oracle/ref_build.py /path/to/cloth-cuda
+
+(default when neither is given: /root/reference).
 
 Only its kernels are used; its host code (PDSolver) is never compiled or run.
 The image is git-ignored and travels to the GPU machine with the rest of the
@@ -23,7 +30,14 @@ import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+DEFAULT_REF_ROOT = "/root/reference"
+
+
+def ref_root() -> str:
+    """The reference tree: CLOTH_CUDA_REFERENCE, else the default."""
+    return os.environ.get("CLOTH_CUDA_REFERENCE") or DEFAULT_REF_ROOT
+
+
 OUT_DIR = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(OUT_DIR, "pd_solver_ref.cubin")
 HARNESS_SRC = os.path.join(HERE, "ref_harness.c")
@@ -38,8 +52,9 @@ def _cuda_home():
     return os.path.dirname(os.path.dirname(os.path.realpath(nvcc))) if nvcc else None
 
 
-def build_cubin() -> bool:
-    src = os.path.join(REF_ROOT, "src", "pd_solver.cu")
+def build_cubin(root: str | None = None) -> bool:
+    root = root or ref_root()
+    src = os.path.join(root, "src", "pd_solver.cu")
     if not os.path.exists(src):
         return os.path.exists(CUBIN)
     if os.path.exists(CUBIN) and os.path.getmtime(CUBIN) >= os.path.getmtime(src):
@@ -48,7 +63,7 @@ def build_cubin() -> bool:
     ch = _cuda_home()
     nvcc = os.path.join(ch, "bin", "nvcc") if ch else "nvcc"
     subprocess.check_call([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
-                           "-I" + os.path.join(REF_ROOT, "include"), "-I" + os.path.join(REF_ROOT, "src"),
+                           "-I" + os.path.join(root, "include"), "-I" + os.path.join(root, "src"),
                            src, "-o", CUBIN])
     return True
 
@@ -80,4 +95,5 @@ def build_if_available() -> None:
 
 
 if __name__ == "__main__":
-    print("cubin", build_cubin(), "harness", build_harness())
+    import sys
+    print("cubin", build_cubin(sys.argv[1] if len(sys.argv) > 1 else None), "harness", build_harness())
