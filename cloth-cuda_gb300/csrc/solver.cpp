@@ -814,6 +814,48 @@ int pdg_solver_set_tolerance(pdg_solver* s, int cloth, float tolerance)
     return PDG_OK;
 }
 
+int pdg_solver_set_pins(pdg_solver* s, int cloth, const int* idx, int P, const float* targets)
+{
+    int vb = 0, n = 0;
+    int rc = cloth_range(s, cloth, &vb, &n);
+    if (rc) return rc;
+    if (P < 0 || (P > 0 && !idx)) return set_error(PDG_ERR_ARG, "pdg_solver_set_pins: bad pin list");
+    ClothSetup& c = s->cloths[cloth];
+    const int N = c.mesh->N;
+    std::vector<char> seen(N, 0);
+    for (int q = 0; q < P; ++q) {
+        if (idx[q] < 0 || idx[q] >= N) return set_error(PDG_ERR_ARG, "pdg_solver_set_pins: pin %d out of range", idx[q]);
+        if (seen[idx[q]]++) return set_error(PDG_ERR_ARG, "pdg_solver_set_pins: pin %d repeated", idx[q]);
+        if (targets && (!std::isfinite(targets[3 * q]) || !std::isfinite(targets[3 * q + 1]) ||
+                        !std::isfinite(targets[3 * q + 2])))
+            return set_error(PDG_ERR_ARG, "pdg_solver_set_pins: non-finite target");
+    }
+    c.cons.pins.assign(idx, idx + P);
+    c.cons.targets.resize(3 * (size_t)P);
+    for (int q = 0; q < P; ++q)
+        for (int d = 0; d < 3; ++d)
+            c.cons.targets[3 * q + d] = targets ? targets[3 * q + d] : c.mesh->rest[3 * (size_t)idx[q] + d];
+    // a vertex's record: its target with w = -1 when pinned, else its
+    // inverse Jacobi diagonal (as the layout builds it)
+    std::vector<float> diag;
+    jacobi_diag(*c.mesh, c.cons, c.cfg.dt, diag);
+    std::vector<int> slot(N, -1);
+    for (int q = 0; q < P; ++q) slot[idx[q]] = q;
+    for (int g = vb; g < vb + n; ++g) {
+        const int o = s->L.perm_local[g];
+        float4& a = s->L.aux[g];
+        if (slot[o] >= 0) {
+            const int q = slot[o];
+            a = make_float4(c.cons.targets[3 * q], c.cons.targets[3 * q + 1], c.cons.targets[3 * q + 2], -1.f);
+        } else {
+            a = make_float4(0.f, 0.f, 0.f, diag[o] > 1e-10f ? 1.0f / diag[o] : 0.f);
+        }
+    }
+    CK(cudaMemcpyAsync(s->aux.p + vb, s->L.aux.data() + vb, sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return PDG_OK;
+}
+
 int pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets)
 {
     int vb = 0, n = 0;

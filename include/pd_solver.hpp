@@ -185,11 +185,24 @@ public:
     PDSolver& operator=(const PDSolver&) = delete;
     ~PDSolver() { if (s_) pdg_solver_destroy(s_); }
 
-    // PDSolver::step (src/pd_solver.cu:496-621).  The first call (or a change
-    // of the pin list) builds the GPU solver; the cloth starts at rest.
+    // PDSolver::step (src/pd_solver.cu:496-621).  The first call builds the
+    // GPU solver (the cloth starts at rest); later calls pass a changed pin
+    // list or changed pin targets on to it, as the reference's
+    // Constraints::upload_to_gpu re-uploads them (src/constraints.cpp:77-101).
     void step(ClothMesh& mesh, SimConstraints& sim, const Constraints& pins)
     {
-        if (!s_ || pins.pinned_indices != pins_) build(mesh, sim, pins);
+        if (!s_) {
+            build(mesh, sim, pins);
+        } else {
+            std::vector<float> tgt = targets_of(pins);
+            if (pins.pinned_indices != pins_)
+                check(pdg_solver_set_pins(s_, 0, pins.pinned_indices.data(), (int)pins.pinned_indices.size(),
+                                          tgt.empty() ? nullptr : tgt.data()));
+            else if (tgt != tgt_ && !tgt.empty())
+                check(pdg_solver_set_pin_targets(s_, 0, tgt.data()));
+            pins_ = pins.pinned_indices;
+            tgt_ = tgt;
+        }
         check(pdg_solver_step(s_, 1, &last_));
     }
     void reset() { if (s_) check(pdg_solver_reset(s_)); }
@@ -203,12 +216,17 @@ public:
     const pdg_frame_stats& last_stats() const { return last_; }
 
 private:
-    void build(ClothMesh& mesh, SimConstraints& sim, const Constraints& pins)
+    static std::vector<float> targets_of(const Constraints& pins)
     {
-        sim.ensure(mesh);
         std::vector<float> tgt;
         for (int i : pins.pinned_indices)
             for (int d = 0; d < 3; ++d) tgt.push_back(pins.target_positions[3 * i + d]);
+        return tgt;
+    }
+    void build(ClothMesh& mesh, SimConstraints& sim, const Constraints& pins)
+    {
+        sim.ensure(mesh);
+        const std::vector<float> tgt = targets_of(pins);
         check(pdg_constraints_set_pins(sim.h, pins.pinned_indices.data(), (int)pins.pinned_indices.size(),
                                        tgt.empty() ? nullptr : tgt.data()));
         pdg_config c;
@@ -223,22 +241,15 @@ private:
         c.bend_stiffness = cfg_.bend_stiffness;
         c.damping = cfg_.damping;
         if (cfg_.reference_literal) { c.mode = PDG_MODE_REFERENCE_LITERAL; c.init = PDG_INIT_PREVIOUS; }
-        const bool had = s_ != nullptr;
-        std::vector<float> x, v;
-        if (had) {
-            download(mesh);
-            x = mesh.pos_cpu; v = mesh.vel_cpu;
-            pdg_solver_destroy(s_);
-            s_ = nullptr;
-        }
         check(pdg_solver_create(&c, mesh.h, sim.h, nullptr, &s_));
-        if (had) check(pdg_solver_set_state(s_, 0, x.data(), v.data(), 0));
         pins_ = pins.pinned_indices;
+        tgt_ = tgt;
     }
     PDSolverConfig cfg_;
     int n_;
     pdg_solver* s_ = nullptr;
     std::vector<int> pins_;
+    std::vector<float> tgt_;
     pdg_frame_stats last_{};
 };
 

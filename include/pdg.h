@@ -248,6 +248,12 @@ int  pdg_solver_step_host(pdg_solver* s, int nframes, const float* x_in, const f
 /* Relative-residual target of one cloth (cloth = -1: every cloth), as
  * pdg_config.tolerance at creation; 0 runs the sweep cap. */
 int  pdg_solver_set_tolerance(pdg_solver* s, int cloth, float tolerance);
+/* Replace the pin set of one cloth on a live solver (Constraints::set_from_list
+ * + upload_to_gpu, src/constraints.cpp:14-22 and 77-101): idx P distinct
+ * vertex indices of the cloth, targets P*3 (NULL = rest positions).  The
+ * patch layout does not depend on the pins; only the per-vertex records
+ * change. */
+int  pdg_solver_set_pins(pdg_solver* s, int cloth, const int* idx, int P, const float* targets);
 /* Move the pins of one cloth (Constraints::target_positions). */
 int  pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets);
 /* Inertial prediction y of the last frame and the residual r(x) of a given

@@ -568,3 +568,28 @@ def test_batch_with_a_single_triangle_cloth(pdg, oracle):
     xt = singles[0][0]
     assert np.array_equal(xt[0], np.array([0, 0, 0], np.float32))   # pinned corner stays
     assert np.all(np.isfinite(xt))
+
+
+def test_set_pins_on_a_live_solver_equals_a_solver_built_with_them(pdg, oracle):
+    # Constraints::set_from_list + upload_to_gpu on a running solver: the new
+    # pin set (with moved targets) gives the bits of a solver created with it
+    n = 17
+    m, c, cfg, sc, a = scene(pdg, oracle, n=n, max_iterations=12)
+    s = pdg.Solver(cfg, m, c)
+    s.step(2, stats=False)
+    x, v = s.get_state()
+    top = np.arange(n, dtype=np.int32)
+    tgt = a["rest"][top] + np.array([0.0, 0.01, 0.02], np.float32)
+    _check = pdg._check
+    _check(pdg.lib().pdg_solver_set_pins(s.h, 0, pdg._p(top), len(top), pdg._p(np.ascontiguousarray(tgt))))
+    s.step(2, stats=False)
+    got = s.get_state()
+    c2 = pdg.Constraints(m).build_stretch(1e3).build_bend(1e-2).set_pins(top, tgt)
+    s2 = pdg.Solver(cfg, m, c2)
+    s2.set_state(x, v)
+    s2.step(2, stats=False)
+    ref = s2.get_state()
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    assert np.allclose(got[0][top], tgt) and np.all(got[1][top] == 0)
+    with pytest.raises(pdg.PDGError):
+        _check(pdg.lib().pdg_solver_set_pins(s.h, 0, pdg._p(np.array([0, 0], np.int32)), 2, None))
