@@ -26,6 +26,7 @@ struct pdg_warmstart {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     DevBuf<float> p, g, m, v, bdp;
+    DevBuf<float> part;   // per-block partial weight gradients (summed in a fixed order)
     DevBuf<bf16> wbuf;
     Bf16Weights W{};
     // graph and activations
@@ -51,6 +52,9 @@ namespace {
 
 inline int nb(long long n, int b) { return (int)((n + b - 1) / b); }
 
+constexpr int kWgradBlocks = 304;        // at most, blocks of a weight-gradient reduction
+constexpr int kMsgBwdBlocks = 4 * 152;   // at most, blocks of the message backward
+
 int refresh_bf16(pdg_warmstart* w, cudaStream_t st)
 {
     const Layout& y = w->lay;
@@ -71,6 +75,7 @@ int alloc_params(pdg_warmstart* w)
 {
     const int n = w->lay.total;
     GK(w->p.alloc(n)); GK(w->g.alloc(n)); GK(w->m.alloc(n)); GK(w->v.alloc(n)); GK(w->bdp.alloc(16));
+    GK(w->part.alloc(std::max((size_t)kWgradBlocks * (2 * H * H + 2 * H), (size_t)kMsgBwdBlocks * H * (EF + 1))));
     // bf16 copies: We 64x16, per layer AB 128x64, ABt 64x128, U 64x128, Ut 128x64, Wd 16x64, Wdt 64x16
     const size_t sizes[] = {(size_t)H * NFP, 2u * H * H, 2u * H * H, 2u * H * H, 2u * H * H, 16u * H, (size_t)H * 16};
     size_t total = sizes[0] + L * (sizes[1] + sizes[2] + sizes[3] + sizes[4]) + sizes[5] + sizes[6];
@@ -134,14 +139,25 @@ int forward(pdg_warmstart* w, cudaStream_t st)
     return PDG_OK;
 }
 
-int wgrad_grid(int M) { return std::max(1, std::min(304, nb(M, 32))); }
+int wgrad_grid(int M) { return std::max(1, std::min(kWgradBlocks, nb(M, 32))); }
+
+// dW (nout x K) and db (nout, may be null) of dY^T X over M rows: block
+// partial sums, then their sum in a fixed order
+template <typename TY, typename TX>
+void wgrad(pdg_warmstart* w, const TY* dY, int ldy, int nout, const TX* X, int ldx, int K, int M, float* dW,
+           float* db, cudaStream_t st)
+{
+    const int gw = wgrad_grid(M);
+    k_wgrad<TY, TX><<<gw, 256, 0, st>>>(dY, ldy, nout, X, ldx, K, M, w->part.p);
+    k_sum_parts<<<nb(nout * K + nout, 256), 256, 0, st>>>(w->part.p, gw, nout * K, nout, dW, db);
+}
 
 // gradients of the loss w.r.t. all parameters into w->g (zeroed here);
 // loss accumulated into w->loss; ew: per-edge weights of the smoothness term
 // (null: 1)
 int backward(pdg_warmstart* w, float inv_cnt, const float* ew, cudaStream_t st)
 {
-    const int N = w->N, gb = nb(N, 64), gw = wgrad_grid(N);
+    const int N = w->N, gb = nb(N, 64);
     const Layout& y = w->lay;
     const float* p = w->p.p;
     float* g = w->g.p;
@@ -149,24 +165,25 @@ int backward(pdg_warmstart* w, float inv_cnt, const float* ew, cudaStream_t st)
     GK(cudaMemsetAsync(w->loss.p, 0, sizeof(double), st));
     k_loss<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, w->target.p, w->freew.p, w->ptr.p, w->adj.p, ew, w->smooth,
                                        inv_cnt, w->dout.p, w->loss.p);
-    k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dout.p, 16, NO, w->hfin.p, H, H, N, g + y.Wd, g + y.bd);
+    wgrad<float, bf16>(w, w->dout.p, 16, NO, w->hfin.p, H, H, N, g + y.Wd, g + y.bd, st);
     k_gemm<float, 16, H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dout.p, 16, N, w->W.Wdt, nullptr, nullptr, 0, nullptr, 0,
                                                          nullptr, 0, w->dh.p, H);
     for (int l = L - 1; l >= 0; --l) {
         k_relu_bwd<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dh.p, H, w->uo[l].p, H, w->dtmp.p, H);
-        k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dtmp.p, H, H, w->cat[l].p, 2 * H, 2 * H, N, g + y.U[l], g + y.u[l]);
+        wgrad<float, bf16>(w, w->dtmp.p, H, H, w->cat[l].p, 2 * H, 2 * H, N, g + y.U[l], g + y.u[l], st);
         k_gemm<float, H, 2 * H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dtmp.p, H, N, w->W.Ut[l], nullptr, nullptr, 0,
                                                                 nullptr, 0, nullptr, 0, w->dcat.p, 2 * H);
         k_add<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dcat.p, 2 * H, w->dh.p, H);
-        k_msg_bwd<<<std::max(1, std::min(4 * 152, nb(N, 8))), 256, 0, st>>>(
-            N, w->ptr.p, w->adj.p, w->rev.p, w->ef.p, w->deg_inv.p, w->pq[l].p, p + y.C[l], p + y.c[l], w->dcat.p,
-            w->dpq.p, g + y.C[l], g + y.c[l]);
-        k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dpq.p, 2 * H, 2 * H, w->cat[l].p, 2 * H, H, N, g + y.A[l], nullptr);
+        const int gm = std::max(1, std::min(kMsgBwdBlocks, nb(N, 8)));
+        k_msg_bwd<<<gm, 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rev.p, w->ef.p, w->deg_inv.p, w->pq[l].p, p + y.C[l],
+                                      p + y.c[l], w->dcat.p, w->dpq.p, w->part.p);
+        k_sum_parts<<<nb(H * (EF + 1), 256), 256, 0, st>>>(w->part.p, gm, H * EF, H, g + y.C[l], g + y.c[l]);
+        wgrad<float, bf16>(w, w->dpq.p, 2 * H, 2 * H, w->cat[l].p, 2 * H, H, N, g + y.A[l], nullptr, st);
         k_gemm<float, 2 * H, H, EPI_ACCF><<<gb, 128, 0, st>>>(w->dpq.p, 2 * H, N, w->W.ABt[l], nullptr, nullptr, 0,
                                                               nullptr, 0, nullptr, 0, w->dh.p, H);
     }
     k_relu_bwd<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dh.p, H, w->cat[0].p, 2 * H, w->dtmp.p, H);
-    k_wgrad<float, bf16><<<gw, 256, 0, st>>>(w->dtmp.p, H, H, w->xin.p, NFP, NF, N, g + y.We, g + y.be);
+    wgrad<float, bf16>(w, w->dtmp.p, H, H, w->xin.p, NFP, NF, N, g + y.We, g + y.be, st);
     GK(cudaGetLastError());
     return PDG_OK;
 }
@@ -258,7 +275,8 @@ int pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out)
     int rc = alloc_params(w.get());
     if (rc) return rc;
     // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases; the
-    // decoder starts 10x smaller so the first predictions sit near y
+    // decoder starts at zero, so an untrained network predicts no change of
+    // the offset: the previous frame's offset where it is valid, else y
     const Layout& y = w->lay;
     std::vector<float> h(y.total, 0.f);
     std::mt19937_64 rng(seed);
@@ -270,7 +288,7 @@ int pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out)
     for (int l = 0; l < L; ++l) {
         fill(y.A[l], H, H, 1.f); fill(y.B[l], H, H, 1.f); fill(y.C[l], H, EF, 1.f); fill(y.U[l], H, 2 * H, 1.f);
     }
-    fill(y.Wd, NO, H, 0.1f);
+    // (decoder Wd, bd stay zero)
     GK(cudaMemcpyAsync(w->p.p, h.data(), sizeof(float) * y.total, cudaMemcpyHostToDevice, w->stream));
     rc = refresh_bf16(w.get(), w->stream);
     if (rc) return rc;
@@ -468,9 +486,9 @@ int pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* 
         rc = adam_step(w, lr, st);
         if (rc) return rc;
     }
-    // features and target 3, forward 2 + 3L, loss and backward 5 + 7L, Adam
-    // and the bf16 refresh 3 + 3L
-    s->launches += 3 + (2 + 3 * L) + (5 + 7 * L) + (lr > 0.f ? 3 + 3 * L : 0);
+    // features and target 3, forward 2 + 3L, loss and backward 7 + 11L,
+    // Adam and the bf16 refresh 3 + 3L
+    s->launches += 3 + (2 + 3 * L) + (7 + 11 * L) + (lr > 0.f ? 3 + 3 * L : 0);
     double l = 0.0;
     GK(cudaMemcpyAsync(&l, w->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     GK(cudaStreamSynchronize(st));
@@ -517,7 +535,7 @@ int pdg_warmstart_train_pair(pdg_warmstart* w, pdg_solver* traj, pdg_solver* dee
         rc = adam_step(w, lr, st);
         if (rc) return rc;
     }
-    traj->launches += 3 + (2 + 3 * L) + (5 + 7 * L) + (lr > 0.f ? 3 + 3 * L : 0);
+    traj->launches += 3 + (2 + 3 * L) + (7 + 11 * L) + (lr > 0.f ? 3 + 3 * L : 0);
     double l = 0.0;
     GK(cudaMemcpyAsync(&l, w->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     GK(cudaStreamSynchronize(st));

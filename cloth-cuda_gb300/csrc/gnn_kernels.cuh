@@ -5,8 +5,9 @@
 // prediction.  Node GEMMs run on the tensor cores (bf16 mma.sync m16n8k16,
 // fp32 accumulation, bf16 activations); edge messages are warp-per-node
 // gathers over the mesh adjacency (deterministic, no atomics); weight
-// gradients are fp32 block reductions; Adam keeps fp32 master weights and
-// refreshes their bf16 copies after each step.
+// gradients are fp32 per-block partial sums added in a fixed block order
+// (bitwise reproducible); Adam keeps fp32 master weights and refreshes their
+// bf16 copies after each step.
 //
 // Network (x: 14 node features, e_ij: 4 edge features):
 //   h0 = relu(We x + be)
@@ -111,13 +112,15 @@ __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx,
 __device__ __forceinline__ float tofloat(float v) { return v; }
 __device__ __forceinline__ float tofloat(bf16 v) { return __bfloat162float(v); }
 
-// dW[nout][k] += sum_rows dY[r][n] X[r][k];  db[n] += sum_rows dY[r][n].
-// Grid-stride over tiles of 32 rows; each thread owns up to 32 outputs in
-// registers; one atomic per output per block at the end.
+// Per-block partial weight gradients: block b writes
+//   part[b][n*K + k] = sum over its rows of dY[r][n] X[r][k]   (n < nout, k < K)
+//   part[b][nout*K + n] = sum over its rows of dY[r][n]
+// (grid-stride over tiles of 32 rows; each thread owns up to 32 outputs in
+// registers).  k_sum_parts then adds the blocks in a fixed order, so the
+// gradients are bitwise reproducible.
 template <typename TY, typename TX>
 __global__ void __launch_bounds__(256) k_wgrad(const TY* __restrict__ dY, int ldy, int nout, const TX* __restrict__ X,
-                                               int ldx, int K, int M, float* __restrict__ dW,
-                                               float* __restrict__ db)
+                                               int ldx, int K, int M, float* __restrict__ part)
 {
     constexpr int RT = 32, NT = 256, MAXO = 32;
     __shared__ float sy[RT][2 * H + 1];
@@ -149,15 +152,29 @@ __global__ void __launch_bounds__(256) k_wgrad(const TY* __restrict__ dY, int ld
                 acc[j] += s;
             }
         }
-        if (db && threadIdx.x < nout)
+        if (threadIdx.x < nout)
             for (int r = 0; r < RT; ++r) bacc += sy[r][threadIdx.x];
     }
+    float* row = part + (size_t)blockIdx.x * (nouts + nout);
     #pragma unroll
     for (int j = 0; j < MAXO; ++j) {
         const int o = threadIdx.x + j * NT;
-        if (o < nouts) atomicAdd(&dW[o], acc[j]);
+        if (o < nouts) row[o] = acc[j];
     }
-    if (db && threadIdx.x < nout) atomicAdd(&db[threadIdx.x], bacc);
+    if (threadIdx.x < nout) row[nouts + threadIdx.x] = bacc;
+}
+
+// dW[i] = sum_b part[b][i] (i < nw), db[i] = sum_b part[b][nw + i] (i < nb,
+// db may be null), blocks added in order b = 0, 1, ...
+__global__ void k_sum_parts(const float* __restrict__ part, int nblocks, int nw, int nbias, float* __restrict__ dW,
+                            float* __restrict__ db)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int width = nw + nbias;
+    if (i >= width || (i >= nw && !db)) return;
+    float s = 0.f;
+    for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * width + i];
+    if (i < nw) dW[i] = s; else db[i - nw] = s;
 }
 
 // Messages of layer l, warp per node, lane owns channels 2*lane, 2*lane+1:
@@ -189,14 +206,14 @@ __global__ void k_msg_fwd(int N, const int* __restrict__ ptr, const int* __restr
 
 // Backward of the messages: dP_i = sum_j g_ij, dQ_j = sum_i g_ij with
 // g_ij = [z_ij > 0] da_i / deg_i (da = dcat[:, H:2H]); dC, dc reduced per
-// block.  Each warp handles node n as receiver (dP) and as sender (dQ, via
+// block into `part`.  Each warp handles node n as receiver (dP) and as sender (dQ, via
 // the reverse edge's features).
 __global__ void __launch_bounds__(256) k_msg_bwd(int N, const int* __restrict__ ptr, const int* __restrict__ adj,
                                                  const int* __restrict__ rev, const float4* __restrict__ ef,
                                                  const float* __restrict__ deg_inv, const bf16* __restrict__ PQ,
                                                  const float* __restrict__ C, const float* __restrict__ cb,
                                                  const float* __restrict__ dcat, float* __restrict__ dpq,
-                                                 float* __restrict__ dC, float* __restrict__ dc)
+                                                 float* __restrict__ part)
 {
     __shared__ float red[8][H * (EF + 1)];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, ch = 2 * lane;
@@ -243,10 +260,12 @@ __global__ void __launch_bounds__(256) k_msg_bwd(int N, const int* __restrict__ 
     red[warp][H * EF + ch] = gc0;
     red[warp][H * EF + ch + 1] = gc1;
     __syncthreads();
+    // the block's partial dC (H x EF) then dc (H), summed over blocks in
+    // order by k_sum_parts
     for (int i = threadIdx.x; i < H * (EF + 1); i += 256) {
         float s = 0.f;
         for (int w = 0; w < 8; ++w) s += red[w][i];
-        if (i < H * EF) atomicAdd(&dC[i], s); else atomicAdd(&dc[i - H * EF], s);
+        part[(size_t)blockIdx.x * H * (EF + 1) + i] = s;
     }
 }
 

@@ -20,8 +20,13 @@ x* - y - d_prev from a deep solve of the same frame from the same state (cap
 to the converged positions (pdg_warmstart_train_pair).
 Loss: MSE, plus --smoothness times the squared error differences over the
 mesh edges (weighted by the PD system's stiffness with --energy-norm); Adam,
-lr 1e-3.  Evaluation on --eval-seeds held-out cloths (seeds disjoint from
-training): the same frames are solved from the inertial start and from the
+lr 1e-3.  The network starts with a zero decoder (it then predicts the
+previous frame's offset); before training and every --select-every batches
+it is validated by the mean sweeps its judged start needs to --val-tol on
+--val-seeds validation cloths, and the checkpoint with the fewest sweeps is
+kept (a lower offset error does not by itself mean fewer sweeps).
+Evaluation on --eval-seeds held-out cloths (seeds disjoint from training and
+validation): the same frames are solved from the inertial start and from the
 judged learned start (judge after K sweeps for each K of --judge) to each
 relative residual of --eval-tols with cap 200; the script reports sweeps,
 convergence, the fraction of cloth-frames where the learned start was kept,
@@ -45,6 +50,7 @@ import scenes  # noqa: E402
 
 PARAMS = os.path.join(HERE, "warmstart_params.npy")
 TRAIN_SEED0 = 1000          # training batches: seeds 1000, 1001, ...
+VAL_SEED0 = 700000          # validation batches (checkpoint selection)
 EVAL_SEED0 = 900000         # held-out evaluation batches
 
 
@@ -65,11 +71,41 @@ def _pair(args, seed):
     return out
 
 
+def validate(params, args):
+    """Mean sweeps to --val-tol (cap 200) of the judged learned start with
+    `params` on the validation cloths (seeds disjoint from training and
+    evaluation); the checkpoint selection's measure."""
+    rows = []
+    for b in range(max(1, args.val_seeds // args.batch)):
+        r, _, _ = solve_frames(params, dict(max_iterations=200, tolerance=args.val_tol, kernel=pdg.KERNEL_STREAM,
+                                            patch_verts=128, block_threads=128, init=pdg.INIT_WARMSTART),
+                               VAL_SEED0 + b, args.batch, args.val_frames, args.n_range, judge=args.val_judge)
+        rows += r
+    return float(np.mean([x["iterations"] for x in rows]))
+
+
 def train(args, log=print):
+    """Adam on the training trajectories; every --select-every batches (and
+    before the first) the network is validated by sweeps and the best
+    checkpoint is kept.  Returns (best parameters, losses, validation log)."""
     w = pdg.WarmStart(seed=args.seed).set_smoothness(args.smoothness).set_energy_norm(args.energy_norm)
     nbatches = max(1, args.trajectories // args.batch)
-    losses = []
+    losses, val = [], []
+    best = None
     t0 = time.time()
+
+    def checkpoint(b):
+        nonlocal best
+        if not args.select_every:
+            return
+        p = w.get_params()
+        sw = validate(p, args)
+        val.append(dict(batch=b, sweeps=sw))
+        log("checkpoint after %d batches: validation sweeps %.2f" % (b, sw))
+        if best is None or sw < best[1]:
+            best = (p, sw, b)
+
+    checkpoint(0)
     for b in range(nbatches):
         traj, deep = _pair(args, TRAIN_SEED0 + b)
         w.attach(traj)
@@ -79,7 +115,11 @@ def train(args, log=print):
             log("batch %d/%d  mean loss %.4f  (%.1f s)" % (b + 1, nbatches, losses[-1], time.time() - t0))
         traj.close(); deep.close()
         w.solver = None
-    return w, losses
+        if args.select_every and ((b + 1) % args.select_every == 0 or b == nbatches - 1):
+            checkpoint(b + 1)
+    if best is None:
+        return w.get_params(), losses, val, nbatches
+    return best[0], losses, val, best[2]
 
 
 def score(params, args, seeds=2, frames=32, base_seed=500000):
@@ -183,6 +223,12 @@ def main():
     ap.add_argument("--n-min", type=int, default=17)
     ap.add_argument("--n-max", type=int, default=129)
     ap.add_argument("--params", default="", help="evaluate these parameters instead of training")
+    ap.add_argument("--select-every", type=int, default=8,
+                    help="validate every this many batches and keep the checkpoint with the fewest sweeps (0: keep the last)")
+    ap.add_argument("--val-seeds", type=int, default=64)
+    ap.add_argument("--val-frames", type=int, default=8)
+    ap.add_argument("--val-tol", type=float, default=1e-2)
+    ap.add_argument("--val-judge", type=int, default=4)
     ap.add_argument("--out", default="")
     ap.add_argument("--json", default="")
     args = ap.parse_args()
@@ -190,12 +236,11 @@ def main():
     args.eval_tols = [float(x) for x in args.eval_tols.split(",") if x]
     args.judge = [int(x) for x in args.judge.split(",") if x]
     t0 = time.time()
-    losses = []
+    losses, val, chosen = [], [], None
     if args.params:
         params = np.load(args.params).astype(np.float32)
     else:
-        w, losses = train(args)
-        params = w.get_params()
+        params, losses, val, chosen = train(args)
         if args.out:
             np.save(args.out, params)
     t_train = time.time() - t0
@@ -204,7 +249,8 @@ def main():
     print("held-out loss: trained %.4f, zero parameters (previous offset) %.4f" % (held_out, zero))
     ev = evaluate(params, args)
     result = dict(args={k: v for k, v in vars(args).items() if k != "n_range"}, train_seconds=t_train,
-                  train_loss=losses, held_out_loss=held_out, zero_params_loss=zero, eval=ev)
+                  train_loss=losses, validation=val, chosen_checkpoint_batches=chosen, held_out_loss=held_out,
+                  zero_params_loss=zero, eval=ev)
     print(json.dumps(result))
     if args.json:
         json.dump(result, open(args.json, "w"), indent=1)

@@ -328,6 +328,8 @@ void pdg_autotune_clear_cache(void);
  * the prediction.  Parameter layout: see pdg_warmstart_get_params
  * (We[64][14] be[64] {A[64][64] B[64][64] C[64][4] c[64] U[64][128] u[64]}
  * x 2 Wd[3][64] bd[3], fp32). */
+/* A new network from `seed`: random hidden layers and a zero decoder, so
+ * that before training it predicts the previous frame's offset. */
 int  pdg_warmstart_create(unsigned long long seed, pdg_warmstart** out);
 int  pdg_warmstart_param_count(const pdg_warmstart* w, int* n);
 int  pdg_warmstart_get_params(pdg_warmstart* w, float* host);

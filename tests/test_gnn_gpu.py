@@ -85,10 +85,8 @@ def test_adam_step_matches_oracle(pdg):
 def test_training_on_solver_data_beats_previous_offset_and_never_hurts(pdg):
     import scenes
     w = pdg.WarmStart(seed=0)
-    # fresh trajectories of cloths from the batched distribution; training
-    # is not bit-reproducible (the blocks add their weight-gradient partial
-    # sums with float atomics), so it runs long enough to clear the bar by a
-    # wide margin
+    # fresh trajectories of cloths from the batched distribution, long enough
+    # to clear the bar by a wide margin
     for b in range(20):
         ms, cs, cfgs, _ = scenes.batch(16, seed=100 + b, max_iterations=300, tolerance=1e-6, n_range=(17, 33),
                                        kernel=pdg.KERNEL_GRAPH)
@@ -244,3 +242,22 @@ def test_previous_offset_is_kept_across_an_unchanged_state_and_dropped_when_it_c
     moved = run("moved")
     moved_reatt = run("moved_reattached")
     assert all(np.array_equal(a, b) for a, b in zip(moved, moved_reatt))
+
+
+def test_training_is_bitwise_reproducible(pdg):
+    # the solver's frames, the network and the weight-gradient reductions
+    # (block partial sums added in a fixed order) are all deterministic
+    import scenes
+    params = []
+    for _ in range(2):
+        ms, cs, cfgs, _ = scenes.batch(6, seed=77, max_iterations=40, tolerance=0.0, n_range=(17, 33),
+                                       kernel=pdg.KERNEL_GRAPH)
+        s = pdg.Solver(cfgs, ms, cs)
+        w = pdg.WarmStart(seed=5)
+        w.attach(s)
+        for _ in range(4):
+            w.train_frame(s, 1e-3)
+        params.append(w.get_params())
+        s.close()
+        w.close()
+    assert np.array_equal(params[0], params[1])
