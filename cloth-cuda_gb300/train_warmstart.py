@@ -2,12 +2,13 @@
 
     python cloth-cuda_gb300/train_warmstart.py [--trajectories 2000] [--frames 64]
         [--batch 32] [--lr 1e-3] [--smoothness 0] [--energy-norm] [--eval-seeds 128]
-        [--eval-frames 16] [--judge 0,4] [--out params.npy] [--json result.json]
+        [--eval-frames 16] [--eval-cap 200] [--judge 0,4] [--out params.npy] [--json result.json]
 
 The committed parameters (cloth-cuda_gb300/warmstart_params.npy) were made by
 
     python cloth-cuda_gb300/train_warmstart.py --trajectories 2000 --frames 64 --batch 32 \\
-        --out cloth-cuda_gb300/warmstart_params.npy --json gpurun_out/train.json
+        --eval-seeds 128 --eval-frames 16 --eval-tols 3e-2,1e-2,1e-5 --judge 4 \\
+        --out cloth-cuda_gb300/warmstart_params.npy --json train.json
 
 Training data: 2,000 trajectories of 64 frames of cloths drawn from the
 batched-workload distribution (scenes.batch: grid side 17..129, 0.5-2 m,
@@ -28,7 +29,7 @@ kept (a lower offset error does not by itself mean fewer sweeps).
 Evaluation on --eval-seeds held-out cloths (seeds disjoint from training and
 validation): the same frames are solved from the inertial start and from the
 judged learned start (judge after K sweeps for each K of --judge) to each
-relative residual of --eval-tols with cap 200; the script reports sweeps,
+relative residual of --eval-tols with cap --eval-cap (200); the script reports sweeps,
 convergence, the fraction of cloth-frames where the learned start was kept,
 and the sweeps saved on the frames both starts solve.
 """
@@ -175,7 +176,7 @@ def evaluate(params, args, log=print):
     nb = max(1, args.eval_seeds // args.batch)
     out = {}
     for tol in args.eval_tols:
-        common = dict(max_iterations=200, tolerance=tol, kernel=pdg.KERNEL_STREAM, patch_verts=128,
+        common = dict(max_iterations=args.eval_cap, tolerance=tol, kernel=pdg.KERNEL_STREAM, patch_verts=128,
                       block_threads=128)
         arms = {"inertial": dict(params=None, init=pdg.INIT_INERTIAL, judge=0)}
         for K in args.judge:
@@ -219,6 +220,7 @@ def main():
     ap.add_argument("--eval-seeds", type=int, default=128)
     ap.add_argument("--eval-frames", type=int, default=16)
     ap.add_argument("--eval-tols", default="1e-2,1e-5", help="relative residuals the evaluation solves to")
+    ap.add_argument("--eval-cap", type=int, default=200, help="sweep cap of the evaluation's frames")
     ap.add_argument("--judge", default="0,4", help="judge sweep counts to evaluate")
     ap.add_argument("--n-min", type=int, default=17)
     ap.add_argument("--n-max", type=int, default=129)
