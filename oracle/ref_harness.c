@@ -7,7 +7,8 @@
  * predict, then per iteration stretch projection, bend projection, clear rhs,
  * stretch rhs, bend rhs, inertial rhs, Jacobi divide, pins; finally the
  * velocity update and pins.  Block size 256, legacy default stream, as the
- * reference.  Used only to produce golden vectors for the oracle.
+ * reference.  Used only to produce golden vectors for the oracle and, in a
+ * GPU test, to time the reference's kernels beside the fused sweep.
  */
 #include <cuda.h>
 #include <stdio.h>
@@ -35,22 +36,90 @@ enum { K_PREDICT, K_TRI, K_TRI_RHS, K_BEND, K_BEND_RHS, K_CLEAR, K_INERT, K_DIV,
 
 static unsigned nb(int n) { return (unsigned)((n + 255) / 256); }
 
-int ref_step(const char* cubin, int N, int T, int E, int P, float* pos, float* vel, const float* mass,
-             const int* tris, const float* Dm_inv, const float* rest_area, const float* stretch_k,
-             const float* diag, const int* quads, const float* bw, const float* bn, const float* bk,
-             const int* pins, const float* targets, int iters, float dt, float gravity, float damping,
-             char* err, int errlen)
+/* The reference's frame: its launches in PDSolver::step order.  ev0/ev1
+ * (may be 0) are recorded around the iteration loop. */
+typedef struct {
+    CUfunction fn[NK];
+    int N, T, E, P;
+    CUdeviceptr pos, vel, mass, tris, G, area, k, diag, quads, bw, bn, bk, pins, tgt;
+    CUdeviceptr pred, rhs, prev, nw, proj, bproj;
+} RefFrame;
+
+static CUresult ref_frame(RefFrame* f, int iters, float dt, float gravity, float damping, CUevent ev0, CUevent ev1)
+{
+    CUresult r;
+    int N = f->N, T = f->T, E = f->E, P = f->P;
+    const size_t b3 = sizeof(float) * 3 * (size_t)N;
+    const float h2 = dt * dt;
+#define L(x) do { r = (x); if (r != CUDA_SUCCESS) return r; } while (0)
+    L(cuMemcpyDtoD(f->prev, f->pos, b3));
+    { void* a[] = {&f->pos, &f->vel, &f->pred, &N, &dt, &gravity};
+      L(cuLaunchKernel(f->fn[K_PREDICT], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
+    if (ev0) L(cuEventRecord(ev0, 0));
+    CUdeviceptr d_in = f->pos, d_out = f->nw;
+    for (int it = 0; it < iters; ++it) {
+        if (T > 0) {
+            void* a[] = {&d_in, &f->tris, &f->G, &f->proj, &T};
+            L(cuLaunchKernel(f->fn[K_TRI], nb(T), 1, 1, 256, 1, 1, 0, 0, a, NULL));
+        }
+        if (E > 0) {
+            void* a[] = {&d_in, &f->quads, &f->bw, &f->bn, &f->bproj, &E};
+            L(cuLaunchKernel(f->fn[K_BEND], nb(E), 1, 1, 256, 1, 1, 0, 0, a, NULL));
+        }
+        { void* a[] = {&f->rhs, &N};
+          L(cuLaunchKernel(f->fn[K_CLEAR], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
+        if (T > 0) {
+            void* a[] = {&f->tris, &f->G, &f->area, &f->k, &f->proj, &f->rhs, &T, (void*)&h2};
+            L(cuLaunchKernel(f->fn[K_TRI_RHS], nb(T), 1, 1, 256, 1, 1, 0, 0, a, NULL));
+        }
+        if (E > 0) {
+            void* a[] = {&f->quads, &f->bw, &f->bk, &f->bproj, &f->rhs, &E, (void*)&h2};
+            L(cuLaunchKernel(f->fn[K_BEND_RHS], nb(E), 1, 1, 256, 1, 1, 0, 0, a, NULL));
+        }
+        { void* a[] = {&f->rhs, &f->mass, &f->pred, &N};
+          L(cuLaunchKernel(f->fn[K_INERT], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
+        { void* a[] = {&d_out, &f->rhs, &f->diag, &N};
+          L(cuLaunchKernel(f->fn[K_DIV], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
+        if (P > 0) {
+            void* a[] = {&d_out, &f->vel, &f->pins, &f->tgt, &P};
+            L(cuLaunchKernel(f->fn[K_PINS], nb(P), 1, 1, 256, 1, 1, 0, 0, a, NULL));
+        }
+        { CUdeviceptr t = d_in; d_in = d_out; d_out = t; }
+    }
+    if (ev1) L(cuEventRecord(ev1, 0));
+    if (d_in != f->pos) L(cuMemcpyDtoD(f->pos, d_in, b3));
+    { void* a[] = {&f->prev, &f->vel, &f->pos, &N, &dt, &damping};
+      L(cuLaunchKernel(f->fn[K_VEL], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
+    if (P > 0) {
+        void* a[] = {&f->pos, &f->vel, &f->pins, &f->tgt, &P};
+        L(cuLaunchKernel(f->fn[K_PINS], nb(P), 1, 1, 256, 1, 1, 0, 0, a, NULL));
+    }
+#undef L
+    return CUDA_SUCCESS;
+}
+
+/* Loads the reference's kernels and uploads one cloth; `nframes` frames
+ * follow.  With timing (frame_ms != NULL), `nframes` frames are timed after
+ * one untimed frame, each from the input state (re-uploaded before it,
+ * outside the timed region): frame_ms and loop_ms receive the mean time of a
+ * whole frame and of its iteration loop (CUDA events on the legacy stream).
+ * Without timing, the frames run one after another and the result is copied
+ * back into pos / vel. */
+static int ref_run(const char* cubin, int N, int T, int E, int P, float* pos, float* vel, const float* mass,
+                   const int* tris, const float* Dm_inv, const float* rest_area, const float* stretch_k,
+                   const float* diag, const int* quads, const float* bw, const float* bn, const float* bk,
+                   const int* pins, const float* targets, int iters, float dt, float gravity, float damping,
+                   int nframes, float* frame_ms, float* loop_ms, char* err, int errlen)
 {
     int rc = 0;
     CUdevice dev;
     CUcontext ctx = NULL;
     CUmodule mod = NULL;
-    CUfunction fn[NK];
-    CUdeviceptr d_pos = 0, d_vel = 0, d_mass = 0, d_tris = 0, d_G = 0, d_area = 0, d_k = 0, d_diag = 0;
-    CUdeviceptr d_quads = 0, d_bw = 0, d_bn = 0, d_bk = 0, d_pins = 0, d_tgt = 0;
-    CUdeviceptr d_pred = 0, d_rhs = 0, d_prev = 0, d_new = 0, d_proj = 0, d_bproj = 0;
+    CUevent e[4] = {0, 0, 0, 0};
+    RefFrame f;
+    memset(&f, 0, sizeof(f));
+    f.N = N; f.T = T; f.E = E; f.P = P;
     const size_t b3 = sizeof(float) * 3 * (size_t)N;
-    memset(fn, 0, sizeof(fn));
 
     CHK(cuInit(0));
     CHK(cuDeviceGet(&dev, 0));
@@ -67,87 +136,89 @@ int ref_step(const char* cubin, int N, int T, int E, int P, float* pos, float* v
             const char* name = NULL;
             CHK(cuFuncGetName(&name, all[i]));
             for (int k = 0; k < NK; ++k)
-                if (name && strncmp(name, kNames[k], strlen(kNames[k])) == 0) fn[k] = all[i];
+                if (name && strncmp(name, kNames[k], strlen(kNames[k])) == 0) f.fn[k] = all[i];
         }
         for (int k = 0; k < NK; ++k)
-            if (!fn[k]) { snprintf(err, (size_t)errlen, "kernel %s not found", kNames[k]); rc = -2; goto done; }
+            if (!f.fn[k]) { snprintf(err, (size_t)errlen, "kernel %s not found", kNames[k]); rc = -2; goto done; }
     }
 #define ALLOC_COPY(d, h, bytes) do { if ((bytes) > 0) { CHK(cuMemAlloc(&d, (bytes))); CHK(cuMemcpyHtoD(d, (h), (bytes))); } } while (0)
-    ALLOC_COPY(d_pos, pos, b3);
-    ALLOC_COPY(d_vel, vel, b3);
-    ALLOC_COPY(d_mass, mass, sizeof(float) * (size_t)N);
-    ALLOC_COPY(d_tris, tris, sizeof(int) * 3 * (size_t)T);
-    ALLOC_COPY(d_G, Dm_inv, sizeof(float) * 4 * (size_t)T);
-    ALLOC_COPY(d_area, rest_area, sizeof(float) * (size_t)T);
-    ALLOC_COPY(d_k, stretch_k, sizeof(float) * (size_t)T);
-    ALLOC_COPY(d_diag, diag, sizeof(float) * (size_t)N);
-    ALLOC_COPY(d_quads, quads, sizeof(int) * 4 * (size_t)E);
-    ALLOC_COPY(d_bw, bw, sizeof(float) * 4 * (size_t)E);
-    ALLOC_COPY(d_bn, bn, sizeof(float) * (size_t)E);
-    ALLOC_COPY(d_bk, bk, sizeof(float) * (size_t)E);
-    ALLOC_COPY(d_pins, pins, sizeof(int) * (size_t)P);
-    ALLOC_COPY(d_tgt, targets, sizeof(float) * 3 * (size_t)P);
-    CHK(cuMemAlloc(&d_pred, b3));
-    CHK(cuMemAlloc(&d_rhs, b3));
-    CHK(cuMemAlloc(&d_prev, b3));
-    CHK(cuMemAlloc(&d_new, b3));
-    if (T > 0) CHK(cuMemAlloc(&d_proj, sizeof(float) * 6 * (size_t)T));
-    if (E > 0) CHK(cuMemAlloc(&d_bproj, sizeof(float) * 3 * (size_t)E));
+    ALLOC_COPY(f.pos, pos, b3);
+    ALLOC_COPY(f.vel, vel, b3);
+    ALLOC_COPY(f.mass, mass, sizeof(float) * (size_t)N);
+    ALLOC_COPY(f.tris, tris, sizeof(int) * 3 * (size_t)T);
+    ALLOC_COPY(f.G, Dm_inv, sizeof(float) * 4 * (size_t)T);
+    ALLOC_COPY(f.area, rest_area, sizeof(float) * (size_t)T);
+    ALLOC_COPY(f.k, stretch_k, sizeof(float) * (size_t)T);
+    ALLOC_COPY(f.diag, diag, sizeof(float) * (size_t)N);
+    ALLOC_COPY(f.quads, quads, sizeof(int) * 4 * (size_t)E);
+    ALLOC_COPY(f.bw, bw, sizeof(float) * 4 * (size_t)E);
+    ALLOC_COPY(f.bn, bn, sizeof(float) * (size_t)E);
+    ALLOC_COPY(f.bk, bk, sizeof(float) * (size_t)E);
+    ALLOC_COPY(f.pins, pins, sizeof(int) * (size_t)P);
+    ALLOC_COPY(f.tgt, targets, sizeof(float) * 3 * (size_t)P);
+    CHK(cuMemAlloc(&f.pred, b3));
+    CHK(cuMemAlloc(&f.rhs, b3));
+    CHK(cuMemAlloc(&f.prev, b3));
+    CHK(cuMemAlloc(&f.nw, b3));
+    if (T > 0) CHK(cuMemAlloc(&f.proj, sizeof(float) * 6 * (size_t)T));
+    if (E > 0) CHK(cuMemAlloc(&f.bproj, sizeof(float) * 3 * (size_t)E));
 
-    {
-        const float h2 = dt * dt;
-        CHK(cuMemcpyDtoD(d_prev, d_pos, b3));
-        { void* a[] = {&d_pos, &d_vel, &d_pred, &N, &dt, &gravity};
-          CHK(cuLaunchKernel(fn[K_PREDICT], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
-        CUdeviceptr d_in = d_pos, d_out = d_new;
-        for (int it = 0; it < iters; ++it) {
-            if (T > 0) {
-                void* a[] = {&d_in, &d_tris, &d_G, &d_proj, &T};
-                CHK(cuLaunchKernel(fn[K_TRI], nb(T), 1, 1, 256, 1, 1, 0, 0, a, NULL));
-            }
-            if (E > 0) {
-                void* a[] = {&d_in, &d_quads, &d_bw, &d_bn, &d_bproj, &E};
-                CHK(cuLaunchKernel(fn[K_BEND], nb(E), 1, 1, 256, 1, 1, 0, 0, a, NULL));
-            }
-            { void* a[] = {&d_rhs, &N};
-              CHK(cuLaunchKernel(fn[K_CLEAR], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
-            if (T > 0) {
-                void* a[] = {&d_tris, &d_G, &d_area, &d_k, &d_proj, &d_rhs, &T, (void*)&h2};
-                CHK(cuLaunchKernel(fn[K_TRI_RHS], nb(T), 1, 1, 256, 1, 1, 0, 0, a, NULL));
-            }
-            if (E > 0) {
-                void* a[] = {&d_quads, &d_bw, &d_bk, &d_bproj, &d_rhs, &E, (void*)&h2};
-                CHK(cuLaunchKernel(fn[K_BEND_RHS], nb(E), 1, 1, 256, 1, 1, 0, 0, a, NULL));
-            }
-            { void* a[] = {&d_rhs, &d_mass, &d_pred, &N};
-              CHK(cuLaunchKernel(fn[K_INERT], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
-            { void* a[] = {&d_out, &d_rhs, &d_diag, &N};
-              CHK(cuLaunchKernel(fn[K_DIV], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
-            if (P > 0) {
-                void* a[] = {&d_out, &d_vel, &d_pins, &d_tgt, &P};
-                CHK(cuLaunchKernel(fn[K_PINS], nb(P), 1, 1, 256, 1, 1, 0, 0, a, NULL));
-            }
-            { CUdeviceptr t = d_in; d_in = d_out; d_out = t; }
-        }
-        if (d_in != d_pos) CHK(cuMemcpyDtoD(d_pos, d_in, b3));
-        { void* a[] = {&d_prev, &d_vel, &d_pos, &N, &dt, &damping};
-          CHK(cuLaunchKernel(fn[K_VEL], nb(N), 1, 1, 256, 1, 1, 0, 0, a, NULL)); }
-        if (P > 0) {
-            void* a[] = {&d_pos, &d_vel, &d_pins, &d_tgt, &P};
-            CHK(cuLaunchKernel(fn[K_PINS], nb(P), 1, 1, 256, 1, 1, 0, 0, a, NULL));
-        }
+    if (!frame_ms) {
+        for (int q = 0; q < nframes; ++q) CHK(ref_frame(&f, iters, dt, gravity, damping, 0, 0));
         CHK(cuCtxSynchronize());
-        CHK(cuMemcpyDtoH(pos, d_pos, b3));
-        CHK(cuMemcpyDtoH(vel, d_vel, b3));
+        CHK(cuMemcpyDtoH(pos, f.pos, b3));
+        CHK(cuMemcpyDtoH(vel, f.vel, b3));
+    } else {
+        double tf = 0.0, tl = 0.0;
+        for (int i = 0; i < 4; ++i) CHK(cuEventCreate(&e[i], CU_EVENT_DEFAULT));
+        for (int q = -1; q < nframes; ++q) {
+            CHK(cuMemcpyHtoD(f.pos, pos, b3));
+            CHK(cuMemcpyHtoD(f.vel, vel, b3));
+            CHK(cuEventRecord(e[0], 0));
+            CHK(ref_frame(&f, iters, dt, gravity, damping, e[1], e[2]));
+            CHK(cuEventRecord(e[3], 0));
+            CHK(cuEventSynchronize(e[3]));
+            float a = 0.f, b = 0.f;
+            CHK(cuEventElapsedTime(&a, e[0], e[3]));
+            CHK(cuEventElapsedTime(&b, e[1], e[2]));
+            if (q >= 0) { tf += a; tl += b; }
+        }
+        *frame_ms = (float)(tf / (nframes > 0 ? nframes : 1));
+        if (loop_ms) *loop_ms = (float)(tl / (nframes > 0 ? nframes : 1));
     }
 done:
+    for (int i = 0; i < 4; ++i)
+        if (e[i]) cuEventDestroy(e[i]);
     {
-        CUdeviceptr all[] = {d_pos, d_vel, d_mass, d_tris, d_G, d_area, d_k, d_diag, d_quads, d_bw, d_bn, d_bk,
-                             d_pins, d_tgt, d_pred, d_rhs, d_prev, d_new, d_proj, d_bproj};
+        CUdeviceptr all[] = {f.pos, f.vel, f.mass, f.tris, f.G, f.area, f.k, f.diag, f.quads, f.bw, f.bn, f.bk,
+                             f.pins, f.tgt, f.pred, f.rhs, f.prev, f.nw, f.proj, f.bproj};
         for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i)
             if (all[i]) cuMemFree(all[i]);
     }
     if (mod) cuModuleUnload(mod);
     if (ctx) cuDevicePrimaryCtxRelease(dev);
     return rc;
+}
+
+int ref_step(const char* cubin, int N, int T, int E, int P, float* pos, float* vel, const float* mass,
+             const int* tris, const float* Dm_inv, const float* rest_area, const float* stretch_k,
+             const float* diag, const int* quads, const float* bw, const float* bn, const float* bk,
+             const int* pins, const float* targets, int iters, float dt, float gravity, float damping,
+             char* err, int errlen)
+{
+    return ref_run(cubin, N, T, E, P, pos, vel, mass, tris, Dm_inv, rest_area, stretch_k, diag, quads, bw, bn, bk,
+                   pins, targets, iters, dt, gravity, damping, 1, NULL, NULL, err, errlen);
+}
+
+/* Timing of the reference's frame: the mean of `nframes` frames from the
+ * input state (not changed), after one untimed frame. */
+int ref_time(const char* cubin, int N, int T, int E, int P, float* pos, float* vel, const float* mass,
+             const int* tris, const float* Dm_inv, const float* rest_area, const float* stretch_k,
+             const float* diag, const int* quads, const float* bw, const float* bn, const float* bk,
+             const int* pins, const float* targets, int iters, float dt, float gravity, float damping,
+             int nframes, float* frame_ms, float* loop_ms, char* err, int errlen)
+{
+    if (!frame_ms || nframes <= 0) { snprintf(err, (size_t)errlen, "ref_time: bad arguments"); return -3; }
+    return ref_run(cubin, N, T, E, P, pos, vel, mass, tris, Dm_inv, rest_area, stretch_k, diag, quads, bw, bn, bk,
+                   pins, targets, iters, dt, gravity, damping, nframes, frame_ms, loop_ms, err, errlen);
 }

@@ -3,7 +3,8 @@
 Wraps oracle/libref_harness.so (ref_harness.c), which loads the reference's
 src/pd_solver.cu compiled into oracle/_ref/pd_solver_ref.cubin by
 ref_build.py.  Used by tests/golden/make_ref_golden.py to record golden
-vectors on a GPU machine.
+vectors on a GPU machine, and by a GPU test that times the reference's kernels
+beside the fused sweep.
 """
 from __future__ import annotations
 
@@ -31,6 +32,35 @@ def _load():
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None and a.size else None
+
+
+def _args(scene):
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)
+    i32 = lambda a: np.ascontiguousarray(a, np.int32)
+    return dict(mass=f32(scene.mass), tris=i32(scene.tris), G=f32(scene.G), area=f32(scene.area),
+                k=f32(scene.k_stretch), diag=f32(scene.diag), quads=i32(scene.hinge), bw=f32(scene.w),
+                bn=f32(scene.nrest), bk=f32(scene.hk), pins=i32(scene.pins), tgt=f32(scene.pin_targets))
+
+
+def ref_time(scene, x, v, iters, nframes, gravity=None):
+    """Mean device time (ms) of the reference's frame (PDSolver::step's
+    launches, `iters` iterations) and of its iteration loop, over `nframes`
+    frames from the state (x, v) after one untimed frame (CUDA events)."""
+    L = _load()
+    x = np.ascontiguousarray(x, np.float32).reshape(-1).copy()
+    v = np.ascontiguousarray(v, np.float32).reshape(-1).copy()
+    g = scene.ext[1] if gravity is None else gravity
+    err = C.create_string_buffer(512)
+    a = _args(scene)
+    fm, lm = C.c_float(), C.c_float()
+    rc = L.ref_time(ref_build.CUBIN.encode(), scene.N, scene.T, len(scene.hinge), len(scene.pins), _p(x), _p(v),
+                    _p(a["mass"]), _p(a["tris"]), _p(a["G"]), _p(a["area"]), _p(a["k"]), _p(a["diag"]),
+                    _p(a["quads"]), _p(a["bw"]), _p(a["bn"]), _p(a["bk"]), _p(a["pins"]), _p(a["tgt"]), int(iters),
+                    C.c_float(scene.h), C.c_float(g), C.c_float(scene.damping), int(nframes), C.byref(fm),
+                    C.byref(lm), err, 512)
+    if rc != 0:
+        raise RuntimeError("reference kernels failed: " + err.value.decode())
+    return fm.value, lm.value
 
 
 def ref_step(scene, x, v, iters, gravity=None):
