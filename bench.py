@@ -14,9 +14,11 @@ update) of the named workload, all synthetic and generated from seeds:
             plain PD (inertial start) and batched learned PD (the learned warm
             start with the committed network, judged after K sweeps against
             the inertial start), then both again at a tolerance the iteration
-            reaches within the cap (1e-2).  `value` is the learned arm at the
-            metric's tolerance; every arm's sweeps, converged fraction and
-            vertex-steps/s are in `config.arms`.
+            reaches within the cap (1e-2).  A third arm always keeps the
+            learned start (no judge), to show what the judge costs.  `value`
+            is the judged learned arm at the metric's tolerance; every arm's
+            sweeps, converged fraction and vertex-steps/s are in
+            `config.arms`.
   plain257  257x257 hanging cloth (66,049 vertices, 131,072 triangles), 2 m x
             2 m, z jitter N(0, 1e-4), two top corners pinned, g = -9.81 on y,
             areal density 0.1, stretch k 1e3 (x area), cotangent bend k 1e-2,
@@ -396,8 +398,12 @@ def run_batch(args, rank, world, local_rank):
     stream = torch.cuda.Stream()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
     params = train_warmstart.load_params()
+    # plain PD, the learned start judged against the inertial start (the
+    # metric's arm), and the learned start always kept (no judge: what the
+    # judge costs)
     solvers = {}
-    for arm, init in (("plain", pdg.INIT_INERTIAL), ("learned", pdg.INIT_WARMSTART)):
+    for arm, init in (("plain", pdg.INIT_INERTIAL), ("learned", pdg.INIT_WARMSTART),
+                      ("learned_kept", pdg.INIT_WARMSTART_KEEP)):
         for c in cfgs:
             c.init = init
         solvers[arm] = pdg.Solver(cfgs, meshes, cons, stream=stream.cuda_stream)
@@ -406,6 +412,9 @@ def run_batch(args, rank, world, local_rank):
     if args.judge_sweeps is not None:
         ws.set_judge_sweeps(args.judge_sweeps)
     ws.attach(solvers["learned"])
+    ws_kept = pdg.WarmStart(seed=0)
+    ws_kept.set_params(params)
+    ws_kept.attach(solvers["learned_kept"])
     info = solvers["plain"].launch_info()
 
     if args.quick:
@@ -429,7 +438,7 @@ def run_batch(args, rank, world, local_rank):
     launches = 0
     for tol in (wl["tol"], reach):
         key = "tol_%g" % tol
-        for arm in ("plain", "learned"):
+        for arm in ("plain", "learned", "learned_kept"):
             s = solvers[arm]
             s.set_tolerance(tol)
             s.set_state_all(rest, zero)   # every arm from the same rest state
@@ -446,10 +455,12 @@ def run_batch(args, rank, world, local_rank):
                 launches = nl
             dev[(key, arm)] = dev_s
             arms.setdefault(key, {})[arm] = _arm_summary(rows, N, dev_s, args.steps)
-        pl, le = arms[key]["plain"], arms[key]["learned"]
-        arms[key]["learned_over_plain"] = {
-            "vertex_steps_per_s": le["vertex_steps_per_s"] / pl["vertex_steps_per_s"],
-            "iterations": le["iterations_mean"] / max(pl["iterations_mean"], 1e-9)}
+        pl = arms[key]["plain"]
+        for arm in ("learned", "learned_kept"):
+            le = arms[key][arm]
+            arms[key]["%s_over_plain" % arm] = {
+                "vertex_steps_per_s": le["vertex_steps_per_s"] / pl["vertex_steps_per_s"],
+                "iterations": le["iterations_mean"] / max(pl["iterations_mean"], 1e-9)}
     total_s = dev[("tol_%g" % wl["tol"], "learned")]
     if world > 1:
         t = torch.tensor([total_s], device="cuda")

@@ -68,3 +68,39 @@ def test_residual_judge_after_4_sweeps_rejects_a_start_that_finishes_first(oracl
     mi, mp, mj = np.mean(inertial), np.mean(prev), np.mean(judged)
     assert mp < 0.9 * mi, (mp, mi)       # the previous offset finishes first
     assert mj > mp + 0.5 * (mi - mp), (mj, mp, mi)   # the judge keeps less than half of that gain
+
+
+def test_always_keeping_the_previous_offset_is_unstable_in_closed_loop(oracle):
+    # The same kind of cloth when every frame starts from the previous
+    # frame's offset and the trajectory continues from that solve (stopped at
+    # 1e-2).  A solve stopped at a tolerance leaves error in the direction of
+    # its start: from the inertial start the offset comes out too small and
+    # the cloth loses energy; from the previous offset it repeats the last
+    # frame's internal force and the cloth gains energy.  Within 20 frames
+    # the cloth (which the wind accelerates either way) runs to more than
+    # twice the inertial trajectory's peak speed and its frames stop
+    # converging, while the inertial start's trajectory stays converged.
+    import scenes
+    p = scenes.batch_params(3, seed=7, n_range=(17, 33))[2]
+    pos, tris, _ = oracle.hanging_cloth(p["n"], p["size"], seed=p["mesh_seed"])
+    sc = oracle.Scene(pos, tris, k_stretch=p["ks"], k_bend=p["kb"], pins=p["pins"], h=1 / 60, gravity=-9.81,
+                      wind=tuple(p["wind"]))
+    out = {}
+    for mode in ("inertial", "previous"):
+        x = pos.astype(np.float64).reshape(-1); v = np.zeros_like(x); d1 = None
+        speeds, failed = [], 0
+        for f in range(20):
+            y = sc.predict(x, v)
+            if mode == "previous" and d1 is not None:
+                xa, va, info = sc.step_jacobi(x, v, 200, tol=1e-2, rho=0.99, init=2, x0=y + d1)
+            else:
+                xa, va, info = sc.step_jacobi(x, v, 200, tol=1e-2, rho=0.99)
+            failed += int(info["res"][-1] > 1e-2 * info["res_y"])
+            d1 = xa - y
+            x, v = xa, va
+            speeds.append(np.abs(v).max())
+        out[mode] = (speeds, failed)
+    si, fi = out["inertial"]
+    sp, fp = out["previous"]
+    assert fi == 0, fi
+    assert fp >= 2 and max(sp) > 2 * max(si), (fp, max(sp), max(si))
