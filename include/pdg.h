@@ -44,7 +44,10 @@ extern "C" {
 #define PDG_INIT_WARMSTART 2  /* the learned prediction, kept only if its
                                  residual is below the inertial start's     */
 #define PDG_INIT_WARMSTART_KEEP 3  /* the learned prediction, always kept (no
-                                 residual judge; for evaluating the network) */
+                                 residual judge; for evaluating the network:
+                                 a trajectory that always keeps a prediction
+                                 close to the previous frame's offset gains
+                                 energy when its frames stop at a tolerance) */
 
 /* Launch structure of the iteration loop. */
 #define PDG_KERNEL_AUTO       0  /* resident when it fits, else the streaming
