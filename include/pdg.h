@@ -255,7 +255,9 @@ int  pdg_solver_set_tolerance(pdg_solver* s, int cloth, float tolerance);
  * + upload_to_gpu, src/constraints.cpp:14-22 and 77-101): idx P distinct
  * vertex indices of the cloth, targets P*3 (NULL = rest positions).  The
  * patch layout does not depend on the pins; only the per-vertex records
- * change. */
+ * change.  An attached network reads the new pins from the next frame on;
+ * its energy-norm loss weights (training only) keep the old ones until it is
+ * attached again. */
 int  pdg_solver_set_pins(pdg_solver* s, int cloth, const int* idx, int P, const float* targets);
 /* Move the pins of one cloth (Constraints::target_positions). */
 int  pdg_solver_set_pin_targets(pdg_solver* s, int cloth, const float* targets);
