@@ -116,25 +116,32 @@ int alloc_graph(pdg_warmstart* w, int N, int E)
     return PDG_OK;
 }
 
-int forward(pdg_warmstart* w, cudaStream_t st)
+// The network on the current features.  `train` keeps what the backward
+// pass needs (the update's ReLU output per layer); inference skips it.
+int forward(pdg_warmstart* w, cudaStream_t st, bool train)
 {
-    const int N = w->N, gb = nb(N, 64);
+    const int N = w->N;
     const Layout& y = w->lay;
     const float* p = w->p.p;
-    k_gemm<bf16, NFP, H, EPI_RELU | EPI_STORE1><<<gb, 128, 0, st>>>(w->xin.p, NFP, N, w->W.We, p + y.be, nullptr, 0,
-                                                                    w->cat[0].p, 2 * H, nullptr, 0, nullptr, 0);
+    gemm<bf16, NFP, H, EPI_RELU | EPI_STORE1>(st, w->xin.p, NFP, N, w->W.We, p + y.be, nullptr, 0, w->cat[0].p, 2 * H,
+                                              nullptr, 0, nullptr, 0);
     for (int l = 0; l < L; ++l) {
-        k_gemm<bf16, H, 2 * H, EPI_STORE1><<<gb, 128, 0, st>>>(w->cat[l].p, 2 * H, N, w->W.AB[l], nullptr, nullptr, 0,
-                                                               w->pq[l].p, 2 * H, nullptr, 0, nullptr, 0);
-        k_msg_fwd<<<nb((long long)N * 32, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->ef.p, w->deg_inv.p, w->pq[l].p,
+        gemm<bf16, H, 2 * H, EPI_STORE1>(st, w->cat[l].p, 2 * H, N, w->W.AB[l], nullptr, nullptr, 0, w->pq[l].p, 2 * H,
+                                         nullptr, 0, nullptr, 0);
+        k_msg_fwd<<<msg_grid(N), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->ef.p, w->deg_inv.p, w->pq[l].p,
                                                              p + y.C[l], p + y.c[l], w->cat[l].p);
         bf16* next = l + 1 < L ? w->cat[l + 1].p : w->hfin.p;
         const int ldn = l + 1 < L ? 2 * H : H;
-        k_gemm<bf16, 2 * H, H, EPI_RELU | EPI_STORE1 | EPI_RESID2><<<gb, 128, 0, st>>>(
-            w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l], w->cat[l].p, 2 * H, w->uo[l].p, H, next, ldn, nullptr, 0);
+        if (train)
+            gemm<bf16, 2 * H, H, EPI_RELU | EPI_STORE1 | EPI_RESID2>(st, w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l],
+                                                                     w->cat[l].p, 2 * H, w->uo[l].p, H, next, ldn,
+                                                                     nullptr, 0);
+        else
+            gemm<bf16, 2 * H, H, EPI_RELU | EPI_RESID2>(st, w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l], w->cat[l].p,
+                                                        2 * H, nullptr, 0, next, ldn, nullptr, 0);
     }
-    k_gemm<bf16, H, 16, EPI_STOREF><<<gb, 128, 0, st>>>(w->hfin.p, H, N, w->W.Wd, w->bdp.p, nullptr, 0, nullptr, 0,
-                                                        nullptr, 0, w->out.p, 16);
+    gemm<bf16, H, 16, EPI_STOREF>(st, w->hfin.p, H, N, w->W.Wd, w->bdp.p, nullptr, 0, nullptr, 0, nullptr, 0,
+                                  w->out.p, 16);
     GK(cudaGetLastError());
     return PDG_OK;
 }
@@ -157,7 +164,7 @@ void wgrad(pdg_warmstart* w, const TY* dY, int ldy, int nout, const TX* X, int l
 // (null: 1)
 int backward(pdg_warmstart* w, float inv_cnt, const float* ew, cudaStream_t st)
 {
-    const int N = w->N, gb = nb(N, 64);
+    const int N = w->N;
     const Layout& y = w->lay;
     const float* p = w->p.p;
     float* g = w->g.p;
@@ -166,21 +173,21 @@ int backward(pdg_warmstart* w, float inv_cnt, const float* ew, cudaStream_t st)
     k_loss<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, w->target.p, w->freew.p, w->ptr.p, w->adj.p, ew, w->smooth,
                                        inv_cnt, w->dout.p, w->loss.p);
     wgrad<float, bf16>(w, w->dout.p, 16, NO, w->hfin.p, H, H, N, g + y.Wd, g + y.bd, st);
-    k_gemm<float, 16, H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dout.p, 16, N, w->W.Wdt, nullptr, nullptr, 0, nullptr, 0,
-                                                         nullptr, 0, w->dh.p, H);
+    gemm<float, 16, H, EPI_STOREF>(st, w->dout.p, 16, N, w->W.Wdt, nullptr, nullptr, 0, nullptr, 0, nullptr, 0, w->dh.p,
+                                   H);
     for (int l = L - 1; l >= 0; --l) {
         k_relu_bwd<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dh.p, H, w->uo[l].p, H, w->dtmp.p, H);
         wgrad<float, bf16>(w, w->dtmp.p, H, H, w->cat[l].p, 2 * H, 2 * H, N, g + y.U[l], g + y.u[l], st);
-        k_gemm<float, H, 2 * H, EPI_STOREF><<<gb, 128, 0, st>>>(w->dtmp.p, H, N, w->W.Ut[l], nullptr, nullptr, 0,
-                                                                nullptr, 0, nullptr, 0, w->dcat.p, 2 * H);
+        gemm<float, H, 2 * H, EPI_STOREF>(st, w->dtmp.p, H, N, w->W.Ut[l], nullptr, nullptr, 0, nullptr, 0, nullptr, 0,
+                                          w->dcat.p, 2 * H);
         k_add<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dcat.p, 2 * H, w->dh.p, H);
         const int gm = std::max(1, std::min(kMsgBwdBlocks, nb(N, 8)));
         k_msg_bwd<<<gm, 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rev.p, w->ef.p, w->deg_inv.p, w->pq[l].p, p + y.C[l],
                                       p + y.c[l], w->dcat.p, w->dpq.p, w->part.p);
         k_sum_parts<<<nb(H * (EF + 1), 256), 256, 0, st>>>(w->part.p, gm, H * EF, H, g + y.C[l], g + y.c[l]);
         wgrad<float, bf16>(w, w->dpq.p, 2 * H, 2 * H, w->cat[l].p, 2 * H, H, N, g + y.A[l], nullptr, st);
-        k_gemm<float, 2 * H, H, EPI_ACCF><<<gb, 128, 0, st>>>(w->dpq.p, 2 * H, N, w->W.ABt[l], nullptr, nullptr, 0,
-                                                              nullptr, 0, nullptr, 0, w->dh.p, H);
+        gemm<float, 2 * H, H, EPI_ACCF>(st, w->dpq.p, 2 * H, N, w->W.ABt[l], nullptr, nullptr, 0, nullptr, 0, nullptr, 0,
+                                        w->dh.p, H);
     }
     k_relu_bwd<<<nb((long long)N * H, 256), 256, 0, st>>>(N, H, w->dh.p, H, w->cat[0].p, 2 * H, w->dtmp.p, H);
     wgrad<float, bf16>(w, w->dtmp.p, H, H, w->xin.p, NFP, NF, N, g + y.We, g + y.be, st);
@@ -246,7 +253,7 @@ int warm_infer_enqueue(pdg_warmstart* w, pdg_solver* s)
     k_node_feat<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->V.p, s->Y.p, s->aux.p, w->stat.p, s->vcloth.p, s->cinfo.p,
                                             s->dprev.p, w->xin.p);
     k_edge_feat<<<nb(N, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rest.p, s->Y.p, w->ef.p);
-    const int rc = forward(w, st);
+    const int rc = forward(w, st, false);
     if (rc) return rc;
     k_warm_out<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, s->A.p, s->dprev.p, s->warm.p);
     GK(cudaGetLastError());
@@ -353,7 +360,7 @@ int pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr, 
     if (ew && E) GK(cudaMemcpyAsync(w->ew.p, ew, sizeof(float) * E, cudaMemcpyHostToDevice, st));
     double cnt = 0.0;
     for (int i = 0; i < N; ++i) cnt += freew[i] > 0.f ? 3.0 : 0.0;
-    rc = forward(w, st);
+    rc = forward(w, st, true);
     if (rc) return rc;
     rc = backward(w, (float)(1.0 / std::max(cnt, 1.0)), (ew && E) ? w->ew.p : nullptr, st);
     if (rc) return rc;
@@ -478,7 +485,7 @@ int pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* 
     k_target<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->Y.p, s->aux.p, w->Dn.p, w->target.p, w->freew.p);
     int nfree = 0;
     for (const auto& a : s->L.aux) nfree += a.w >= 0.f ? 1 : 0;
-    rc = forward(w, st);
+    rc = forward(w, st, true);
     if (rc) return rc;
     rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), w->energy ? w->ew.p : nullptr, st);
     if (rc) return rc;
@@ -527,7 +534,7 @@ int pdg_warmstart_train_pair(pdg_warmstart* w, pdg_solver* traj, pdg_solver* dee
     k_target<<<nb(N, 256), 256, 0, st>>>(N, deep->X.p, traj->Y.p, traj->aux.p, w->Dn.p, w->target.p, w->freew.p);
     int nfree = 0;
     for (const auto& a : traj->L.aux) nfree += a.w >= 0.f ? 1 : 0;
-    rc = forward(w, st);
+    rc = forward(w, st, true);
     if (rc) return rc;
     rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), w->energy ? w->ew.p : nullptr, st);
     if (rc) return rc;

@@ -17,6 +17,7 @@
 #include "gnn.cuh"
 #include "pdg_solver.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -47,9 +48,11 @@ __device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uin
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// Y[M x NOUT] = X[M x K] W^T (+ bias), W stored [NOUT][K] bf16.  Each warp
-// computes 16 rows; W is staged in shared memory with a padded row stride
-// (K + 8 elements) so the B-fragment loads are bank-conflict free.
+// Y[M x NOUT] = X[M x K] W^T (+ bias), W stored [NOUT][K] bf16.  A block
+// stages W (with a padded row stride of K + 8 elements, so the B-fragment
+// loads are bank-conflict free) and the bias in shared memory once, in
+// 16-byte pieces, and its warps then walk 16-row tiles with a grid stride
+// (gemm_grid sizes the grid to the resident blocks).
 // Epilogue: optional ReLU; Y1 <- bf16(v); Y2 <- bf16(R + v); Yf <- v or += v.
 template <typename TA, int K, int NOUT, int EPI>
 __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx, int M, const bf16* __restrict__ W,
@@ -57,56 +60,97 @@ __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx,
                                               bf16* __restrict__ Y1, int ld1, bf16* __restrict__ Y2, int ld2,
                                               float* __restrict__ Yf, int ldf)
 {
+    static_assert(K % 16 == 0 && NOUT % 8 == 0, "mma tile shape");
     __shared__ __align__(16) bf16 sW[NOUT * (K + 8)];
-    for (int i = threadIdx.x; i < NOUT * K; i += 128) sW[(i / K) * (K + 8) + i % K] = W[i];
+    __shared__ float sb[NOUT];
+    for (int i = threadIdx.x; i < NOUT * K / 8; i += 128) {
+        const int r = i / (K / 8), c = (i % (K / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW + r * (K + 8) + c) = *reinterpret_cast<const uint4*>(W + (size_t)r * K + c);
+    }
+    for (int i = threadIdx.x; i < NOUT; i += 128) sb[i] = bias ? bias[i] : 0.f;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int r0 = (blockIdx.x * 4 + warp) * 16;
-    if (r0 >= M) return;
-    float acc[NOUT / 8][4];
-    #pragma unroll
-    for (int n = 0; n < NOUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
-    const bool ok0 = r0 + g < M, ok1 = r0 + g + 8 < M;
-    const TA* x0 = X + (size_t)(r0 + g) * ldx;
-    const TA* x1 = X + (size_t)(r0 + g + 8) * ldx;
-    #pragma unroll
-    for (int ks = 0; ks < K / 16; ++ks) {
-        const int c0 = ks * 16 + 2 * t;
-        const uint32_t a0 = ok0 ? ld_pair(x0 + c0) : 0u;
-        const uint32_t a1 = ok1 ? ld_pair(x1 + c0) : 0u;
-        const uint32_t a2 = ok0 ? ld_pair(x0 + c0 + 8) : 0u;
-        const uint32_t a3 = ok1 ? ld_pair(x1 + c0 + 8) : 0u;
+    const int ntile = (M + 15) >> 4;
+    for (int tile = blockIdx.x * 4 + warp; tile < ntile; tile += gridDim.x * 4) {
+        const int r0 = tile * 16;
+        float acc[NOUT / 8][4];
         #pragma unroll
-        for (int n = 0; n < NOUT / 8; ++n) {
-            const bf16* wr = sW + (n * 8 + g) * (K + 8) + c0;
-            mma_bf16(acc[n], a0, a1, a2, a3, *reinterpret_cast<const uint32_t*>(wr),
-                     *reinterpret_cast<const uint32_t*>(wr + 8));
+        for (int n = 0; n < NOUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+        const bool ok0 = r0 + g < M, ok1 = r0 + g + 8 < M;
+        const TA* x0 = X + (size_t)(r0 + g) * ldx;
+        const TA* x1 = X + (size_t)(r0 + g + 8) * ldx;
+        uint32_t a[K / 16][4];
+        #pragma unroll
+        for (int ks = 0; ks < K / 16; ++ks) {
+            const int c0 = ks * 16 + 2 * t;
+            a[ks][0] = ok0 ? ld_pair(x0 + c0) : 0u;
+            a[ks][1] = ok1 ? ld_pair(x1 + c0) : 0u;
+            a[ks][2] = ok0 ? ld_pair(x0 + c0 + 8) : 0u;
+            a[ks][3] = ok1 ? ld_pair(x1 + c0 + 8) : 0u;
         }
+        #pragma unroll
+        for (int ks = 0; ks < K / 16; ++ks) {
+            const int c0 = ks * 16 + 2 * t;
+            #pragma unroll
+            for (int n = 0; n < NOUT / 8; ++n) {
+                const bf16* wr = sW + (n * 8 + g) * (K + 8) + c0;
+                mma_bf16(acc[n], a[ks][0], a[ks][1], a[ks][2], a[ks][3], *reinterpret_cast<const uint32_t*>(wr),
+                         *reinterpret_cast<const uint32_t*>(wr + 8));
+            }
+        }
+        #pragma unroll
+        for (int n = 0; n < NOUT / 8; ++n)
+            #pragma unroll
+            for (int hf = 0; hf < 2; ++hf) {
+                const int row = r0 + g + 8 * hf;
+                if (row >= M) continue;
+                const int col = n * 8 + 2 * t;
+                float v0 = acc[n][2 * hf], v1 = acc[n][2 * hf + 1];
+                if (bias) { v0 += sb[col]; v1 += sb[col + 1]; }
+                if (EPI & EPI_RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                if (EPI & EPI_STORE1)
+                    *reinterpret_cast<__nv_bfloat162*>(Y1 + (size_t)row * ld1 + col) = __floats2bfloat162_rn(v0, v1);
+                if (EPI & EPI_RESID2) {
+                    const __nv_bfloat162 r = *reinterpret_cast<const __nv_bfloat162*>(R + (size_t)row * ldr + col);
+                    *reinterpret_cast<__nv_bfloat162*>(Y2 + (size_t)row * ld2 + col) =
+                        __floats2bfloat162_rn(__bfloat162float(r.x) + v0, __bfloat162float(r.y) + v1);
+                }
+                if (EPI & EPI_STOREF) *reinterpret_cast<float2*>(Yf + (size_t)row * ldf + col) = make_float2(v0, v1);
+                if (EPI & EPI_ACCF) {
+                    float2* p = reinterpret_cast<float2*>(Yf + (size_t)row * ldf + col);
+                    const float2 o = *p;
+                    *p = make_float2(o.x + v0, o.y + v1);
+                }
+            }
     }
-    #pragma unroll
-    for (int n = 0; n < NOUT / 8; ++n)
-        #pragma unroll
-        for (int hf = 0; hf < 2; ++hf) {
-            const int row = r0 + g + 8 * hf;
-            if (row >= M) continue;
-            const int col = n * 8 + 2 * t;
-            float v0 = acc[n][2 * hf], v1 = acc[n][2 * hf + 1];
-            if (bias) { v0 += bias[col]; v1 += bias[col + 1]; }
-            if (EPI & EPI_RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
-            if (EPI & EPI_STORE1)
-                *reinterpret_cast<__nv_bfloat162*>(Y1 + (size_t)row * ld1 + col) = __floats2bfloat162_rn(v0, v1);
-            if (EPI & EPI_RESID2) {
-                const __nv_bfloat162 r = *reinterpret_cast<const __nv_bfloat162*>(R + (size_t)row * ldr + col);
-                *reinterpret_cast<__nv_bfloat162*>(Y2 + (size_t)row * ld2 + col) =
-                    __floats2bfloat162_rn(__bfloat162float(r.x) + v0, __bfloat162float(r.y) + v1);
-            }
-            if (EPI & EPI_STOREF) *reinterpret_cast<float2*>(Yf + (size_t)row * ldf + col) = make_float2(v0, v1);
-            if (EPI & EPI_ACCF) {
-                float2* p = reinterpret_cast<float2*>(Yf + (size_t)row * ldf + col);
-                const float2 o = *p;
-                *p = make_float2(o.x + v0, o.y + v1);
-            }
-        }
+}
+
+// Grid of k_gemm for M rows: enough blocks for every row tile, at most the
+// blocks that are resident at once on this device.
+template <typename TA, int K, int NOUT, int EPI>
+int gemm_grid(int M)
+{
+    static int resident[16] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& r = resident[dev & 15];
+    if (r == 0) {
+        int nsm = 0, per = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gemm<TA, K, NOUT, EPI>, 128, 0);
+        r = std::max(1, nsm * std::max(per, 1));
+    }
+    const int need = (((M + 15) >> 4) + 3) / 4;
+    return std::max(1, std::min(need, r));
+}
+
+// Launch of k_gemm on `st` with the grid above.
+template <typename TA, int K, int NOUT, int EPI>
+void gemm(cudaStream_t st, const TA* X, int ldx, int M, const bf16* W, const float* bias, const bf16* R, int ldr,
+          bf16* Y1, int ld1, bf16* Y2, int ld2, float* Yf, int ldf)
+{
+    k_gemm<TA, K, NOUT, EPI><<<gemm_grid<TA, K, NOUT, EPI>(M), 128, 0, st>>>(X, ldx, M, W, bias, R, ldr, Y1, ld1, Y2,
+                                                                            ld2, Yf, ldf);
 }
 
 __device__ __forceinline__ float tofloat(float v) { return v; }
@@ -177,31 +221,113 @@ __global__ void k_sum_parts(const float* __restrict__ part, int nblocks, int nw,
     if (i < nw) dW[i] = s; else db[i - nw] = s;
 }
 
-// Messages of layer l, warp per node, lane owns channels 2*lane, 2*lane+1:
-// a_i = deg_inv_i * sum_j relu(P_i + Q_j + C e_ij + c), written to cat[:, H:2H].
-__global__ void k_msg_fwd(int N, const int* __restrict__ ptr, const int* __restrict__ adj,
-                          const float4* __restrict__ ef, const float* __restrict__ deg_inv,
-                          const bf16* __restrict__ PQ, const float* __restrict__ C, const float* __restrict__ cb,
-                          bf16* __restrict__ cat)
+// Messages of layer l:
+//   a_i = deg_inv_i * sum_j relu(P_i + Q_j + C e_ij + c), written to cat[:, H:2H].
+// Half a warp per node, lane s of a half owning channels 4s..4s+3; each warp
+// walks pairs of nodes with a grid stride (msg_grid sizes the grid to the
+// resident blocks).  A half reads its node's neighbour indices 16 at a time,
+// one per lane, and broadcasts them by shuffles; the Q rows and edge
+// features of two edges are loaded before either is summed, so their
+// latencies overlap.  Each node sums its edges in list order, one at a time;
+// channel pairs go through the two-lane fp32 instructions, which round each
+// lane like the scalar add and fused multiply-add.
+__global__ void __launch_bounds__(256) k_msg_fwd(int N, const int* __restrict__ ptr, const int* __restrict__ adj,
+                                                 const float4* __restrict__ ef, const float* __restrict__ deg_inv,
+                                                 const bf16* __restrict__ PQ, const float* __restrict__ C,
+                                                 const float* __restrict__ cb, bf16* __restrict__ cat)
 {
-    const int node = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (node >= N) return;
-    const int ch = 2 * lane;
-    const float2 P = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)node * 2 * H + ch));
-    const float4 C0 = *reinterpret_cast<const float4*>(C + ch * EF), C1 = *reinterpret_cast<const float4*>(C + (ch + 1) * EF);
-    const float c0 = cb[ch], c1 = cb[ch + 1];
-    float s0 = 0.f, s1 = 0.f;
-    for (int e = ptr[node]; e < ptr[node + 1]; ++e) {
-        const int j = adj[e];
-        const float4 f = ef[e];
-        const float2 Q = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(PQ + (size_t)j * 2 * H + H + ch));
-        const float z0 = P.x + Q.x + C0.x * f.x + C0.y * f.y + C0.z * f.z + C0.w * f.w + c0;
-        const float z1 = P.y + Q.y + C1.x * f.x + C1.y * f.y + C1.z * f.z + C1.w * f.w + c1;
-        s0 += fmaxf(z0, 0.f);
-        s1 += fmaxf(z1, 0.f);
+    const unsigned full = 0xffffffffu;
+    const int s = threadIdx.x & 15, ch = 4 * s;
+    float4 Cw[4];
+    float cv[4];
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) { Cw[k] = *reinterpret_cast<const float4*>(C + (ch + k) * EF); cv[k] = cb[ch + k]; }
+    const int npair = (N + 1) >> 1, stride = gridDim.x * (blockDim.x >> 5);
+    // the pair index is the same for the whole warp, so every lane takes
+    // part in every shuffle below
+    for (int pair = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; pair < npair; pair += stride) {
+        const int node = 2 * pair + ((threadIdx.x >> 4) & 1);
+        const bool live = node < N;
+        int e0 = 0, deg = 0;
+        float P[4] = {0.f, 0.f, 0.f, 0.f};
+        if (live) {
+            e0 = ptr[node];
+            deg = ptr[node + 1] - e0;
+            const uint2 pr = *reinterpret_cast<const uint2*>(PQ + (size_t)node * 2 * H + ch);
+            const float2 p01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&pr.x));
+            const float2 p23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&pr.y));
+            P[0] = p01.x; P[1] = p01.y; P[2] = p23.x; P[3] = p23.y;
+        }
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        // steps over the larger degree of the warp's two nodes
+        const int dmax = max(deg, __shfl_xor_sync(full, deg, 16));
+        for (int base = 0; base < dmax; base += 16) {
+            const int n = deg - base;   // edges of this node left (may be <= 0)
+            const int jl = s < n ? adj[e0 + base + s] : 0;
+            const int m = min(16, dmax - base);
+            for (int t0 = 0; t0 < m; t0 += 2) {
+                int j[2];
+                uint2 qr[2];
+                float4 f[2];
+                #pragma unroll
+                for (int u = 0; u < 2; ++u) j[u] = __shfl_sync(full, jl, (t0 + u) & 15, 16);
+                #pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const bool ok = t0 + u < n;
+                    qr[u] = ok ? *reinterpret_cast<const uint2*>(PQ + (size_t)j[u] * 2 * H + H + ch) : make_uint2(0u, 0u);
+                    f[u] = ok ? ef[e0 + base + t0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                #pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    if (t0 + u < n) {
+                        const float2 q01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&qr[u].x));
+                        const float2 q23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&qr[u].y));
+                        float2 z01 = __fadd2_rn(make_float2(P[0], P[1]), q01);
+                        float2 z23 = __fadd2_rn(make_float2(P[2], P[3]), q23);
+                        z01 = __ffma2_rn(make_float2(Cw[0].x, Cw[1].x), make_float2(f[u].x, f[u].x), z01);
+                        z23 = __ffma2_rn(make_float2(Cw[2].x, Cw[3].x), make_float2(f[u].x, f[u].x), z23);
+                        z01 = __ffma2_rn(make_float2(Cw[0].y, Cw[1].y), make_float2(f[u].y, f[u].y), z01);
+                        z23 = __ffma2_rn(make_float2(Cw[2].y, Cw[3].y), make_float2(f[u].y, f[u].y), z23);
+                        z01 = __ffma2_rn(make_float2(Cw[0].z, Cw[1].z), make_float2(f[u].z, f[u].z), z01);
+                        z23 = __ffma2_rn(make_float2(Cw[2].z, Cw[3].z), make_float2(f[u].z, f[u].z), z23);
+                        z01 = __ffma2_rn(make_float2(Cw[0].w, Cw[1].w), make_float2(f[u].w, f[u].w), z01);
+                        z23 = __ffma2_rn(make_float2(Cw[2].w, Cw[3].w), make_float2(f[u].w, f[u].w), z23);
+                        z01 = __fadd2_rn(z01, make_float2(cv[0], cv[1]));
+                        z23 = __fadd2_rn(z23, make_float2(cv[2], cv[3]));
+                        const float2 a01 =
+                            __fadd2_rn(make_float2(acc[0], acc[1]), make_float2(fmaxf(z01.x, 0.f), fmaxf(z01.y, 0.f)));
+                        const float2 a23 =
+                            __fadd2_rn(make_float2(acc[2], acc[3]), make_float2(fmaxf(z23.x, 0.f), fmaxf(z23.y, 0.f)));
+                        acc[0] = a01.x; acc[1] = a01.y; acc[2] = a23.x; acc[3] = a23.y;
+                    }
+                }
+            }
+        }
+        if (live) {
+            const float di = deg_inv[node];
+            __nv_bfloat162 o[2] = {__floats2bfloat162_rn(acc[0] * di, acc[1] * di),
+                                   __floats2bfloat162_rn(acc[2] * di, acc[3] * di)};
+            *reinterpret_cast<uint2*>(cat + (size_t)node * 2 * H + H + ch) = *reinterpret_cast<const uint2*>(o);
+        }
     }
-    const float di = deg_inv[node];
-    *reinterpret_cast<__nv_bfloat162*>(cat + (size_t)node * 2 * H + H + ch) = __floats2bfloat162_rn(s0 * di, s1 * di);
+}
+
+// Grid of k_msg_fwd for N nodes: one warp per pair of nodes, at most the
+// blocks that are resident at once on this device.
+inline int msg_grid(int N)
+{
+    static int resident[16] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& r = resident[dev & 15];
+    if (r == 0) {
+        int nsm = 0, per = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_msg_fwd, 256, 0);
+        r = std::max(1, nsm * std::max(per, 1));
+    }
+    const int need = (((N + 1) >> 1) + 7) / 8;
+    return std::max(1, std::min(need, r));
 }
 
 // Backward of the messages: dP_i = sum_j g_ij, dQ_j = sum_i g_ij with
