@@ -116,9 +116,11 @@ int alloc_graph(pdg_warmstart* w, int N, int E)
     return PDG_OK;
 }
 
-// The network on the current features.  `train` keeps what the backward
-// pass needs (the update's ReLU output per layer); inference skips it.
-int forward(pdg_warmstart* w, cudaStream_t st, bool train)
+// The network on the current features for training: every activation the
+// backward pass needs is kept (h and a per layer, P and Q, the update's ReLU
+// output, the last h and the decoder output).  Inference runs the fused
+// kernels instead (warm_infer_enqueue), with bitwise the same start offsets.
+int forward(pdg_warmstart* w, cudaStream_t st)
 {
     const int N = w->N;
     const Layout& y = w->lay;
@@ -132,13 +134,10 @@ int forward(pdg_warmstart* w, cudaStream_t st, bool train)
                                                              p + y.C[l], p + y.c[l], w->cat[l].p);
         bf16* next = l + 1 < L ? w->cat[l + 1].p : w->hfin.p;
         const int ldn = l + 1 < L ? 2 * H : H;
-        if (train)
-            gemm<bf16, 2 * H, H, EPI_RELU | EPI_STORE1 | EPI_RESID2>(st, w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l],
-                                                                     w->cat[l].p, 2 * H, w->uo[l].p, H, next, ldn,
-                                                                     nullptr, 0);
-        else
-            gemm<bf16, 2 * H, H, EPI_RELU | EPI_RESID2>(st, w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l], w->cat[l].p,
-                                                        2 * H, nullptr, 0, next, ldn, nullptr, 0);
+        // h <- h + relu(U [h; a] + u): the residual h is the A operand's
+        // first H columns
+        gemm<bf16, 2 * H, H, EPI_RELU | EPI_STORE1 | EPI_RESIDA>(st, w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l],
+                                                                 nullptr, 0, w->uo[l].p, H, next, ldn, nullptr, 0);
     }
     gemm<bf16, H, 16, EPI_STOREF>(st, w->hfin.p, H, N, w->W.Wd, w->bdp.p, nullptr, 0, nullptr, 0, nullptr, 0,
                                   w->out.p, 16);
@@ -253,14 +252,30 @@ int warm_infer_enqueue(pdg_warmstart* w, pdg_solver* s)
     k_node_feat<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->V.p, s->Y.p, s->aux.p, w->stat.p, s->vcloth.p, s->cinfo.p,
                                             s->dprev.p, w->xin.p);
     k_edge_feat<<<nb(N, 256), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->rest.p, s->Y.p, w->ef.p);
-    const int rc = forward(w, st, false);
-    if (rc) return rc;
-    k_warm_out<<<nb(N, 256), 256, 0, st>>>(N, w->out.p, s->A.p, s->dprev.p, s->warm.p);
+    // encoder + layer 0's P, Q; per layer the messages, then the update fused
+    // with the next layer's P, Q or, after the last layer, with the decoder
+    // and the start offsets
+    const Layout& y = w->lay;
+    const float* p = w->p.p;
+    fused<FUSE_ENC_PQ>(st, w->xin.p, NFP, N, w->W.We, p + y.be, w->W.AB[0], nullptr, w->cat[0].p, 2 * H, w->pq[0].p,
+                       nullptr, nullptr, nullptr);
+    for (int l = 0; l < L; ++l) {
+        k_msg_fwd<<<msg_grid(N), 256, 0, st>>>(N, w->ptr.p, w->adj.p, w->ef.p, w->deg_inv.p, w->pq[l].p, p + y.C[l],
+                                              p + y.c[l], w->cat[l].p);
+        if (l + 1 < L)
+            fused<FUSE_UPD_PQ>(st, w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l], w->W.AB[l + 1], nullptr,
+                               w->cat[l + 1].p, 2 * H, w->pq[l + 1].p, nullptr, nullptr, nullptr);
+        else
+            fused<FUSE_UPD_OUT>(st, w->cat[l].p, 2 * H, N, w->W.U[l], p + y.u[l], w->W.Wd, w->bdp.p, nullptr, 0,
+                                nullptr, s->A.p, s->dprev.p, s->warm.p);
+    }
     GK(cudaGetLastError());
     return PDG_OK;
 }
 
-int warm_kernel_count() { return 3 + 1 + 3 * L + 1; }
+// launches of one warm_infer_enqueue: features (2), encoder, per layer the
+// messages and the fused update
+int warm_kernel_count() { return 3 + 2 * L; }
 
 void warm_detach(pdg_warmstart* w)
 {
@@ -360,7 +375,7 @@ int pdg_warmstart_eval(pdg_warmstart* w, int N, const float* x, const int* ptr, 
     if (ew && E) GK(cudaMemcpyAsync(w->ew.p, ew, sizeof(float) * E, cudaMemcpyHostToDevice, st));
     double cnt = 0.0;
     for (int i = 0; i < N; ++i) cnt += freew[i] > 0.f ? 3.0 : 0.0;
-    rc = forward(w, st, true);
+    rc = forward(w, st);
     if (rc) return rc;
     rc = backward(w, (float)(1.0 / std::max(cnt, 1.0)), (ew && E) ? w->ew.p : nullptr, st);
     if (rc) return rc;
@@ -485,7 +500,7 @@ int pdg_warmstart_train_frame(pdg_warmstart* w, pdg_solver* s, float lr, float* 
     k_target<<<nb(N, 256), 256, 0, st>>>(N, s->X.p, s->Y.p, s->aux.p, w->Dn.p, w->target.p, w->freew.p);
     int nfree = 0;
     for (const auto& a : s->L.aux) nfree += a.w >= 0.f ? 1 : 0;
-    rc = forward(w, st, true);
+    rc = forward(w, st);
     if (rc) return rc;
     rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), w->energy ? w->ew.p : nullptr, st);
     if (rc) return rc;
@@ -534,7 +549,7 @@ int pdg_warmstart_train_pair(pdg_warmstart* w, pdg_solver* traj, pdg_solver* dee
     k_target<<<nb(N, 256), 256, 0, st>>>(N, deep->X.p, traj->Y.p, traj->aux.p, w->Dn.p, w->target.p, w->freew.p);
     int nfree = 0;
     for (const auto& a : traj->L.aux) nfree += a.w >= 0.f ? 1 : 0;
-    rc = forward(w, st, true);
+    rc = forward(w, st);
     if (rc) return rc;
     rc = backward(w, 1.f / (float)std::max(1, 3 * nfree), w->energy ? w->ew.p : nullptr, st);
     if (rc) return rc;

@@ -28,7 +28,7 @@ namespace gnn {
 
 using bf16 = __nv_bfloat16;
 
-enum { EPI_RELU = 1, EPI_STORE1 = 2, EPI_RESID2 = 4, EPI_STOREF = 8, EPI_ACCF = 16 };
+enum { EPI_RELU = 1, EPI_STORE1 = 2, EPI_RESID2 = 4, EPI_STOREF = 8, EPI_ACCF = 16, EPI_RESIDA = 32 };
 
 __device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 __device__ __forceinline__ uint32_t ld_pair(const float* p)
@@ -53,7 +53,8 @@ __device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uin
 // loads are bank-conflict free) and the bias in shared memory once, in
 // 16-byte pieces, and its warps then walk 16-row tiles with a grid stride
 // (gemm_grid sizes the grid to the resident blocks).
-// Epilogue: optional ReLU; Y1 <- bf16(v); Y2 <- bf16(R + v); Yf <- v or += v.
+// Epilogue: optional ReLU; Y1 <- bf16(v); Y2 <- bf16(R + v) (R read, or taken
+// from the A fragments when it is X's first NOUT columns); Yf <- v or += v.
 template <typename TA, int K, int NOUT, int EPI>
 __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx, int M, const bf16* __restrict__ W,
                                               const float* __restrict__ bias, const bf16* __restrict__ R, int ldr,
@@ -61,6 +62,7 @@ __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx,
                                               float* __restrict__ Yf, int ldf)
 {
     static_assert(K % 16 == 0 && NOUT % 8 == 0, "mma tile shape");
+    static_assert(!(EPI & EPI_RESIDA) || NOUT <= K, "the residual is part of the A operand");
     __shared__ __align__(16) bf16 sW[NOUT * (K + 8)];
     __shared__ float sb[NOUT];
     for (int i = threadIdx.x; i < NOUT * K / 8; i += 128) {
@@ -70,24 +72,33 @@ __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx,
     for (int i = threadIdx.x; i < NOUT; i += 128) sb[i] = bias ? bias[i] : 0.f;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int ntile = (M + 15) >> 4;
-    for (int tile = blockIdx.x * 4 + warp; tile < ntile; tile += gridDim.x * 4) {
-        const int r0 = tile * 16;
-        float acc[NOUT / 8][4];
-        #pragma unroll
-        for (int n = 0; n < NOUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+    const int ntile = (M + 15) >> 4, stride = gridDim.x * 4;
+    // A fragments of row tile `tl` (zero rows past M)
+    auto load_a = [&](int tl, uint32_t (&f)[K / 16][4]) {
+        const int r0 = tl * 16;
         const bool ok0 = r0 + g < M, ok1 = r0 + g + 8 < M;
         const TA* x0 = X + (size_t)(r0 + g) * ldx;
         const TA* x1 = X + (size_t)(r0 + g + 8) * ldx;
-        uint32_t a[K / 16][4];
         #pragma unroll
         for (int ks = 0; ks < K / 16; ++ks) {
             const int c0 = ks * 16 + 2 * t;
-            a[ks][0] = ok0 ? ld_pair(x0 + c0) : 0u;
-            a[ks][1] = ok1 ? ld_pair(x1 + c0) : 0u;
-            a[ks][2] = ok0 ? ld_pair(x0 + c0 + 8) : 0u;
-            a[ks][3] = ok1 ? ld_pair(x1 + c0 + 8) : 0u;
+            f[ks][0] = ok0 ? ld_pair(x0 + c0) : 0u;
+            f[ks][1] = ok1 ? ld_pair(x1 + c0) : 0u;
+            f[ks][2] = ok0 ? ld_pair(x0 + c0 + 8) : 0u;
+            f[ks][3] = ok1 ? ld_pair(x1 + c0 + 8) : 0u;
         }
+    };
+    int tile = blockIdx.x * 4 + warp;
+    uint32_t a[K / 16][4];
+    load_a(tile, a);
+    for (; tile < ntile; tile += stride) {
+        const int r0 = tile * 16;
+        // the next tile's fragments are loaded while this one is multiplied
+        uint32_t an[K / 16][4];
+        load_a(tile + stride, an);
+        float acc[NOUT / 8][4];
+        #pragma unroll
+        for (int n = 0; n < NOUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
         #pragma unroll
         for (int ks = 0; ks < K / 16; ++ks) {
             const int c0 = ks * 16 + 2 * t;
@@ -110,8 +121,16 @@ __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx,
                 if (EPI & EPI_RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
                 if (EPI & EPI_STORE1)
                     *reinterpret_cast<__nv_bfloat162*>(Y1 + (size_t)row * ld1 + col) = __floats2bfloat162_rn(v0, v1);
-                if (EPI & EPI_RESID2) {
-                    const __nv_bfloat162 r = *reinterpret_cast<const __nv_bfloat162*>(R + (size_t)row * ldr + col);
+                if (EPI & (EPI_RESID2 | EPI_RESIDA)) {
+                    // EPI_RESIDA: the residual is the A operand's first NOUT
+                    // columns, already in this thread's fragments
+                    __nv_bfloat162 r;
+                    if (EPI & EPI_RESIDA) {
+                        const uint32_t u = a[n >> 1][(n & 1) * 2 + hf];
+                        r = *reinterpret_cast<const __nv_bfloat162*>(&u);
+                    } else {
+                        r = *reinterpret_cast<const __nv_bfloat162*>(R + (size_t)row * ldr + col);
+                    }
                     *reinterpret_cast<__nv_bfloat162*>(Y2 + (size_t)row * ld2 + col) =
                         __floats2bfloat162_rn(__bfloat162float(r.x) + v0, __bfloat162float(r.y) + v1);
                 }
@@ -122,6 +141,10 @@ __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx,
                     *p = make_float2(o.x + v0, o.y + v1);
                 }
             }
+        #pragma unroll
+        for (int ks = 0; ks < K / 16; ++ks)
+            #pragma unroll
+            for (int i = 0; i < 4; ++i) a[ks][i] = an[ks][i];
     }
 }
 
@@ -151,6 +174,187 @@ void gemm(cudaStream_t st, const TA* X, int ldx, int M, const bf16* W, const flo
 {
     k_gemm<TA, K, NOUT, EPI><<<gemm_grid<TA, K, NOUT, EPI>(M), 128, 0, st>>>(X, ldx, M, W, bias, R, ldr, Y1, ld1, Y2,
                                                                             ld2, Yf, ldf);
+}
+
+// ---- fused inference kernels ----------------------------------------------
+// One warp holds a 16-row tile from its first product to its last store: the
+// first product's epilogue rounds h to bf16 in the accumulator layout of
+// m16n8k16, which is exactly the A-fragment layout of the next mma (n-tiles
+// 2k and 2k+1 form k-step k), so the second product starts from registers.
+// Every product is the mma sequence k_gemm issues on the same bf16 operands
+// and every epilogue the same float operations, so the results are bitwise
+// those of the separate kernels (encoder; update; P/Q; decoder + start).
+//   FUSE_ENC_PQ:  h = relu(We x + be), stored; P, Q = AB h of layer 0
+//   FUSE_UPD_PQ:  h' = h + relu(U [h; a] + u), stored; P, Q = AB h' of the next layer
+//   FUSE_UPD_OUT: h' as above; out = Wd h' + bd; warm start d_prev + s out
+enum { FUSE_ENC_PQ = 0, FUSE_UPD_PQ = 1, FUSE_UPD_OUT = 2 };
+
+template <int MODE>
+__global__ void __launch_bounds__(128, 4) k_fused(const bf16* __restrict__ X, int ldx, int M,
+                                                  const bf16* __restrict__ W1, const float* __restrict__ b1,
+                                                  const bf16* __restrict__ W2, const float* __restrict__ b2,
+                                                  bf16* __restrict__ hout, int ldh, bf16* __restrict__ pq,
+                                                  const float4* __restrict__ A, const float4* __restrict__ Dp,
+                                                  float4* __restrict__ warm)
+{
+    constexpr int K1 = MODE == FUSE_ENC_PQ ? NFP : 2 * H;   // first product: K1 -> H
+    constexpr int N2 = MODE == FUSE_UPD_OUT ? 8 : 2 * H;     // second product: H -> N2 (decoder: first n-tile)
+    __shared__ __align__(16) bf16 sW1[H * (K1 + 8)];
+    __shared__ __align__(16) bf16 sW2[N2 * (H + 8)];
+    __shared__ float sb1[H], sb2[N2];
+    for (int i = threadIdx.x; i < H * K1 / 8; i += 128) {
+        const int r = i / (K1 / 8), c = (i % (K1 / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW1 + r * (K1 + 8) + c) = *reinterpret_cast<const uint4*>(W1 + (size_t)r * K1 + c);
+    }
+    for (int i = threadIdx.x; i < N2 * H / 8; i += 128) {
+        const int r = i / (H / 8), c = (i % (H / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW2 + r * (H + 8) + c) = *reinterpret_cast<const uint4*>(W2 + (size_t)r * H + c);
+    }
+    for (int i = threadIdx.x; i < H; i += 128) sb1[i] = b1[i];
+    for (int i = threadIdx.x; i < N2; i += 128) sb2[i] = b2 ? b2[i] : 0.f;
+    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int ntile = (M + 15) >> 4, stride = gridDim.x * 4;
+    auto load_a = [&](int tl, uint32_t (&f)[K1 / 16][4]) {
+        const int r0 = tl * 16;
+        const bool ok0 = r0 + g < M, ok1 = r0 + g + 8 < M;
+        const bf16* x0 = X + (size_t)(r0 + g) * ldx;
+        const bf16* x1 = X + (size_t)(r0 + g + 8) * ldx;
+        #pragma unroll
+        for (int ks = 0; ks < K1 / 16; ++ks) {
+            const int c0 = ks * 16 + 2 * t;
+            f[ks][0] = ok0 ? ld_pair(x0 + c0) : 0u;
+            f[ks][1] = ok1 ? ld_pair(x1 + c0) : 0u;
+            f[ks][2] = ok0 ? ld_pair(x0 + c0 + 8) : 0u;
+            f[ks][3] = ok1 ? ld_pair(x1 + c0 + 8) : 0u;
+        }
+    };
+    int tile = blockIdx.x * 4 + warp;
+    uint32_t a[K1 / 16][4];
+    load_a(tile, a);
+    for (; tile < ntile; tile += stride) {
+        const int r0 = tile * 16;
+        uint32_t an[K1 / 16][4];
+        load_a(tile + stride, an);
+        // first product and its epilogue: hp = bf16(h) in fragment layout
+        uint32_t hp[H / 8][2];
+        {
+            float acc[H / 8][4];
+            #pragma unroll
+            for (int n = 0; n < H / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+            #pragma unroll
+            for (int ks = 0; ks < K1 / 16; ++ks) {
+                const int c0 = ks * 16 + 2 * t;
+                #pragma unroll
+                for (int n = 0; n < H / 8; ++n) {
+                    const bf16* wr = sW1 + (n * 8 + g) * (K1 + 8) + c0;
+                    mma_bf16(acc[n], a[ks][0], a[ks][1], a[ks][2], a[ks][3], *reinterpret_cast<const uint32_t*>(wr),
+                             *reinterpret_cast<const uint32_t*>(wr + 8));
+                }
+            }
+            #pragma unroll
+            for (int n = 0; n < H / 8; ++n)
+                #pragma unroll
+                for (int hf = 0; hf < 2; ++hf) {
+                    const int col = n * 8 + 2 * t;
+                    const float v0 = fmaxf(acc[n][2 * hf] + sb1[col], 0.f);
+                    const float v1 = fmaxf(acc[n][2 * hf + 1] + sb1[col + 1], 0.f);
+                    __nv_bfloat162 o;
+                    if (MODE == FUSE_ENC_PQ) {
+                        o = __floats2bfloat162_rn(v0, v1);
+                    } else {   // residual: the A operand's first H columns
+                        const uint32_t u = a[n >> 1][(n & 1) * 2 + hf];
+                        const __nv_bfloat162 r = *reinterpret_cast<const __nv_bfloat162*>(&u);
+                        o = __floats2bfloat162_rn(__bfloat162float(r.x) + v0, __bfloat162float(r.y) + v1);
+                    }
+                    hp[n][hf] = *reinterpret_cast<const uint32_t*>(&o);
+                    const int row = r0 + g + 8 * hf;
+                    if (MODE != FUSE_UPD_OUT && row < M)
+                        *reinterpret_cast<uint32_t*>(hout + (size_t)row * ldh + col) = hp[n][hf];
+                }
+        }
+        if (MODE != FUSE_UPD_OUT) {
+            // P, Q of the next layer, 64 columns at a time
+            #pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                float acc[8][4];
+                #pragma unroll
+                for (int n = 0; n < 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+                #pragma unroll
+                for (int ks = 0; ks < H / 16; ++ks) {
+                    const int c0 = ks * 16 + 2 * t;
+                    #pragma unroll
+                    for (int n = 0; n < 8; ++n) {
+                        const bf16* wr = sW2 + ((half * 8 + n) * 8 + g) * (H + 8) + c0;
+                        mma_bf16(acc[n], hp[2 * ks][0], hp[2 * ks][1], hp[2 * ks + 1][0], hp[2 * ks + 1][1],
+                                 *reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8));
+                    }
+                }
+                #pragma unroll
+                for (int n = 0; n < 8; ++n)
+                    #pragma unroll
+                    for (int hf = 0; hf < 2; ++hf) {
+                        const int row = r0 + g + 8 * hf;
+                        if (row >= M) continue;
+                        const int col = half * H + n * 8 + 2 * t;
+                        *reinterpret_cast<__nv_bfloat162*>(pq + (size_t)row * 2 * H + col) =
+                            __floats2bfloat162_rn(acc[n][2 * hf], acc[n][2 * hf + 1]);
+                    }
+            }
+        } else {
+            // decoder, first n-tile (outputs 0..7 of which 0..2 are used),
+            // then the start offsets of k_warm_out
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            #pragma unroll
+            for (int ks = 0; ks < H / 16; ++ks) {
+                const int c0 = ks * 16 + 2 * t;
+                const bf16* wr = sW2 + g * (H + 8) + c0;
+                mma_bf16(acc, hp[2 * ks][0], hp[2 * ks][1], hp[2 * ks + 1][0], hp[2 * ks + 1][1],
+                         *reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8));
+            }
+            #pragma unroll
+            for (int hf = 0; hf < 2; ++hf) {
+                // lane t holds outputs 2t, 2t+1 of rows g and g + 8; output 2
+                // comes from the next lane (t = 1)
+                const float o0 = acc[2 * hf] + sb2[2 * t], o1 = acc[2 * hf + 1] + sb2[2 * t + 1];
+                const float o2 = __shfl_down_sync(full, o0, 1);
+                const int row = r0 + g + 8 * hf;
+                if (t == 0 && row < M) {
+                    const float4 av = A[row];
+                    const float4 dp = Dp ? Dp[row] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float ok = dp.w > 0.f ? 1.f : 0.f;
+                    warm[row] = av.w < 0.f ? av
+                                           : make_float4(fmaf(o0, kOffsetScale, ok * dp.x),
+                                                         fmaf(o1, kOffsetScale, ok * dp.y),
+                                                         fmaf(o2, kOffsetScale, ok * dp.z), av.w);
+                }
+            }
+        }
+        #pragma unroll
+        for (int ks = 0; ks < K1 / 16; ++ks)
+            #pragma unroll
+            for (int i = 0; i < 4; ++i) a[ks][i] = an[ks][i];
+    }
+}
+
+// Launch of k_fused on `st`, the grid sized to the resident blocks.
+template <int MODE>
+void fused(cudaStream_t st, const bf16* X, int ldx, int M, const bf16* W1, const float* b1, const bf16* W2,
+           const float* b2, bf16* hout, int ldh, bf16* pq, const float4* A, const float4* Dp, float4* warm)
+{
+    static int resident[16] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& r = resident[dev & 15];
+    if (r == 0) {
+        int nsm = 0, per = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fused<MODE>, 128, 0);
+        r = std::max(1, nsm * std::max(per, 1));
+    }
+    const int grid = std::max(1, std::min((((M + 15) >> 4) + 3) / 4, r));
+    k_fused<MODE><<<grid, 128, 0, st>>>(X, ldx, M, W1, b1, W2, b2, hout, ldh, pq, A, Dp, warm);
 }
 
 __device__ __forceinline__ float tofloat(float v) { return v; }
@@ -546,22 +750,6 @@ __global__ void k_target(int N, const float4* __restrict__ Xs, const float4* __r
     target[3 * i + 1] = (x.y - y.y - ok * dp.y) * is;
     target[3 * i + 2] = (x.z - y.z - ok * dp.z) * is;
     freew[i] = aux[i].w < 0.f ? 0.f : 1.f;
-}
-
-// predicted start offsets d_prev + s out (pinned vertices keep the inertial
-// start's target offset)
-__global__ void k_warm_out(int N, const float* __restrict__ out, const float4* __restrict__ A,
-                           const float4* __restrict__ Dp, float4* __restrict__ warm)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const float4 a = A[i];
-    const float4 dp = Dp ? Dp[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float ok = dp.w > 0.f ? 1.f : 0.f;
-    warm[i] = a.w < 0.f ? a
-                        : make_float4(fmaf(out[(size_t)i * 16], kOffsetScale, ok * dp.x),
-                                      fmaf(out[(size_t)i * 16 + 1], kOffsetScale, ok * dp.y),
-                                      fmaf(out[(size_t)i * 16 + 2], kOffsetScale, ok * dp.z), a.w);
 }
 
 }  // namespace gnn
