@@ -187,7 +187,81 @@ void gemm(cudaStream_t st, const TA* X, int ldx, int M, const bf16* W, const flo
 //   FUSE_ENC_PQ:  h = relu(We x + be), stored; P, Q = AB h of layer 0
 //   FUSE_UPD_PQ:  h' = h + relu(U [h; a] + u), stored; P, Q = AB h' of the next layer
 //   FUSE_UPD_OUT: h' as above; out = Wd h' + bd; warm start d_prev + s out
+// B fragments come from the staged weights by ldmatrix (two n-tiles per
+// instruction); outputs go through a per-warp shared tile (stmatrix) and
+// leave as 16-byte row pieces.
 enum { FUSE_ENC_PQ = 0, FUSE_UPD_PQ = 1, FUSE_UPD_OUT = 2 };
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void ldsm_x4(const bf16* p, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void stsm_x4(bf16* p, uint32_t r0, uint32_t r1, uint32_t r2, uint32_t r3)
+{
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(smem_u32(p)), "r"(r0), "r"(r1),
+                 "r"(r2), "r"(r3)
+                 : "memory");
+}
+
+// acc[n] (n-tiles 0..NT-1) += A (16 x K, fragments a) W^T, W staged as
+// [NT*8][K + 8]: one ldmatrix.x4 gives b0, b1 of n-tiles n and n + 1.
+template <int K, int NT>
+__device__ __forceinline__ void mma_tile(float (&acc)[NT][4], const uint32_t (&a)[K / 16][4], const bf16* sW,
+                                         int lane)
+{
+    const int m = lane >> 3, r = lane & 7;
+    #pragma unroll
+    for (int ks = 0; ks < K / 16; ++ks)
+        #pragma unroll
+        for (int n = 0; n < NT; n += 2) {
+            uint32_t b00, b01, b10, b11;
+            ldsm_x4(sW + ((n + (m >> 1)) * 8 + r) * (K + 8) + ks * 16 + (m & 1) * 8, b00, b01, b10, b11);
+            mma_bf16(acc[n], a[ks][0], a[ks][1], a[ks][2], a[ks][3], b00, b01);
+            mma_bf16(acc[n + 1], a[ks][0], a[ks][1], a[ks][2], a[ks][3], b10, b11);
+        }
+}
+
+// Rows r0..r0+15 of a bf16 tile (the first COLS columns of sO, row stride
+// SROW) to global memory (row stride ld), 16 bytes per piece.
+template <int COLS, int SROW>
+__device__ __forceinline__ void tile_out(const bf16* sO, bf16* dst, int ld, int r0, int M, int lane)
+{
+    constexpr int PR = COLS / 8;   // 16-byte pieces per row
+    #pragma unroll
+    for (int q = lane; q < 16 * PR; q += 32) {
+        const int row = q / PR, c = (q % PR) * 8;
+        if (r0 + row < M)
+            *reinterpret_cast<uint4*>(dst + (size_t)(r0 + row) * ld + c) =
+                *reinterpret_cast<const uint4*>(sO + row * SROW + c);
+    }
+}
+
+// Fragment pairs c[n][0..1] (rows 0-7 / 8-15 of n-tile n, bf16x2) of NT
+// n-tiles into the staged tile sO (row stride COLS + 8) at column col0.
+template <int NT, int COLS>
+__device__ __forceinline__ void tile_stage(const uint32_t (&c)[NT][2], bf16* sO, int col0, int lane)
+{
+    const int m = lane >> 3, r = lane & 7;
+    #pragma unroll
+    for (int n = 0; n < NT; n += 2)
+        stsm_x4(sO + ((m & 1) * 8 + r) * (COLS + 8) + col0 + (n + (m >> 1)) * 8, c[n][0], c[n][1], c[n + 1][0],
+                c[n + 1][1]);
+}
+
+template <int MODE>
+struct FusedShape {
+    static constexpr int K1 = MODE == FUSE_ENC_PQ ? NFP : 2 * H;   // first product: K1 -> H
+    static constexpr int N2 = MODE == FUSE_UPD_OUT ? 8 : 2 * H;     // second: H -> N2 (decoder: first n-tile)
+    static constexpr int OCOLS = MODE == FUSE_UPD_OUT ? 8 : 2 * H;  // staged output tile width
+    static constexpr size_t smem = sizeof(bf16) * ((size_t)H * (K1 + 8) + (size_t)N2 * (H + 8) +
+                                                   (MODE == FUSE_UPD_OUT ? 0 : 4 * 16 * (OCOLS + 8)));
+};
 
 template <int MODE>
 __global__ void __launch_bounds__(128, 4) k_fused(const bf16* __restrict__ X, int ldx, int M,
@@ -197,10 +271,11 @@ __global__ void __launch_bounds__(128, 4) k_fused(const bf16* __restrict__ X, in
                                                   const float4* __restrict__ A, const float4* __restrict__ Dp,
                                                   float4* __restrict__ warm)
 {
-    constexpr int K1 = MODE == FUSE_ENC_PQ ? NFP : 2 * H;   // first product: K1 -> H
-    constexpr int N2 = MODE == FUSE_UPD_OUT ? 8 : 2 * H;     // second product: H -> N2 (decoder: first n-tile)
-    __shared__ __align__(16) bf16 sW1[H * (K1 + 8)];
-    __shared__ __align__(16) bf16 sW2[N2 * (H + 8)];
+    using S = FusedShape<MODE>;
+    constexpr int K1 = S::K1, N2 = S::N2;
+    extern __shared__ __align__(16) unsigned char fsm[];
+    bf16* sW1 = reinterpret_cast<bf16*>(fsm);
+    bf16* sW2 = sW1 + H * (K1 + 8);
     __shared__ float sb1[H], sb2[N2];
     for (int i = threadIdx.x; i < H * K1 / 8; i += 128) {
         const int r = i / (K1 / 8), c = (i % (K1 / 8)) * 8;
@@ -215,6 +290,7 @@ __global__ void __launch_bounds__(128, 4) k_fused(const bf16* __restrict__ X, in
     __syncthreads();
     const unsigned full = 0xffffffffu;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    bf16* sO = sW2 + N2 * (H + 8) + warp * 16 * (S::OCOLS + 8);   // this warp's output tile
     const int ntile = (M + 15) >> 4, stride = gridDim.x * 4;
     auto load_a = [&](int tl, uint32_t (&f)[K1 / 16][4]) {
         const int r0 = tl * 16;
@@ -243,16 +319,7 @@ __global__ void __launch_bounds__(128, 4) k_fused(const bf16* __restrict__ X, in
             float acc[H / 8][4];
             #pragma unroll
             for (int n = 0; n < H / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
-            #pragma unroll
-            for (int ks = 0; ks < K1 / 16; ++ks) {
-                const int c0 = ks * 16 + 2 * t;
-                #pragma unroll
-                for (int n = 0; n < H / 8; ++n) {
-                    const bf16* wr = sW1 + (n * 8 + g) * (K1 + 8) + c0;
-                    mma_bf16(acc[n], a[ks][0], a[ks][1], a[ks][2], a[ks][3], *reinterpret_cast<const uint32_t*>(wr),
-                             *reinterpret_cast<const uint32_t*>(wr + 8));
-                }
-            }
+            mma_tile<K1, H / 8>(acc, a, sW1, lane);
             #pragma unroll
             for (int n = 0; n < H / 8; ++n)
                 #pragma unroll
@@ -269,42 +336,43 @@ __global__ void __launch_bounds__(128, 4) k_fused(const bf16* __restrict__ X, in
                         o = __floats2bfloat162_rn(__bfloat162float(r.x) + v0, __bfloat162float(r.y) + v1);
                     }
                     hp[n][hf] = *reinterpret_cast<const uint32_t*>(&o);
-                    const int row = r0 + g + 8 * hf;
-                    if (MODE != FUSE_UPD_OUT && row < M)
-                        *reinterpret_cast<uint32_t*>(hout + (size_t)row * ldh + col) = hp[n][hf];
                 }
         }
         if (MODE != FUSE_UPD_OUT) {
-            // P, Q of the next layer, 64 columns at a time
+            constexpr int OC = S::OCOLS;
+            tile_stage<H / 8, OC>(hp, sO, 0, lane);
+            __syncwarp();
+            tile_out<H, OC + 8>(sO, hout, ldh, r0, M, lane);
+            __syncwarp();
+            // P, Q of the next layer, 64 columns at a time, staged then stored
             #pragma unroll
             for (int half = 0; half < 2; ++half) {
                 float acc[8][4];
                 #pragma unroll
                 for (int n = 0; n < 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+                uint32_t hk[H / 16][4];
                 #pragma unroll
                 for (int ks = 0; ks < H / 16; ++ks) {
-                    const int c0 = ks * 16 + 2 * t;
-                    #pragma unroll
-                    for (int n = 0; n < 8; ++n) {
-                        const bf16* wr = sW2 + ((half * 8 + n) * 8 + g) * (H + 8) + c0;
-                        mma_bf16(acc[n], hp[2 * ks][0], hp[2 * ks][1], hp[2 * ks + 1][0], hp[2 * ks + 1][1],
-                                 *reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8));
-                    }
+                    hk[ks][0] = hp[2 * ks][0]; hk[ks][1] = hp[2 * ks][1];
+                    hk[ks][2] = hp[2 * ks + 1][0]; hk[ks][3] = hp[2 * ks + 1][1];
                 }
+                mma_tile<H, 8>(acc, hk, sW2 + half * H * (H + 8), lane);
+                uint32_t c[8][2];
                 #pragma unroll
                 for (int n = 0; n < 8; ++n)
                     #pragma unroll
                     for (int hf = 0; hf < 2; ++hf) {
-                        const int row = r0 + g + 8 * hf;
-                        if (row >= M) continue;
-                        const int col = half * H + n * 8 + 2 * t;
-                        *reinterpret_cast<__nv_bfloat162*>(pq + (size_t)row * 2 * H + col) =
-                            __floats2bfloat162_rn(acc[n][2 * hf], acc[n][2 * hf + 1]);
+                        const __nv_bfloat162 o = __floats2bfloat162_rn(acc[n][2 * hf], acc[n][2 * hf + 1]);
+                        c[n][hf] = *reinterpret_cast<const uint32_t*>(&o);
                     }
+                tile_stage<8, OC>(c, sO, half * H, lane);
             }
+            __syncwarp();
+            tile_out<2 * H, OC + 8>(sO, pq, 2 * H, r0, M, lane);
+            __syncwarp();
         } else {
             // decoder, first n-tile (outputs 0..7 of which 0..2 are used),
-            // then the start offsets of k_warm_out
+            // then the start offsets of the separate path
             float acc[4] = {0.f, 0.f, 0.f, 0.f};
             #pragma unroll
             for (int ks = 0; ks < H / 16; ++ks) {
@@ -344,17 +412,19 @@ void fused(cudaStream_t st, const bf16* X, int ldx, int M, const bf16* W1, const
            const float* b2, bf16* hout, int ldh, bf16* pq, const float4* A, const float4* Dp, float4* warm)
 {
     static int resident[16] = {};
+    const size_t smem = FusedShape<MODE>::smem;
     int dev = 0;
     cudaGetDevice(&dev);
     int& r = resident[dev & 15];
     if (r == 0) {
         int nsm = 0, per = 0;
+        cudaFuncSetAttribute(k_fused<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fused<MODE>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fused<MODE>, 128, smem);
         r = std::max(1, nsm * std::max(per, 1));
     }
     const int grid = std::max(1, std::min((((M + 15) >> 4) + 3) / 4, r));
-    k_fused<MODE><<<grid, 128, 0, st>>>(X, ldx, M, W1, b1, W2, b2, hout, ldh, pq, A, Dp, warm);
+    k_fused<MODE><<<grid, 128, smem, st>>>(X, ldx, M, W1, b1, W2, b2, hout, ldh, pq, A, Dp, warm);
 }
 
 __device__ __forceinline__ float tofloat(float v) { return v; }
