@@ -148,10 +148,12 @@ __global__ void __launch_bounds__(128) k_gemm(const TA* __restrict__ X, int ldx,
     }
 }
 
-// Grid of k_gemm for M rows: enough blocks for every row tile, at most the
-// blocks that are resident at once on this device.
-template <typename TA, int K, int NOUT, int EPI>
-int gemm_grid(int M)
+// Grid of a grid-stride kernel: `need` blocks, at most the blocks of
+// `threads` threads and `smem` dynamic shared bytes that are resident at once
+// on the current device (looked up once per kernel and device; the kernel's
+// dynamic shared-memory limit is raised to `smem` then).
+template <auto KERN>
+int resident_grid(int threads, size_t smem, long long need)
 {
     static int resident[16] = {};
     int dev = 0;
@@ -159,12 +161,20 @@ int gemm_grid(int M)
     int& r = resident[dev & 15];
     if (r == 0) {
         int nsm = 0, per = 0;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gemm<TA, K, NOUT, EPI>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, KERN, threads, smem);
         r = std::max(1, nsm * std::max(per, 1));
     }
-    const int need = (((M + 15) >> 4) + 3) / 4;
-    return std::max(1, std::min(need, r));
+    return (int)std::max(1LL, std::min(need, (long long)r));
+}
+
+// Grid of k_gemm for M rows: enough blocks for every row tile, at most the
+// resident ones.
+template <typename TA, int K, int NOUT, int EPI>
+int gemm_grid(int M)
+{
+    return resident_grid<k_gemm<TA, K, NOUT, EPI>>(128, 0, ((((long long)M + 15) >> 4) + 3) / 4);
 }
 
 // Launch of k_gemm on `st` with the grid above.
@@ -411,19 +421,8 @@ template <int MODE>
 void fused(cudaStream_t st, const bf16* X, int ldx, int M, const bf16* W1, const float* b1, const bf16* W2,
            const float* b2, bf16* hout, int ldh, bf16* pq, const float4* A, const float4* Dp, float4* warm)
 {
-    static int resident[16] = {};
     const size_t smem = FusedShape<MODE>::smem;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int& r = resident[dev & 15];
-    if (r == 0) {
-        int nsm = 0, per = 0;
-        cudaFuncSetAttribute(k_fused<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fused<MODE>, 128, smem);
-        r = std::max(1, nsm * std::max(per, 1));
-    }
-    const int grid = std::max(1, std::min((((M + 15) >> 4) + 3) / 4, r));
+    const int grid = resident_grid<k_fused<MODE>>(128, smem, ((((long long)M + 15) >> 4) + 3) / 4);
     k_fused<MODE><<<grid, 128, smem, st>>>(X, ldx, M, W1, b1, W2, b2, hout, ldh, pq, A, Dp, warm);
 }
 
@@ -588,21 +587,7 @@ __global__ void __launch_bounds__(256) k_msg_fwd(int N, const int* __restrict__ 
 
 // Grid of k_msg_fwd for N nodes: one warp per pair of nodes, at most the
 // blocks that are resident at once on this device.
-inline int msg_grid(int N)
-{
-    static int resident[16] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int& r = resident[dev & 15];
-    if (r == 0) {
-        int nsm = 0, per = 0;
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_msg_fwd, 256, 0);
-        r = std::max(1, nsm * std::max(per, 1));
-    }
-    const int need = (((N + 1) >> 1) + 7) / 8;
-    return std::max(1, std::min(need, r));
-}
+inline int msg_grid(int N) { return resident_grid<k_msg_fwd>(256, 0, ((((long long)N + 1) >> 1) + 7) / 8); }
 
 // Backward of the messages: dP_i = sum_j g_ij, dQ_j = sum_i g_ij with
 // g_ij = [z_ij > 0] da_i / deg_i (da = dcat[:, H:2H]); dC, dc reduced per
