@@ -310,6 +310,34 @@ def test_step_host_several_frames_mixed_buffers(pdg, oracle, kernel):
     assert np.array_equal(xd, ux) and buf[0] == 0
 
 
+def test_step_host_large_state_moves_by_dma(pdg):
+    # from 4 MB per array the host buffers go through DMA into the staging
+    # buffers instead of being read in place: a 641x641 cloth (410,881
+    # vertices, 4.9 MB per array) on the streaming kernel, page-locked and
+    # pageable buffers, equal bitwise to set_state_all + step + get_state_all
+    torch = pytest.importorskip("torch")
+    import scenes
+    m, c = scenes.hanging(641, 3.0, ks=1e3, kb=1e-2, seed=2)
+    cfg = pdg.Config.default(max_iterations=4, tolerance=0.0, rho=0.99, dt=scenes.H, gravity=scenes.G,
+                             kernel=pdg.KERNEL_STREAM)
+    s1 = pdg.Solver(cfg, m, c)
+    s2 = pdg.Solver(cfg, m, c)
+    n = m.N
+    assert 12 * n >= 4 << 20
+    rng = np.random.default_rng(5)
+    x = (np.asarray(m.arrays()["rest"]).reshape(-1, 3) + rng.normal(0, 1e-3, (n, 3))).astype(np.float32)
+    v = rng.normal(0, 1e-2, (n, 3)).astype(np.float32)
+    pinned = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    s1.set_state_all(x, v); s1.step(2, stats=False); xa, va = s1.get_state_all()
+    px, pv = pinned(x), pinned(v)
+    s2.step_host(px, pv, px, pv, nframes=2)
+    assert np.array_equal(xa, px) and np.array_equal(va, pv)
+    s1.step(1, stats=False); xb, vb = s1.get_state_all()
+    xo, vo = np.full_like(x, np.nan), np.full_like(v, np.nan)
+    s2.step_host(px.copy(), pv.copy(), xo, vo)
+    assert np.array_equal(xb, xo) and np.array_equal(vb, vo)
+
+
 def test_apply_pins_device(pdg):
     torch = pytest.importorskip("torch")
     pos = torch.arange(30, dtype=torch.float32, device="cuda")
