@@ -281,3 +281,67 @@ def test_committed_learned_start_needs_fewer_sweeps_than_the_inertial_start(pdg)
     assert all(x["status"] == 0 for x in rows["learned"])
     assert any(x["warm_start_used"] for x in rows["learned"])
     assert sl < si, (sl, si)
+
+
+def test_solver_inference_matches_the_oracle_forward(pdg):
+    # The solver's own inference (the fused inference kernels) against the
+    # float64 network on features built here from the same state, with a
+    # network whose decoder is not zero.  A frame of no sweeps in keep mode
+    # ends at x = y + start, so the start offsets read back as x - y.  The
+    # state is written by the caller, so no previous offset is valid.
+    import scenes
+    import gnn_oracle as G
+    ms, cs, cfgs, _ = scenes.batch(3, seed=41, max_iterations=0, tolerance=0.0, n_range=(17, 33),
+                                   kernel=pdg.KERNEL_STREAM, init=pdg.INIT_WARMSTART_KEEP, patch_verts=128,
+                                   block_threads=128)
+    s = pdg.Solver(cfgs, ms, cs)
+    rng = np.random.default_rng(17)
+    p = {k: rng.normal(scale=0.2, size=shp) for k, shp in G.shapes()}
+    flat = G.flatten(p).astype(np.float32)
+    w = pdg.WarmStart(seed=0)
+    w.set_params(flat)
+    w.attach(s)
+    xs, vs = [], []
+    for m in ms:
+        rest = np.asarray(m.arrays()["rest"], np.float32).reshape(-1, 3)
+        xs.append((rest + rng.normal(0, 2e-3, rest.shape)).astype(np.float32))
+        vs.append(rng.normal(0, 0.1, rest.shape).astype(np.float32))
+    s.set_state_all(np.concatenate(xs), np.concatenate(vs))
+    st = s.step(1)
+    assert all(t["status"] == 0 and t["warm_start_used"] == 1 and t["iterations"] == 0 for t in st)
+    sc = 2.725e-3   # the network's output scale: one frame's gravity drop at h = 1/60
+    got, want = [], []
+    for i, (m, c, cfg) in enumerate(zip(ms, cs, cfgs)):
+        x1, _ = s.get_state(i)
+        y = s.prediction(i).astype(np.float64)
+        a, ca, tp = m.arrays(), c.arrays(), m.topology()
+        n = m.N
+        pinned = np.zeros(n, bool)
+        pinned[ca["pins"]] = True
+        ks = float(np.mean(ca["k_stretch"].astype(np.float64))) if len(ca["k_stretch"]) else 1.0
+        kb = float(np.mean(ca["bend_k"].astype(np.float64))) if len(ca["bend_k"]) else 1e-3
+        mass = np.maximum(a["mass"].astype(np.float64), 1e-12)
+        f = np.zeros((n, G.NF))
+        f[:, 0:3] = (y - xs[i]) / sc
+        f[:, 3:6] = cfg.dt * vs[i].astype(np.float64) / sc
+        f[:, 6] = pinned
+        f[:, 7] = (np.log(mass) + 11.0) / 2.0
+        f[:, 8] = (np.log(max(ks, 1e-6)) - 6.9) / 1.2
+        f[:, 9] = (np.log(max(kb, 1e-9)) + 4.6) / 1.2
+        ed = tp["edges"][:, :2].astype(np.int64)
+        r = np.maximum(tp["rest_len"].astype(np.float64), 1e-12)
+        dst = np.concatenate([ed[:, 0], ed[:, 1]]); src = np.concatenate([ed[:, 1], ed[:, 0]])
+        rr = np.concatenate([r, r])
+        e = np.concatenate([np.log(rr / 0.01)[:, None], (y[src] - y[dst]) / rr[:, None]], axis=1)
+        deg = np.bincount(dst, minlength=n).astype(np.float64)
+        pb = dict(G.unflatten(flat))
+        for k in pb:
+            if k[0] in "WABU":
+                pb[k] = bf16_round(pb[k]).astype(np.float64)
+        out, _ = G.forward(pb, bf16_round(f.astype(np.float32)).astype(np.float64), e, src, dst, deg)
+        free = ~pinned
+        got.append((x1.astype(np.float64) - y)[free])
+        want.append(sc * out[free])
+    got = np.concatenate(got); want = np.concatenate(want)
+    assert np.linalg.norm(want) > 1e-4 * len(want) ** 0.5 * sc   # the decoder moves the start
+    assert np.linalg.norm(got - want) <= 2e-2 * np.linalg.norm(want), np.linalg.norm(got - want) / np.linalg.norm(want)
