@@ -91,11 +91,13 @@ __global__ void k_select_vertex(int n, const int* __restrict__ vcloth, const Clo
 // every cloth continues from the chain with the lower residual.
 // Start of the learned chain: per cloth its record (normaliser r(y)^2 from
 // the inertial start's evaluation in acc[slot_y], also given to the
-// inertial chain) and cleared per-sweep sums; one block per cloth.
+// inertial chain; 0 when slot_y < 0, in which case k_warm_start_norm sets it
+// after the inertial chain's first sweep) and cleared per-sweep sums; one
+// block per cloth.
 __global__ void k_warm_init_cloth(IterArgs a, IterArgs b, int slot_y)
 {
     const int c = blockIdx.x;
-    const double r2y = a.acc[(size_t)c * a.acc_stride + slot_y];
+    const double r2y = slot_y >= 0 ? a.acc[(size_t)c * a.acc_stride + slot_y] : 0.0;
     if (threadIdx.x == 0) {
         a.crt[c].res_y2 = r2y;
         if (a.cinfo[c].init == 3) a.crt[c].warm = 1;
@@ -105,6 +107,20 @@ __global__ void k_warm_init_cloth(IterArgs a, IterArgs b, int slot_y)
         b.crt[c] = r;
     }
     for (int k = threadIdx.x; k < b.acc_stride; k += blockDim.x) b.acc[(size_t)c * b.acc_stride + k] = 0.0;
+}
+
+// The normaliser of both chains from the inertial chain's first sweep: that
+// sweep's residual sum acc[0] is r(x^0)^2 of the chain's start offsets, the
+// value k_res_eval gives for them (used when no cloth starts the inertial
+// chain from the prediction, i.e. none always keeps it).  One thread per
+// cloth, between the inertial chain's sweeps 0 and 1.
+__global__ void k_warm_start_norm(IterArgs a, IterArgs b)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncloth) return;
+    const double r2y = __ldcg(&a.acc[(size_t)c * a.acc_stride]);
+    a.crt[c].res_y2 = r2y;
+    b.crt[c].res_y2 = r2y;
 }
 
 // Start iterates of both chains: the learned chain starts from the
@@ -372,9 +388,15 @@ cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t sme
 }
 
 cudaError_t launch_warm_chain_init(const IterArgs& a, const IterArgs& b, int nt, int npatch, size_t smem,
-                                   const float4* warm, const int* vcloth, int n, cudaStream_t s)
+                                   const float4* warm, const int* vcloth, int n, bool eval_start, cudaStream_t s)
 {
     const int slot_y = a.acc_stride - 2;
+    if (!eval_start) {
+        k_warm_init_cloth<<<a.ncloth, 64, 0, s>>>(a, b, -1);
+        k_warm_init_vertex<<<nblk(n, 256), 256, 0, s>>>(n, vcloth, a.cinfo, warm, a.buf[0], a.buf[1], b.buf[0],
+                                                         b.buf[1]);
+        return cudaGetLastError();
+    }
     static bool attr_set[3] = {false, false, false};
     const int ti = nt == 128 ? 0 : (nt == 256 ? 1 : 2);
     void* f = nt == 128 ? (void*)k_res_eval<128> : (nt == 256 ? (void*)k_res_eval<256> : (void*)k_res_eval<512>);
@@ -388,6 +410,12 @@ cudaError_t launch_warm_chain_init(const IterArgs& a, const IterArgs& b, int nt,
     else k_res_eval<512><<<npatch, 512, smem, s>>>(a, a.buf[0], slot_y);
     k_warm_init_cloth<<<a.ncloth, 64, 0, s>>>(a, b, slot_y);
     k_warm_init_vertex<<<nblk(n, 256), 256, 0, s>>>(n, vcloth, a.cinfo, warm, a.buf[0], a.buf[1], b.buf[0], b.buf[1]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warm_start_norm(const IterArgs& a, const IterArgs& b, cudaStream_t s)
+{
+    k_warm_start_norm<<<nblk(a.ncloth, 128), 128, 0, s>>>(a, b);
     return cudaGetLastError();
 }
 

@@ -17,11 +17,16 @@ cudaError_t launch_finalize(const IterArgs& a, float4* X, float4* V, const float
 // then the per-cloth choice between them (slots acc_stride-2 / -1).
 cudaError_t launch_warm_select(const IterArgs& a, int nt, int npatch, size_t smem, const float4* warm,
                                const int* vcloth, int n, cudaStream_t s);
-// Learned start judged after K sweeps: r(y) of the inertial start, then the
-// start records and iterates of the inertial chain `a` and the learned chain
-// `b` (same layout, own iterates, records and per-sweep sums).
+// Learned start judged after K sweeps: r(y) of the inertial start (with
+// `eval_start`; else launch_warm_start_norm takes it from the inertial
+// chain's first sweep), then the start records and iterates of the inertial
+// chain `a` and the learned chain `b` (same layout, own iterates, records and
+// per-sweep sums).
 cudaError_t launch_warm_chain_init(const IterArgs& a, const IterArgs& b, int nt, int npatch, size_t smem,
-                                   const float4* warm, const int* vcloth, int n, cudaStream_t s);
+                                   const float4* warm, const int* vcloth, int n, bool eval_start, cudaStream_t s);
+// Both chains' normaliser r(y)^2 from the inertial chain's sweep-0 residual
+// sum (between its sweeps 0 and 1).
+cudaError_t launch_warm_start_norm(const IterArgs& a, const IterArgs& b, cudaStream_t s);
 // After K sweeps of both chains: per cloth the chain with the lower residual
 // continues on `a`.
 cudaError_t launch_warm_judge(const IterArgs& a, const IterArgs& b, int K, const int* vcloth, int n, cudaStream_t s);

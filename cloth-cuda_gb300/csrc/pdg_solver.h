@@ -123,6 +123,7 @@ struct pdg_solver {
     bool warm_valid = false;
     pdg_warmstart* ws = nullptr;   // attached learned warm start (not owned)
     bool any_warm = false;         // some cloth asks for a learned start
+    bool any_keep = false;         // some cloth always keeps it (PDG_INIT_WARMSTART_KEEP)
     std::vector<pdg_tune_entry> tune;   // autotuner candidate table
 
     ~pdg_solver();

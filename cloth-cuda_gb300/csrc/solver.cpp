@@ -174,10 +174,19 @@ cudaError_t enqueue_frame_launches(pdg_solver* s, cudaStream_t st, cudaEvent_t e
         } else {
             // both starts run K sweeps on their own chains; every cloth then
             // continues from the chain with the lower residual
+            // The normaliser r(y): when no cloth always keeps the prediction,
+            // every cloth's inertial chain starts from the offsets whose
+            // residual it needs, so its first sweep measures it and a
+            // separate evaluation is not needed.
             const IterArgs b = learned_chain(s, a);
-            e = launch_warm_chain_init(a, b, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot, st);
+            const bool eval_start = s->any_keep;
+            e = launch_warm_chain_init(a, b, s->nt, L.npatch, L.smem_bytes, s->warm.p, s->vcloth.p, L.ntot,
+                                       eval_start, st);
             if (ev_sweeps0) cudaEventRecord(ev_sweeps0, st);
-            for (int k = 0; k < K && e == cudaSuccess; ++k) e = launch_sweep(s, a, k, 0, st, k >= 1);
+            for (int k = 0; k < K && e == cudaSuccess; ++k) {
+                e = launch_sweep(s, a, k, 0, st, k >= 2 || (k == 1 && eval_start));
+                if (k == 0 && !eval_start && e == cudaSuccess) e = launch_warm_start_norm(a, b, st);
+            }
             for (int k = 0; k < K && e == cudaSuccess; ++k) e = launch_sweep(s, b, k, 0, st, true);
             if (e == cudaSuccess) e = launch_warm_judge(a, b, K, s->vcloth.p, L.ntot, st);
             k0 = K;
@@ -283,6 +292,7 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     s->kernel = c0.kernel == PDG_KERNEL_AUTO ? PDG_KERNEL_STREAM : c0.kernel;
     for (const auto& c : s->cloths)
         s->any_warm = s->any_warm || c.cfg.init == PDG_INIT_WARMSTART || c.cfg.init == PDG_INIT_WARMSTART_KEEP;
+    for (const auto& c : s->cloths) s->any_keep = s->any_keep || c.cfg.init == PDG_INIT_WARMSTART_KEEP;
     if (s->any_warm && (c0.kernel == PDG_KERNEL_PERSISTENT || c0.kernel == PDG_KERNEL_RESIDENT))
         return set_error(PDG_ERR_ARG, "the learned warm start runs with the per-sweep (graph) kernels only");
 
