@@ -36,10 +36,9 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_iter(IterArgs a, int k, int re
         omega = (k < a.omega_stride) ? a.omega[c * a.omega_stride + k] : 1.f;
     }
     float4* sx = smem;
-    float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
-    float* cy = cx + ph.vm_nslot;
-    float* cz = cy + ph.vm_nslot;
-    process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, 1.f, sx, cx, cy, cz, red,
+    float2* cxy = reinterpret_cast<float2*>(sx + 2 * ph.nlocal);
+    float* cz = reinterpret_cast<float*>(cxy + ph.vm_nslot);
+    process_patch<MODE, NT>(a, ph, k, res_only != 0 || k >= a.cinfo[ph.cloth].max_iter, 1.f, sx, cxy, cz, red,
                             &skip, &omega);
 }
 
@@ -56,10 +55,9 @@ __global__ void __launch_bounds__(NT) k_res_eval(IterArgs a, const float4* D, in
     b.buf[0] = b.buf[1] = const_cast<float4*>(D);
     b.acc = a.acc + slot;
     float4* sx = smem;
-    float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
-    float* cy = cx + ph.vm_nslot;
-    float* cz = cy + ph.vm_nslot;
-    process_patch<kModeConsistent, NT>(b, ph, 0, true, 1.f, sx, cx, cy, cz, red);
+    float2* cxy = reinterpret_cast<float2*>(sx + 2 * ph.nlocal);
+    float* cz = reinterpret_cast<float*>(cxy + ph.vm_nslot);
+    process_patch<kModeConsistent, NT>(b, ph, 0, true, 1.f, sx, cxy, cz, red);
 }
 
 // Keep the learned start of a cloth only if its residual is below the

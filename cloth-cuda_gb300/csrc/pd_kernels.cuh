@@ -388,10 +388,12 @@ __device__ __forceinline__ void cell_force_p(const CellRec& r, const float4* sy,
 }
 
 // Vertex-major slots (every sweep kernel): the record carries each
-// output's slot address (0xffff for a halo corner or an absent output).
+// output's slot address (0xffff for a halo corner or an absent output).  A
+// slot holds its contribution as an (x, y) pair in cxy and z in cz: two
+// shared-memory accesses per slot.
 template <int MODE>
-__device__ __forceinline__ void cell_contrib_vm(const CellRec& r, const float4* sy, const float4* sd, float* cx,
-                                                float* cy, float* cz)
+__device__ __forceinline__ void cell_contrib_vm(const CellRec& r, const float4* sy, const float4* sd, float2* cxy,
+                                                float* cz)
 {
     float3 o[6];
     cell_force<MODE>(r, sy, sd, o);
@@ -399,13 +401,13 @@ __device__ __forceinline__ void cell_contrib_vm(const CellRec& r, const float4* 
                             r.vm45 & 0xffffu, r.vm45 >> 16};
     #pragma unroll
     for (int k = 0; k < 6; ++k)
-        if (vm[k] != 0xffffu) { cx[vm[k]] = o[k].x; cy[vm[k]] = o[k].y; cz[vm[k]] = o[k].z; }
+        if (vm[k] != 0xffffu) { cxy[vm[k]] = make_float2(o[k].x, o[k].y); cz[vm[k]] = o[k].z; }
 }
 
 // Vertex-major slots with the packed cell arithmetic (same bits).
 template <int MODE>
-__device__ __forceinline__ void cell_contrib_vm_p(const CellRec& r, const float4* sy, const float4* sd, float* cx,
-                                                  float* cy, float* cz)
+__device__ __forceinline__ void cell_contrib_vm_p(const CellRec& r, const float4* sy, const float4* sd, float2* cxy,
+                                                  float* cz)
 {
     float3 o[6];
     cell_force_p<MODE>(r, sy, sd, o);
@@ -413,12 +415,12 @@ __device__ __forceinline__ void cell_contrib_vm_p(const CellRec& r, const float4
                             r.vm45 & 0xffffu, r.vm45 >> 16};
     #pragma unroll
     for (int k = 0; k < 6; ++k)
-        if (vm[k] != 0xffffu) { cx[vm[k]] = o[k].x; cy[vm[k]] = o[k].y; cz[vm[k]] = o[k].z; }
+        if (vm[k] != 0xffffu) { cxy[vm[k]] = make_float2(o[k].x, o[k].y); cz[vm[k]] = o[k].z; }
 }
 
 template <int MODE>
 __device__ __forceinline__ void hinge_contrib_vm(const HingeRec& r, uint2 hs, const float4* sy, const float4* sd,
-                                                 float* cx, float* cy, float* cz)
+                                                 float2* cxy, float* cz)
 {
     const int i0 = r.l01 & 0xffffu, i1 = r.l01 >> 16, i2 = r.l23 & 0xffffu, i3 = r.l23 >> 16;
     const float4 y0 = sy[i0], d0 = sd[i0];
@@ -427,10 +429,10 @@ __device__ __forceinline__ void hinge_contrib_vm(const HingeRec& r, uint2 hs, co
     const float3 q = hinge_force<MODE>(edge(sy, sd, i0, i1), edge(sy, sd, i0, i2), edge(sy, sd, i0, i3), x0, w,
                                        r.h2k, r.nrest);
     const uint32_t s0 = hs.x & 0xffffu, s1 = hs.x >> 16, s2 = hs.y & 0xffffu, s3 = hs.y >> 16;
-    if (s0 != 0xffffu) { cx[s0] = fmul(w.x, q.x); cy[s0] = fmul(w.x, q.y); cz[s0] = fmul(w.x, q.z); }
-    if (s1 != 0xffffu) { cx[s1] = fmul(w.y, q.x); cy[s1] = fmul(w.y, q.y); cz[s1] = fmul(w.y, q.z); }
-    if (s2 != 0xffffu) { cx[s2] = fmul(w.z, q.x); cy[s2] = fmul(w.z, q.y); cz[s2] = fmul(w.z, q.z); }
-    if (s3 != 0xffffu) { cx[s3] = fmul(w.w, q.x); cy[s3] = fmul(w.w, q.y); cz[s3] = fmul(w.w, q.z); }
+    if (s0 != 0xffffu) { cxy[s0] = make_float2(fmul(w.x, q.x), fmul(w.x, q.y)); cz[s0] = fmul(w.x, q.z); }
+    if (s1 != 0xffffu) { cxy[s1] = make_float2(fmul(w.y, q.x), fmul(w.y, q.y)); cz[s1] = fmul(w.y, q.z); }
+    if (s2 != 0xffffu) { cxy[s2] = make_float2(fmul(w.z, q.x), fmul(w.z, q.y)); cz[s2] = fmul(w.z, q.z); }
+    if (s3 != 0xffffu) { cxy[s3] = make_float2(fmul(w.w, q.x), fmul(w.w, q.y)); cz[s3] = fmul(w.w, q.z); }
 }
 
 // The force on an owned vertex is defined as (sum of the first half of its
@@ -440,12 +442,12 @@ __device__ __forceinline__ void hinge_contrib_vm(const HingeRec& r, uint2 hs, co
 // one that gives the two halves to two threads produces the same bits.
 __device__ __forceinline__ int gather_half(int deg) { return (deg + 1) >> 1; }
 // vertex-major slots: contribution j of vertex l at j*npad + l
-__device__ __forceinline__ float3 gather_vm(int l, int j0, int j1, int npad, const float* cx, const float* cy,
-                                            const float* cz)
+__device__ __forceinline__ float3 gather_vm(int l, int j0, int j1, int npad, const float2* cxy, const float* cz)
 {
     float fx = 0.f, fy = 0.f, fz = 0.f;
     for (int j = j0, s = j0 * npad + l; j < j1; ++j, s += npad) {
-        fx = fadd(fx, cx[s]); fy = fadd(fy, cy[s]); fz = fadd(fz, cz[s]);
+        const float2 v = cxy[s];
+        fx = fadd(fx, v.x); fy = fadd(fy, v.y); fz = fadd(fz, cz[s]);
     }
     return make_float3(fx, fy, fz);
 }
@@ -453,20 +455,20 @@ __device__ __forceinline__ float3 gather_vm(int l, int j0, int j1, int npad, con
 // gather_vm for at most M contributions: every slot load is issued before
 // the additions, which run in the same order (same bits).
 template <int M>
-__device__ __forceinline__ float3 gather_vm_u(int l, int j0, int j1, int npad, const float* cx, const float* cy,
-                                              const float* cz)
+__device__ __forceinline__ float3 gather_vm_u(int l, int j0, int j1, int npad, const float2* cxy, const float* cz)
 {
-    float vx[M], vy[M], vz[M];
+    float2 vxy[M];
+    float vz[M];
     #pragma unroll
     for (int i = 0; i < M; ++i) {
         const bool ok = j0 + i < j1;
         const int s = ok ? (j0 + i) * npad + l : l;   // always inside the slot arrays
-        vx[i] = cx[s]; vy[i] = cy[s]; vz[i] = cz[s];
+        vxy[i] = cxy[s]; vz[i] = cz[s];
     }
     float fx = 0.f, fy = 0.f, fz = 0.f;
     #pragma unroll
     for (int i = 0; i < M; ++i)
-        if (j0 + i < j1) { fx = fadd(fx, vx[i]); fy = fadd(fy, vy[i]); fz = fadd(fz, vz[i]); }
+        if (j0 + i < j1) { fx = fadd(fx, vxy[i].x); fy = fadd(fy, vxy[i].y); fz = fadd(fz, vz[i]); }
     return make_float3(fx, fy, fz);
 }
 
@@ -537,7 +539,7 @@ __device__ __forceinline__ void block_residual(float r2, float* red, double* acc
 // ---------------------------------------------------------------------------
 template <int MODE, int NT>
 __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr& ph, int k, bool res_only,
-                                              float omega, float4* sy, float* cx, float* cy, float* cz,
+                                              float omega, float4* sy, float2* cxy, float* cz,
                                               float* red, const int* skip_s = nullptr,
                                               const float* omega_s = nullptr)
 {
@@ -588,13 +590,13 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
     // 2. local step: cells then lone hinges, contributions to shared slots
     for (int c = tid; c < ncell; c += NT) {
         const CellRec r = cr[c];
-        cell_contrib_vm<MODE>(r, sy, sd, cx, cy, cz);
+        cell_contrib_vm<MODE>(r, sy, sd, cxy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;
     const uint2* __restrict__ hv = a.hvm + ph.hinge_off;
     for (int e = tid; e < nhin; e += NT) {
         const HingeRec r = hr[e];
-        hinge_contrib_vm<MODE>(r, __ldg(&hv[e]), sy, sd, cx, cy, cz);
+        hinge_contrib_vm<MODE>(r, __ldg(&hv[e]), sy, sd, cxy, cz);
     }
     __syncthreads();
 
@@ -607,7 +609,7 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
         const bool first = l == tid;
         const int deg = first ? cp1 - cp0 : __ldg(&cp[l + 1]) - __ldg(&cp[l]);
         const int h = gather_half(deg);
-        const float3 f = fadd3(gather_vm(l, 0, h, npad, cx, cy, cz), gather_vm(l, h, deg, npad, cx, cy, cz));
+        const float3 f = fadd3(gather_vm(l, 0, h, npad, cxy, cz), gather_vm(l, h, deg, npad, cxy, cz));
         const int g = vbegin + l;
         const float4 d = sd[l];
         const float4 y = sy[l];

@@ -70,11 +70,10 @@ __global__ void __launch_bounds__(NT) k_persistent(PersistArgs p)
             __syncthreads();
             if (!skip) {
                 float4* sx = smem;
-                float* cx = reinterpret_cast<float*>(sx + 2 * ph.nlocal);
-                float* cy = cx + ph.vm_nslot;
-                float* cz = cy + ph.vm_nslot;
+                float2* cxy = reinterpret_cast<float2*>(sx + 2 * ph.nlocal);
+                float* cz = reinterpret_cast<float*>(cxy + ph.vm_nslot);
                 process_patch<MODE, NT>(a, ph, k, res_only || k >= a.cinfo[ph.cloth].max_iter, omega,
-                                        sx, cx, cy, cz, red);
+                                        sx, cxy, cz, red);
             }
             __syncthreads();
         }

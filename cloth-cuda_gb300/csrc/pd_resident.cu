@@ -136,11 +136,11 @@ constexpr int kResOmega = 1024;   // Chebyshev weights kept in shared memory
 template <int MODE, int NT>
 __device__ __forceinline__ void local_records(const CellRec* rc, const HingeRec* rh, const uint2* hvs,
                                               const float4* sy, const float4* sd, int ncell, int nhin, int t0, int t1,
-                                              int e0, int e1, float* cx, float* cy, float* cz, bool rev = false)
+                                              int e0, int e1, float2* cxy, float* cz, bool rev = false)
 {
     const int j0 = rev ? NT - 1 - (int)threadIdx.x : (int)threadIdx.x;
-    for (int t = t0 + j0; t < t1; t += NT) cell_contrib_vm_p<MODE>(rc[t], sy, sd, cx, cy, cz);
-    for (int e = e0 + j0; e < e1; e += NT) hinge_contrib_vm<MODE>(rh[e], hvs[e], sy, sd, cx, cy, cz);
+    for (int t = t0 + j0; t < t1; t += NT) cell_contrib_vm_p<MODE>(rc[t], sy, sd, cxy, cz);
+    for (int e = e0 + j0; e < e1; e += NT) hinge_contrib_vm<MODE>(rh[e], hvs[e], sy, sd, cxy, cz);
 }
 
 // Jacobi update of owned vertex l with force f: o = d^(k+1), d = d^k.
@@ -157,12 +157,12 @@ __device__ __forceinline__ void vertex_update_f(float3 f, int l, const float4* s
 // Gather by one thread and update.
 template <int MODE>
 __device__ __forceinline__ void vertex_update(int npad, const int* sptr, int l, const float4* sy,
-                                              const float4* sd, const float* cx, const float* cy, const float* cz,
+                                              const float4* sd, const float2* cxy, const float* cz,
                                               float4 dprev, float gamma, float omega, float4& o, float4& d, float& r2)
 {
     const int deg = sptr[l + 1] - sptr[l], h = gather_half(deg);
-    const float3 f = deg <= 10 ? fadd3(gather_vm_u<5>(l, 0, h, npad, cx, cy, cz), gather_vm_u<5>(l, h, deg, npad, cx, cy, cz))
-                               : fadd3(gather_vm(l, 0, h, npad, cx, cy, cz), gather_vm(l, h, deg, npad, cx, cy, cz));
+    const float3 f = deg <= 10 ? fadd3(gather_vm_u<5>(l, 0, h, npad, cxy, cz), gather_vm_u<5>(l, h, deg, npad, cxy, cz))
+                               : fadd3(gather_vm(l, 0, h, npad, cxy, cz), gather_vm(l, h, deg, npad, cxy, cz));
     vertex_update_f<MODE>(f, l, sy, sd, dprev, gamma, omega, o, d, r2);
 }
 
@@ -236,9 +236,8 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     uint2* hvs = reinterpret_cast<uint2*>(rh + nhin);
     float4* sy = reinterpret_cast<float4*>(hvs + ((nhin + 1) & ~1));
     float4* sd = sy + nlocal;
-    float* cx = reinterpret_cast<float*>(sd + nlocal);
-    float* cy = cx + ph.vm_nslot;
-    float* cz = cy + ph.vm_nslot;
+    float2* cxy = reinterpret_cast<float2*>(sd + nlocal);
+    float* cz = reinterpret_cast<float*>(cxy + ph.vm_nslot);
     int* sptr = reinterpret_cast<int*>(cz + ph.vm_nslot);
     const int npad = ph.vm_npad;
 
@@ -331,7 +330,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // each list), then the boundary vertices, which the neighbouring
             // patches read; the signal warp publishes them while phase B runs.
             if (!skip_k)
-                local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, 0, ph.ncell_a, 0, ph.nhin_a, cx, cy, cz);
+                local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, 0, ph.ncell_a, 0, ph.nhin_a, cxy, cz);
             named_sync(1, NT);
             // The boundary vertices' sums are on the neighbours' critical path:
             // one thread per vertex, every slot load issued before the
@@ -339,7 +338,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // thread joined by a named barrier, the two halves of its
             // definition, was slower once the loads were hoisted.)
             if (!skip_k && tid < ph.nbnd) {
-                vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                vertex_update<MODE>(npad, sptr, tid, sy, sd, cxy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             named_arrive(2, NTT);
@@ -350,11 +349,11 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             // boundary offsets are out, so that it does not compete with the
             // boundary sums the neighbouring patches wait for.
             if (!skip_k)
-                local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, ph.ncell_a, ncell, ph.nhin_a, nhin, cx,
-                                                cy, cz, (ncell - ph.ncell_a) + (nhin - ph.nhin_a) <= 32);
+                local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, ph.ncell_a, ncell, ph.nhin_a, nhin, cxy,
+                                        cz, (ncell - ph.ncell_a) + (nhin - ph.nhin_a) <= 32);
             named_sync(1, NT);
             if (!skip_k && own && tid >= ph.nbnd) {
-                vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                vertex_update<MODE>(npad, sptr, tid, sy, sd, cxy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
             }
             // every record has read d^k: the owned offsets move on
@@ -384,10 +383,10 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = o;
             float r2 = 0.f;
             if (!skip_k) {
-                if (comp) local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, 0, ncell, 0, nhin, cx, cy, cz);
+                if (comp) local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, 0, ncell, 0, nhin, cxy, cz);
                 __syncthreads();
                 if (own) {
-                    vertex_update<MODE>(npad, sptr, tid, sy, sd, cx, cy, cz, dprev, gamma, omega_k, o, d, r2);
+                    vertex_update<MODE>(npad, sptr, tid, sy, sd, cxy, cz, dprev, gamma, omega_k, o, d, r2);
                     if (!res_only) {
                         ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
                         sd[tid] = o;

@@ -261,9 +261,8 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
     const int G = gridDim.x;
     const float4* __restrict__ Dk = (k & 1) ? a.buf[1] : a.buf[0];
     float4* __restrict__ Dn = (k & 1) ? a.buf[0] : a.buf[1];
-    float* cx = reinterpret_cast<float*>(smem_raw + sa.slot_off);
-    float* cy = cx + sa.max_nslot;
-    float* cz = cy + sa.max_nslot;
+    float2* cxy = reinterpret_cast<float2*>(smem_raw + sa.slot_off);
+    float* cz = reinterpret_cast<float*>(cxy + sa.max_nslot);
     const int p0 = blockIdx.x;
     if (p0 >= sa.npatch) return;
 
@@ -357,15 +356,15 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
                 const int c = r * NT + ((r & 1) ? NT - 1 - tid : tid);
                 if (c < ncell) {
                     const CellRec rec = cr[c];
-                    cell_contrib_vm<MODE>(rec, const_cast<float4*>(sy), const_cast<float4*>(sd), cx, cy, cz);
+                    cell_contrib_vm<MODE>(rec, const_cast<float4*>(sy), const_cast<float4*>(sd), cxy, cz);
                 }
             }
             const HingeRec* __restrict__ hr = a.hinges + h.hinge_off;
             const uint2* __restrict__ hv = a.hvm + h.hinge_off;
             for (int e = tid; e < nhin; e += NT) {
                 const HingeRec rec = hr[e];
-                hinge_contrib_vm<MODE>(rec, __ldg(&hv[e]), const_cast<float4*>(sy), const_cast<float4*>(sd), cx,
-                                       cy, cz);
+                hinge_contrib_vm<MODE>(rec, __ldg(&hv[e]), const_cast<float4*>(sy), const_cast<float4*>(sd), cxy,
+                                       cz);
             }
         }
 
@@ -402,8 +401,8 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
                 const int deg = cp[l + 1] - cp[l];
                 const int hh = gather_half(deg);
                 const float3 f =
-                    deg <= 10 ? fadd3(gather_vm_u<5>(l, 0, hh, npad, cx, cy, cz), gather_vm_u<5>(l, hh, deg, npad, cx, cy, cz))
-                              : fadd3(gather_vm(l, 0, hh, npad, cx, cy, cz), gather_vm(l, hh, deg, npad, cx, cy, cz));
+                    deg <= 10 ? fadd3(gather_vm_u<5>(l, 0, hh, npad, cxy, cz), gather_vm_u<5>(l, hh, deg, npad, cxy, cz))
+                              : fadd3(gather_vm(l, 0, hh, npad, cxy, cz), gather_vm(l, hh, deg, npad, cxy, cz));
                 const int g = vbegin + l;
                 const float4 d = sd[l];
                 const float4 y = sy[l];
