@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
                 const int deg = cp[l + 1] - cp[l];
                 const int hh = gather_half(deg);
                 const float3 f =
-                    deg <= 10 ? fadd3(gather_vm_u<5>(l, 0, hh, npad, cxy, cz), gather_vm_u<5>(l, hh, deg, npad, cxy, cz))
+                    deg <= 10 ? fadd3(gather_vm_p<5>(l, 0, hh, npad, cxy, cz), gather_vm_p<5>(l, hh, deg, npad, cxy, cz))
                               : fadd3(gather_vm(l, 0, hh, npad, cxy, cz), gather_vm(l, hh, deg, npad, cxy, cz));
                 const int g = vbegin + l;
                 const float4 d = sd[l];
