@@ -223,7 +223,11 @@ __device__ __forceinline__ void cell_force(const CellRec& r, const float4* sy, c
     const int j1 = r.x12 & 0xffffu, j2 = r.x12 >> 16;
     const float4 y0 = sy[i0], d0 = sd[i0], y1 = sy[i1], d1 = sd[i1];
     const float4 y2 = sy[i2], d2 = sd[i2], y3 = sy[i3], d3 = sd[i3];
-    const float4 yx1 = sy[j1], dx1 = sd[j1], yx2 = sy[j2], dx2 = sd[j2];
+    // an absent outer hinge names c0 as its outer corner: its data are c0's
+    // (same values, two fewer shared loads; the packed form below, used by
+    // the resident kernel, measured slower with this)
+    const float4 yx1 = j1 == i0 ? y0 : sy[j1], dx1 = j1 == i0 ? d0 : sd[j1];
+    const float4 yx2 = j2 == i0 ? y0 : sy[j2], dx2 = j2 == i0 ? d0 : sd[j2];
     const float3 e01 = edge4(y0, d0, y1, d1), e02 = edge4(y0, d0, y2, d2), e03 = edge4(y0, d0, y3, d3);
     const float3 e13 = edge4(y1, d1, y3, d3);
     const float3 ex1 = edge4(y0, d0, yx1, dx1), ex2 = edge4(y0, d0, yx2, dx2);
