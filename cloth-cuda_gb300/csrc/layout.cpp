@@ -641,7 +641,11 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
     // a copy rounded up to 16 bytes never reads past the end
     for (int q = 0; q < 4; ++q) { L.halo.push_back(0); L.csr_ptr.push_back(0); }
     for (int q = 0; q < 8; ++q) L.csr_ent.push_back(0);
-    // neighbour patches: the owners of each patch's halo vertices
+    // neighbour patches: the owners of each patch's halo vertices.  The
+    // relation is symmetric (a record shared by two patches makes each read
+    // the other's vertices), which the resident kernel's exchange relies on:
+    // a patch overwrites its published d^(k-1) only after it has read d^k of
+    // every patch that reads it (checked by check_layout).
     {
         std::vector<int> vpatch(ntot, -1);
         for (int p = 0; p < L.npatch; ++p)
@@ -740,6 +744,12 @@ std::string check_layout(const std::vector<ClothSetup>& cl, const HostLayout& L)
             const int nnb = L.nbr_ptr[p + 1] - L.nbr_ptr[p];
             if (!std::binary_search(nb, nb + nnb, vpatch[g]))
                 return fail("patch %d: owner %d of halo vertex %d is not a neighbour", p, vpatch[g], g);
+        }
+        //    and the neighbour relation is symmetric
+        for (int j = L.nbr_ptr[p]; j < L.nbr_ptr[p + 1]; ++j) {
+            const int q = L.nbr[j];
+            if (q < 0 || q >= L.npatch || !std::binary_search(L.nbr.data() + L.nbr_ptr[q], L.nbr.data() + L.nbr_ptr[q + 1], p))
+                return fail("patch %d: neighbour %d does not list it back", p, q);
         }
         // 4. boundary vertices first: every owned vertex another patch reads
         //    is published with the first nbnd

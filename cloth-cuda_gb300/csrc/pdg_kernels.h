@@ -69,11 +69,12 @@ struct PersistArgs {
     unsigned* bar;       // [0] arrive counter, [1] generation
     int* err;            // set when a grid barrier times out
     long long spin_budget;  // clock64 cycles a barrier may wait
-    // neighbour synchronisation of the resident kernel (fixed sweep counts)
-    const int* nbr_ptr;  // npatch + 1
-    const int* nbr;      // patches owning halo vertices of each patch
-    unsigned long long* pflag;   // per patch: last (frame, sweep) mark completed
-    unsigned long long frame_seq;  // increments every frame
+    // neighbour synchronisation of the resident kernel (fixed sweep counts):
+    // the boundary offsets d^k of every vertex as tagged words, buffer k & 1
+    // at xch[((k & 1) * n + vertex) * 4 + component], each word the value's
+    // bits | (tag0 + k) << 32; tag0 advances by the frame's sweep count
+    unsigned long long* xch;
+    unsigned tag0;
     int nbr_sync;        // 1: sweeps wait for neighbour patches only
     // caller state moved inside the frame launch (resident kernel only): x, v
     // read by the prediction and written by the finalisation, AoS xyz in
@@ -91,8 +92,8 @@ cudaError_t launch_persistent(const PersistArgs& p, int nt, int grid, size_t sme
 int persistent_max_blocks(int mode, int nt, size_t smem, int* per_sm);
 
 // Resident persistent kernel (pd_resident.cu): one patch per block for the
-// whole frame; nt compute threads (480: one block per SM, 224: two) plus a
-// signal warp.  Limit: nown <= nt.  Kernel variant for nt threads (-1: none).
+// whole frame; nt compute threads (480: one block per SM, 224: two) plus one
+// warp.  Limit: nown <= nt.  Kernel variant for nt threads (-1: none).
 int resident_pick(int nt);
 int resident_max_blocks(int mode, int variant, size_t smem);
 // Whether the kernel has an instance that moves the caller's state (PersistArgs

@@ -103,11 +103,13 @@ struct pdg_solver {
     pdg::DevBuf<pdg::ClothRT> crt2;
     pdg::DevBuf<double> acc2;
     pdg::DevBuf<float> mass, omega, stage_x, stage_v;
-    pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr, nbr_ptr, nbr;
+    pdg::DevBuf<int> vcloth, perm_global, perm_local, halo, csr_ptr;
     pdg::DevBuf<int> inv_global;   // caller-order index in the batch -> reordered vertex
     pdg::DevBuf<double> acc;
-    pdg::DevBuf<unsigned long long> pflag;
-    unsigned long long frame_seq = 0;
+    // resident kernel: tagged boundary offsets exchanged between patches
+    // (2 x vertices x 4 words) and the tag base of the next frame
+    pdg::DevBuf<unsigned long long> xch;
+    unsigned long long xch_tag = 0;
     int acc_stride = 1;
     int nbr_sync = 0;
     pdg::DevBuf<pdg::PatchHdr> patches;

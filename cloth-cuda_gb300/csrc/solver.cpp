@@ -66,14 +66,14 @@ int upload_all(pdg_solver* s)
     CK(s->hinges.upload(L.hinges, st));
     CK(s->hvm.upload(L.hvm, st));
     CK(s->cinfo.upload(L.cinfo, st));
-    CK(s->nbr_ptr.upload(L.nbr_ptr, st));
-    CK(s->nbr.upload(L.nbr, st));
     CK(s->crt.alloc(L.ncloth));
     s->acc_stride = L.cap + 4;   // sweeps 0..cap, then r(y) and r(learned start)
     CK(s->acc.alloc((size_t)L.ncloth * s->acc_stride));
     CK(cudaMemsetAsync(s->acc.p, 0, sizeof(double) * (size_t)L.ncloth * s->acc_stride, st));
-    CK(s->pflag.alloc(L.npatch));
-    CK(cudaMemsetAsync(s->pflag.p, 0, sizeof(unsigned long long) * L.npatch, st));
+    if (s->kernel == PDG_KERNEL_RESIDENT) {
+        CK(s->xch.alloc(8 * (size_t)L.ntot));
+        CK(cudaMemsetAsync(s->xch.p, 0, sizeof(unsigned long long) * 8 * (size_t)L.ntot, st));
+    }
     CK(s->X.alloc(L.ntot)); CK(s->V.alloc(L.ntot)); CK(s->Y.alloc(L.ntot));
     CK(s->A.alloc(L.ntot)); CK(s->B.alloc(L.ntot));
     CK(s->stage_x.alloc(3 * (size_t)L.ntot)); CK(s->stage_v.alloc(3 * (size_t)L.ntot));
@@ -108,6 +108,18 @@ IterArgs iter_args(pdg_solver* s)
     return a;
 }
 
+// Resident frames tag the offsets their patches exchange with 32-bit numbers
+// that grow by the frame's sweep count every frame.  Before the numbers would
+// wrap, the exchange buffer is cleared and they start again, so that no word
+// left by an earlier frame carries a tag the current frame waits for.
+cudaError_t reserve_frame_tags(pdg_solver* s, cudaStream_t st)
+{
+    const unsigned long long n = (unsigned long long)(s->L.cap + (s->have_final ? 1 : 0));
+    if (s->kernel != PDG_KERNEL_RESIDENT || s->xch_tag + n <= 0xffffffffULL) return cudaSuccess;
+    s->xch_tag = 0;
+    return cudaMemsetAsync(s->xch.p, 0, sizeof(unsigned long long) * 8 * (size_t)s->L.ntot, st);
+}
+
 PersistArgs persist_args(pdg_solver* s)
 {
     PersistArgs p;
@@ -117,8 +129,9 @@ PersistArgs persist_args(pdg_solver* s)
     p.n = s->L.ntot; p.npatch = s->L.npatch; p.max_iter = s->L.cap; p.have_final = s->have_final;
     p.mode = s->mode; p.bar = s->bar.p; p.err = reinterpret_cast<int*>(s->bar.p + 2);
     p.spin_budget = s->wait_budget;
-    p.nbr_ptr = s->nbr_ptr.p; p.nbr = s->nbr.p; p.pflag = s->pflag.p;
-    p.frame_seq = ++s->frame_seq;
+    p.xch = s->xch.p;
+    p.tag0 = (unsigned)s->xch_tag;
+    s->xch_tag += (unsigned long long)(s->L.cap + (s->have_final ? 1 : 0));
     p.nbr_sync = s->nbr_sync;
     p.in_x = p.in_v = nullptr;
     p.out_x = p.out_v = nullptr;
@@ -305,7 +318,7 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     if ((c0.kernel == PDG_KERNEL_AUTO && !s->any_warm) || c0.kernel == PDG_KERNEL_RESIDENT) {
         // Resident kernel: every patch co-resident, one 512-thread block per
         // SM, or (block_threads = 256) two half-size patches per SM; a block
-        // is rnt compute threads and a signal warp.
+        // is rnt compute threads and one more warp.
         const int rnt = (c0.kernel == PDG_KERNEL_RESIDENT && c0.block_threads == 256) ? 224 : 480;
         const int per_sm = 512 / (rnt + 32);
         int ntot = 0;
@@ -561,7 +574,7 @@ static int take_wait_error(pdg_solver* s)
     CK(cudaMemsetAsync(s->bar.p + 2, 0, sizeof(int), s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return set_error(PDG_ERR_TIMEOUT, "bounded wait ran out (%s)",
-                     e == 1 ? "grid barrier" : e == 2 ? "resident grid barrier" : "neighbour mark");
+                     e == 1 ? "grid barrier" : e == 2 ? "resident grid barrier" : "neighbour exchange");
 }
 
 // Caller state moved by the resident frame launch itself: inputs read by the
@@ -582,6 +595,7 @@ static int enqueue_frames(pdg_solver* s, int nframes, const FrameIO* io)
             // error word stays set until it is reported, and a kernel that
             // finds it set leaves at its first barrier
             CK(cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), s->stream));
+            CK(reserve_frame_tags(s, s->stream));
             PersistArgs p = persist_args(s);
             if (io && f == 0) { p.in_x = io->in_x; p.in_v = io->in_v; }
             if (io && f == nframes - 1) { p.out_x = io->out_x; p.out_v = io->out_v; }
@@ -920,6 +934,7 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
         cudaEventRecord(e[0], st);
         if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
             cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st);
+            reserve_frame_tags(s, st);
             cudaEventRecord(e[0], st);   // the frame's events bracket the launch only
             const PersistArgs p = persist_args(s);
             cudaError_t err = s->kernel == PDG_KERNEL_RESIDENT
