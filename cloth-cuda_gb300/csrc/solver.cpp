@@ -934,12 +934,13 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
         cudaEventRecord(e[0], st);
         if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
             cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st);
-            reserve_frame_tags(s, st);
+            cudaError_t err = reserve_frame_tags(s, st);
             cudaEventRecord(e[0], st);   // the frame's events bracket the launch only
             const PersistArgs p = persist_args(s);
-            cudaError_t err = s->kernel == PDG_KERNEL_RESIDENT
-                                  ? launch_resident(p, s->res_variant, s->persist_grid, L.smem_resident, st)
-                                  : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
+            if (err == cudaSuccess)
+                err = s->kernel == PDG_KERNEL_RESIDENT
+                          ? launch_resident(p, s->res_variant, s->persist_grid, L.smem_resident, st)
+                          : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "persistent launch: %s", cudaGetErrorString(err));
             s->launches += 1;
             cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
@@ -978,6 +979,13 @@ int pdg_solver_set_wait_budget(pdg_solver* s, long long cycles)
     s->wait_budget = cycles;
     // the streaming kernel's budget is a launch argument inside the graph
     if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+    return PDG_OK;
+}
+
+int pdg_solver_set_frame_tag(pdg_solver* s, unsigned long long tag)
+{
+    if (!s || tag > 0xffffffffULL) return set_error(PDG_ERR_ARG, "pdg_solver_set_frame_tag: bad arguments");
+    s->xch_tag = tag;
     return PDG_OK;
 }
 

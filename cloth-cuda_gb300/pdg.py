@@ -413,6 +413,11 @@ class Solver:
         the one-launch-per-frame kernels give up with ERR_TIMEOUT."""
         _check(lib().pdg_solver_set_wait_budget(self.h, C.c_longlong(int(cycles))))
 
+    def set_frame_tag(self, tag):
+        """Test hook: the tag number the next resident frame's neighbour
+        exchange starts from (near 2**32 it takes the clear-and-restart path)."""
+        _check(lib().pdg_solver_set_frame_tag(self.h, C.c_ulonglong(int(tag))))
+
 
 class WarmStart:
     """Learned warm start (mesh message-passing network on the GPU)."""

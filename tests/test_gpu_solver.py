@@ -418,6 +418,26 @@ def test_bounded_waits_run_out_cleanly(pdg, oracle, kernel):
     assert np.array_equal(x, ref.get_state()[0]) and st["status"] == 0
 
 
+def test_resident_exchange_tags_restart_before_they_wrap(pdg, oracle):
+    # the resident kernel's neighbour exchange tags each published offset with
+    # a 32-bit number that grows by the sweep count (17) every frame;
+    # starting 40 below 2^32, the third frame would pass it, so the library
+    # clears the exchange buffer and restarts the numbers.  Every frame must still give
+    # the per-sweep graph solver's bits, and a restart from a low number
+    # after the buffer holds high tags must not read stale words.
+    m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=16, kernel=pdg.KERNEL_GRAPH)
+    ref = pdg.Solver(cfg, m, c)
+    cfg.kernel = pdg.KERNEL_RESIDENT
+    s = pdg.Solver(cfg, m, c)
+    assert s.launch_info()["kernel"] == pdg.KERNEL_RESIDENT
+    s.set_frame_tag(2**32 - 40)
+    for f in range(4):
+        ref.step(1, stats=False)
+        st = s.step(1)[0]
+        assert st["status"] == 0
+        assert np.array_equal(s.get_state()[0], ref.get_state()[0]), f
+
+
 def test_autotuner_picks_a_plan_and_keeps_the_bits(pdg, oracle):
     # every candidate plan computes the same iterates, so the tuned solver
     # must equal the per-sweep graph solver bit for bit; the second creation
