@@ -295,7 +295,27 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
         predict_vertex(g, p.X, p.V, p.aux, p.mass, p.vcloth, a.cinfo, p.warm, p.Y, a.buf[0], a.buf[1]);
         dprev = __ldcg(&a.buf[0][g]);
     }
+    // The frame's exchange tags: tag0 + k for d^k, tag0 from the device word
+    // that the previous frame advanced (so a replayed launch gets new tags).
+    // Before the 32-bit tags would wrap, every block clears its boundary
+    // vertices' words in both buffers and the frame starts again from 0; the
+    // grid barrier below orders the clearing before any neighbour's poll.
+    const int nsweep = p.max_iter + (p.have_final ? 1 : 0);
+    unsigned tag0 = 0;
+    if (p.xch_tag) {
+        const unsigned t = __ldcg(p.xch_tag);
+        if ((unsigned long long)t + (unsigned long long)nsweep <= 0xffffffffULL) {
+            tag0 = t;
+        } else {
+            for (int q = tid; q < 8 * ph.nbnd; q += NTT) {
+                const int l = q >> 3, b = (q >> 2) & 1, w = q & 3;
+                p.xch[((size_t)b * (size_t)p.n + (size_t)(ph.vbegin + l)) * 4 + w] = 0ull;
+            }
+        }
+    }
     if (!grid_barrier_r(p.bar, p.err, p.spin_budget)) return;
+    // every block has read the word: the next frame's base
+    if (p.xch_tag && blockIdx.x == 0 && tid == 0) *p.xch_tag = tag0 + (unsigned)nsweep;
     if (caller_in && own) dprev = __ldcg(&a.buf[0][g]);
     for (int l = tid; l < nlocal; l += NTT) {
         const int gg = l < nown ? ph.vbegin + l : __ldg(&a.halo[ph.halo_off + l - nown]);
@@ -308,7 +328,6 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     __syncthreads();
 
     const float gamma = ci.gamma;
-    const int nsweep = p.max_iter + (p.have_final ? 1 : 0);
     const bool nbr = p.nbr_sync != 0;
     double* acc = a.acc + (size_t)c * a.acc_stride;
     if (nbr && comp) {
@@ -318,7 +337,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 // the neighbours' d^k (written in their sweep k - 1, which
                 // every sweep up to the cloth's cap has): poll the tagged
                 // words of this thread's halo vertices
-                const unsigned tag = p.tag0 + (unsigned)k;
+                const unsigned tag = tag0 + (unsigned)k;
                 const unsigned long long* xb = p.xch + (size_t)(k & 1) * (size_t)p.n * 4;
                 bool ok = true;
                 for (int l = hl0; ok && l < nlocal; l += NT) {
@@ -353,7 +372,7 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 vertex_update<MODE>(npad, sptr, tid, sy, sd, cxy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) {
                     ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
-                    st_tagged(p.xch + ((size_t)((k + 1) & 1) * (size_t)p.n + g) * 4, o, p.tag0 + (unsigned)(k + 1));
+                    st_tagged(p.xch + ((size_t)((k + 1) & 1) * (size_t)p.n + g) * 4, o, tag0 + (unsigned)(k + 1));
                 }
             }
             // Phase B: the remaining records, then the interior vertices.  At

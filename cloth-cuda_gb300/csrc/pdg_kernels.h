@@ -72,9 +72,10 @@ struct PersistArgs {
     // neighbour synchronisation of the resident kernel (fixed sweep counts):
     // the boundary offsets d^k of every vertex as tagged words, buffer k & 1
     // at xch[((k & 1) * n + vertex) * 4 + component], each word the value's
-    // bits | (tag0 + k) << 32; tag0 advances by the frame's sweep count
+    // bits | (tag0 + k) << 32.  tag0 is read from the device word *xch_tag,
+    // which every frame advances by its sweep count (null: no exchange)
     unsigned long long* xch;
-    unsigned tag0;
+    unsigned* xch_tag;
     int nbr_sync;        // 1: sweeps wait for neighbour patches only
     // caller state moved inside the frame launch (resident kernel only): x, v
     // read by the prediction and written by the finalisation, AoS xyz in

@@ -107,9 +107,10 @@ struct pdg_solver {
     pdg::DevBuf<int> inv_global;   // caller-order index in the batch -> reordered vertex
     pdg::DevBuf<double> acc;
     // resident kernel: tagged boundary offsets exchanged between patches
-    // (2 x vertices x 4 words) and the tag base of the next frame
+    // (2 x vertices x 4 words) and the device word holding the next frame's
+    // tag base
     pdg::DevBuf<unsigned long long> xch;
-    unsigned long long xch_tag = 0;
+    pdg::DevBuf<unsigned> xch_tag;
     int acc_stride = 1;
     int nbr_sync = 0;
     pdg::DevBuf<pdg::PatchHdr> patches;

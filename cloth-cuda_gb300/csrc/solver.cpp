@@ -73,6 +73,8 @@ int upload_all(pdg_solver* s)
     if (s->kernel == PDG_KERNEL_RESIDENT) {
         CK(s->xch.alloc(8 * (size_t)L.ntot));
         CK(cudaMemsetAsync(s->xch.p, 0, sizeof(unsigned long long) * 8 * (size_t)L.ntot, st));
+        CK(s->xch_tag.alloc(1));
+        CK(cudaMemsetAsync(s->xch_tag.p, 0, sizeof(unsigned), st));
     }
     CK(s->X.alloc(L.ntot)); CK(s->V.alloc(L.ntot)); CK(s->Y.alloc(L.ntot));
     CK(s->A.alloc(L.ntot)); CK(s->B.alloc(L.ntot));
@@ -108,18 +110,6 @@ IterArgs iter_args(pdg_solver* s)
     return a;
 }
 
-// Resident frames tag the offsets their patches exchange with 32-bit numbers
-// that grow by the frame's sweep count every frame.  Before the numbers would
-// wrap, the exchange buffer is cleared and they start again, so that no word
-// left by an earlier frame carries a tag the current frame waits for.
-cudaError_t reserve_frame_tags(pdg_solver* s, cudaStream_t st)
-{
-    const unsigned long long n = (unsigned long long)(s->L.cap + (s->have_final ? 1 : 0));
-    if (s->kernel != PDG_KERNEL_RESIDENT || s->xch_tag + n <= 0xffffffffULL) return cudaSuccess;
-    s->xch_tag = 0;
-    return cudaMemsetAsync(s->xch.p, 0, sizeof(unsigned long long) * 8 * (size_t)s->L.ntot, st);
-}
-
 PersistArgs persist_args(pdg_solver* s)
 {
     PersistArgs p;
@@ -130,8 +120,7 @@ PersistArgs persist_args(pdg_solver* s)
     p.mode = s->mode; p.bar = s->bar.p; p.err = reinterpret_cast<int*>(s->bar.p + 2);
     p.spin_budget = s->wait_budget;
     p.xch = s->xch.p;
-    p.tag0 = (unsigned)s->xch_tag;
-    s->xch_tag += (unsigned long long)(s->L.cap + (s->have_final ? 1 : 0));
+    p.xch_tag = s->xch_tag.p;
     p.nbr_sync = s->nbr_sync;
     p.in_x = p.in_v = nullptr;
     p.out_x = p.out_v = nullptr;
@@ -595,7 +584,6 @@ static int enqueue_frames(pdg_solver* s, int nframes, const FrameIO* io)
             // error word stays set until it is reported, and a kernel that
             // finds it set leaves at its first barrier
             CK(cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), s->stream));
-            CK(reserve_frame_tags(s, s->stream));
             PersistArgs p = persist_args(s);
             if (io && f == 0) { p.in_x = io->in_x; p.in_v = io->in_v; }
             if (io && f == nframes - 1) { p.out_x = io->out_x; p.out_v = io->out_v; }
@@ -934,13 +922,11 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
         cudaEventRecord(e[0], st);
         if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
             cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st);
-            cudaError_t err = reserve_frame_tags(s, st);
             cudaEventRecord(e[0], st);   // the frame's events bracket the launch only
             const PersistArgs p = persist_args(s);
-            if (err == cudaSuccess)
-                err = s->kernel == PDG_KERNEL_RESIDENT
-                          ? launch_resident(p, s->res_variant, s->persist_grid, L.smem_resident, st)
-                          : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
+            cudaError_t err = s->kernel == PDG_KERNEL_RESIDENT
+                                  ? launch_resident(p, s->res_variant, s->persist_grid, L.smem_resident, st)
+                                  : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "persistent launch: %s", cudaGetErrorString(err));
             s->launches += 1;
             cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
@@ -985,7 +971,10 @@ int pdg_solver_set_wait_budget(pdg_solver* s, long long cycles)
 int pdg_solver_set_frame_tag(pdg_solver* s, unsigned long long tag)
 {
     if (!s || tag > 0xffffffffULL) return set_error(PDG_ERR_ARG, "pdg_solver_set_frame_tag: bad arguments");
-    s->xch_tag = tag;
+    if (!s->xch_tag.p) return PDG_OK;   // not the resident kernel
+    const unsigned t = (unsigned)tag;
+    CK(cudaMemcpyAsync(s->xch_tag.p, &t, sizeof(unsigned), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));   // `t` is a host temporary
     return PDG_OK;
 }
 

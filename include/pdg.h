@@ -282,10 +282,10 @@ int  pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* 
 int  pdg_solver_set_wait_budget(pdg_solver* s, long long cycles);
 /* Test hook for the resident kernel's neighbour exchange: the tag number the
  * next frame starts from.  Each frame's exchanged offsets carry 32-bit tags
- * that grow by the frame's sweep count; before they would pass 2^32 - 1 the
- * library clears its exchange buffer and starts again from 0.  Setting a
- * base near 2^32 makes the next frames take that path.  No effect on the
- * other kernels. */
+ * from a device word that every frame advances by its sweep count; a frame
+ * whose tags would pass 2^32 - 1 first clears its patches' exchange words
+ * and starts again from 0.  Setting a base near 2^32 makes the next frames
+ * take that path.  No effect on the other kernels. */
 int  pdg_solver_set_frame_tag(pdg_solver* s, unsigned long long tag);
 /* Stream the solver works on (a cudaStream_t). */
 int  pdg_solver_stream(const pdg_solver* s, void** stream);

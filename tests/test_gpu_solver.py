@@ -420,11 +420,12 @@ def test_bounded_waits_run_out_cleanly(pdg, oracle, kernel):
 
 def test_resident_exchange_tags_restart_before_they_wrap(pdg, oracle):
     # the resident kernel's neighbour exchange tags each published offset with
-    # a 32-bit number that grows by the sweep count (17) every frame;
-    # starting 40 below 2^32, the third frame would pass it, so the library
-    # clears the exchange buffer and restarts the numbers.  Every frame must still give
-    # the per-sweep graph solver's bits, and a restart from a low number
-    # after the buffer holds high tags must not read stale words.
+    # a 32-bit number from a device word that grows by the frame's sweep
+    # count every frame; starting 40 below 2^32, the third frame's tags would
+    # pass it, so that frame clears its patches' exchange words and restarts
+    # the numbers.  Every frame must still give the per-sweep graph solver's
+    # bits: a restart from a low number after the words hold high tags must
+    # not read stale words.
     m, c, cfg, sc, a = scene(pdg, oracle, n=33, max_iterations=16, kernel=pdg.KERNEL_GRAPH)
     ref = pdg.Solver(cfg, m, c)
     cfg.kernel = pdg.KERNEL_RESIDENT
