@@ -40,7 +40,9 @@ struct pdg_warmstart {
     DevBuf<double> loss;
     float smooth = 0.f;   // weight of the neighbour-difference term of the loss
     int energy = 0;       // 1: that term weighted by the PD system's stiffness per edge
-    int judge = 4;        // sweeps each start runs before the judge compares them
+    // sweeps each start runs before the judge compares them; 1: the starts'
+    // own residuals, which each chain's first sweep evaluates
+    int judge = 1;
     pdg_solver* solver = nullptr;
     ~pdg_warmstart()
     {

@@ -139,7 +139,7 @@ def score(params, args, seeds=2, frames=32, base_seed=500000):
     return float(np.mean(out))
 
 
-def solve_frames(params, cfg_kw, seed, count, frames, n_range, judge=4):
+def solve_frames(params, cfg_kw, seed, count, frames, n_range, judge=1):
     """Per-cloth frame stats of `frames` frames of one held-out batch, and
     the host time of the frames (each step call synchronises)."""
     ms, cs, cfgs, _ = scenes.batch(count, seed=seed, n_range=n_range, **cfg_kw)
@@ -230,7 +230,7 @@ def main():
     ap.add_argument("--val-seeds", type=int, default=64)
     ap.add_argument("--val-frames", type=int, default=8)
     ap.add_argument("--val-tol", type=float, default=1e-2)
-    ap.add_argument("--val-judge", type=int, default=4)
+    ap.add_argument("--val-judge", type=int, default=1)
     ap.add_argument("--out", default="")
     ap.add_argument("--json", default="")
     args = ap.parse_args()

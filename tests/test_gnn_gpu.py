@@ -265,16 +265,17 @@ def test_training_is_bitwise_reproducible(pdg):
 
 def test_committed_learned_start_needs_fewer_sweeps_than_the_inertial_start(pdg):
     # The committed network (cloth-cuda_gb300/warmstart_params.npy), judged
-    # after 4 sweeps, on held-out cloths of the batched distribution (seeds
-    # disjoint from training and validation), solved to relative residual
-    # 3e-2, a tolerance most frames reach within the 200-sweep cap: fewer mean
-    # sweeps than the inertial start on the same frames, never a failed solve.
+    # by the default rule (the two starts' residuals), on held-out cloths of
+    # the batched distribution (seeds disjoint from training and validation),
+    # solved to relative residual 3e-2, a tolerance most frames reach within
+    # the 200-sweep cap: fewer mean sweeps than the inertial start on the same
+    # frames, never a failed solve.
     import train_warmstart as tw
     params = tw.load_params()
     common = dict(max_iterations=200, tolerance=3e-2, kernel=pdg.KERNEL_STREAM, patch_verts=128, block_threads=128)
     rows = {}
     for name, prm, init in (("inertial", None, pdg.INIT_INERTIAL), ("learned", params, pdg.INIT_WARMSTART)):
-        r, _, _ = tw.solve_frames(prm, dict(common, init=init), tw.EVAL_SEED0, 32, 8, (17, 129), judge=4)
+        r, _, _ = tw.solve_frames(prm, dict(common, init=init), tw.EVAL_SEED0, 32, 8, (17, 129))
         rows[name] = r
     si = np.mean([x["iterations"] for x in rows["inertial"]])
     sl = np.mean([x["iterations"] for x in rows["learned"]])
