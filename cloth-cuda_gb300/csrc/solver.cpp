@@ -921,12 +921,13 @@ int pdg_solver_time_frames(pdg_solver* s, int nframes, float* frame_ms, float* s
     for (int f = 0; f < nframes && rc == PDG_OK; ++f) {
         cudaEventRecord(e[0], st);
         if (s->kernel == PDG_KERNEL_PERSISTENT || s->kernel == PDG_KERNEL_RESIDENT) {
-            cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st);
+            cudaError_t err = cudaMemsetAsync(s->bar.p, 0, 2 * sizeof(unsigned), st);
             cudaEventRecord(e[0], st);   // the frame's events bracket the launch only
             const PersistArgs p = persist_args(s);
-            cudaError_t err = s->kernel == PDG_KERNEL_RESIDENT
-                                  ? launch_resident(p, s->res_variant, s->persist_grid, L.smem_resident, st)
-                                  : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
+            if (err == cudaSuccess)
+                err = s->kernel == PDG_KERNEL_RESIDENT
+                          ? launch_resident(p, s->res_variant, s->persist_grid, L.smem_resident, st)
+                          : launch_persistent(p, s->nt, s->persist_grid, L.smem_bytes, st);
             if (err != cudaSuccess) rc = set_error(PDG_ERR_CUDA, "persistent launch: %s", cudaGetErrorString(err));
             s->launches += 1;
             cudaEventRecord(e[1], st); cudaEventRecord(e[2], st);
