@@ -7,8 +7,11 @@
 The committed parameters (cloth-cuda_gb300/warmstart_params.npy) were made by
 
     python cloth-cuda_gb300/train_warmstart.py --trajectories 2000 --frames 64 --batch 32 \\
-        --eval-seeds 128 --eval-frames 16 --eval-tols 3e-2,1e-2,1e-5 --judge 4 \\
+        --val-judge 4 --eval-seeds 128 --eval-frames 16 --eval-tols 3e-2,1e-2,1e-5 --judge 4 \\
         --out cloth-cuda_gb300/warmstart_params.npy --json train.json
+
+(validation then judged after 4 sweeps; the selected checkpoint, the zero decoder, is also the
+best one judged on the start residuals, the default now)
 
 Training data: 2,000 trajectories of 64 frames of cloths drawn from the
 batched-workload distribution (scenes.batch: grid side 17..129, 0.5-2 m,
