@@ -132,6 +132,14 @@ __device__ __forceinline__ bool ld_tagged(const unsigned long long* w, unsigned 
     return true;
 }
 
+// The three words of one vertex, read once (no tag check).
+__device__ __forceinline__ void ld_words(const unsigned long long* w, unsigned long long& a, unsigned long long& b,
+                                         unsigned long long& c)
+{
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(w) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(c) : "l"(w + 2) : "memory");
+}
+
 // Polls one vertex's words until they carry `tag`, bounded by the clock64
 // budget; false on timeout or when another block reported an error.
 __device__ __forceinline__ bool poll_tagged(const unsigned long long* w, unsigned tag, float4& v, int* err,
@@ -217,7 +225,7 @@ __device__ __forceinline__ void compute_residual(float r2, float* red, double* a
 //   (a vote: a failed poll makes every compute thread leave the sweep loop)
 //   -> phase A records -> bar 1 -> update of the boundary vertices (d^(k+1)
 //   to global memory and as tagged words) -> phase B records -> bar 1 ->
-//   interior update.
+//   [first read of the next sweep's halo words] -> interior update.
 // Barrier 1 counts the NT compute threads.  With a tolerance every sweep ends
 // in a grid barrier instead.
 // IO: the instance that also moves the caller's state (p.in_x ... p.out_v);
@@ -332,6 +340,11 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     double* acc = a.acc + (size_t)c * a.acc_stride;
     if (nbr && comp) {
         // ---- compute threads, neighbour synchronisation ----
+        // the words of this thread's first halo vertex for the next sweep, read
+        // ahead while the interior is updated: when they already carry the
+        // tag the top of the next sweep needs no round trip (257x257 sweep
+        // 4.72 -> 4.60 us; read before phase B instead: 4.76 us)
+        unsigned long long pw0 = 0, pw1 = 0, pw2 = 0;
         for (int k = 0; k < nsweep; ++k) {
             if (k > 0 && k <= ci.max_iter) {
                 // the neighbours' d^k (written in their sweep k - 1, which
@@ -343,7 +356,14 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 for (int l = hl0; ok && l < nlocal; l += NT) {
                     const int gg = l == hl0 ? hg0 : __ldg(&a.halo[ph.halo_off + l - nown]);
                     float4 v = sd[l];
-                    ok = poll_tagged(xb + (size_t)gg * 4, tag, v, p.err, p.spin_budget);
+                    if (l == hl0 && (unsigned)(pw0 >> 32) == tag && (unsigned)(pw1 >> 32) == tag &&
+                        (unsigned)(pw2 >> 32) == tag) {
+                        v.x = __uint_as_float((unsigned)pw0);
+                        v.y = __uint_as_float((unsigned)pw1);
+                        v.z = __uint_as_float((unsigned)pw2);
+                    } else {
+                        ok = poll_tagged(xb + (size_t)gg * 4, tag, v, p.err, p.spin_budget);
+                    }
                     sd[l] = v;
                 }
                 if (!named_and(1, NT, ok)) break;   // the grid barrier below reports the error
@@ -385,6 +405,8 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
                 local_records<MODE, NT>(rc, rh, hvs, sy, sd, ncell, nhin, ph.ncell_a, ncell, ph.nhin_a, nhin, cxy,
                                         cz, (ncell - ph.ncell_a) + (nhin - ph.nhin_a) <= 32);
             named_sync(1, NT);
+            if (k + 1 < nsweep && k + 1 <= ci.max_iter && hl0 < nlocal)
+                ld_words(p.xch + ((size_t)((k + 1) & 1) * (size_t)p.n + hg0) * 4, pw0, pw1, pw2);
             if (!skip_k && own && tid >= ph.nbnd) {
                 vertex_update<MODE>(npad, sptr, tid, sy, sd, cxy, cz, dprev, gamma, omega_k, o, d, r2);
                 if (!res_only) ((k & 1) ? a.buf[0] : a.buf[1])[g] = o;
