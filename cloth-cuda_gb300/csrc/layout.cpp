@@ -15,6 +15,15 @@ namespace pdg {
 
 namespace {
 
+// A record that fills a gap before a group boundary: never read by a kernel
+// (they read records c < ncell of their patch); no outputs.
+CellRec pad_cell()
+{
+    CellRec r{};
+    r.vm01 = r.vm23 = r.vm45 = 0xffffffffu;
+    return r;
+}
+
 uint32_t spread10(uint32_t v)
 {
     v &= 0x3ffu;
@@ -516,6 +525,8 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
             ph.nown = nown;
             ph.nlocal = nlocal;
             ph.halo_off = (int)L.halo.size();
+            // records of every patch start on a group boundary (device format)
+            while (L.cells.size() % kCellGroup) L.cells.push_back(pad_cell());
             ph.cell_off = (int)L.cells.size();
             ph.ncell = ncell;
             ph.hinge_off = (int)L.hinges.size();
@@ -637,6 +648,7 @@ bool build_layout(const std::vector<ClothSetup>& cl, int patch_verts, HostLayout
         L.cinfo[ci] = info;
         vbase += N;
     }
+    while (L.cells.size() % kCellGroup) L.cells.push_back(pad_cell());
     L.npatch = (int)L.patches.size();
     // a copy rounded up to 16 bytes never reads past the end
     for (int q = 0; q < 4; ++q) { L.halo.push_back(0); L.csr_ptr.push_back(0); }

@@ -391,6 +391,31 @@ __device__ __forceinline__ void cell_force_p(const CellRec& r, const float4* sy,
     o[5] = f3(vscale(q2, r.wx2));
 }
 
+// Record c of the patch whose records start at `base`, in the device format
+// (pdg_layout.h): its nine 16-byte pieces lie kCellGroup pieces apart, so
+// the lanes of a warp that load consecutive records read whole lines.
+__device__ __forceinline__ CellRec load_cell(const CellRec* __restrict__ base, int c)
+{
+    static_assert(sizeof(CellRec) == 9 * 16, "CellRec is nine 16-byte pieces");
+    const uint4* p = reinterpret_cast<const uint4*>(base) + (c / kCellGroup) * (9 * kCellGroup) + (c % kCellGroup);
+    const uint4 q0 = __ldg(p), q1 = __ldg(p + kCellGroup), q2 = __ldg(p + 2 * kCellGroup);
+    const uint4 q3 = __ldg(p + 3 * kCellGroup), q4 = __ldg(p + 4 * kCellGroup), q5 = __ldg(p + 5 * kCellGroup);
+    const uint4 q6 = __ldg(p + 6 * kCellGroup), q7 = __ldg(p + 7 * kCellGroup), q8 = __ldg(p + 8 * kCellGroup);
+    auto f4 = [](uint4 q) {
+        return make_float4(__uint_as_float(q.x), __uint_as_float(q.y), __uint_as_float(q.z), __uint_as_float(q.w));
+    };
+    CellRec r;
+    r.G0 = f4(q0); r.G1 = f4(q1); r.W0 = f4(q2); r.W1 = f4(q3); r.W2 = f4(q4);
+    r.h2wA0 = __uint_as_float(q5.x); r.h2wA1 = __uint_as_float(q5.y);
+    r.h2k0 = __uint_as_float(q5.z); r.nrest0 = __uint_as_float(q5.w);
+    r.h2k1 = __uint_as_float(q6.x); r.nrest1 = __uint_as_float(q6.y);
+    r.wx1 = __uint_as_float(q6.z); r.h2k2 = __uint_as_float(q6.w);
+    r.nrest2 = __uint_as_float(q7.x); r.wx2 = __uint_as_float(q7.y);
+    r.c01 = q7.z; r.c23 = q7.w;
+    r.x12 = q8.x; r.vm01 = q8.y; r.vm23 = q8.z; r.vm45 = q8.w;
+    return r;
+}
+
 // Vertex-major slots (every sweep kernel): the record carries each
 // output's slot address (0xffff for a halo corner or an absent output).  A
 // slot holds its contribution as an (x, y) pair in cxy and z in cz: two
@@ -615,7 +640,7 @@ __device__ __forceinline__ void process_patch(const IterArgs& a, const PatchHdr&
 
     // 2. local step: cells then lone hinges, contributions to shared slots
     for (int c = tid; c < ncell; c += NT) {
-        const CellRec r = cr[c];
+        const CellRec r = load_cell(cr, c);
         cell_contrib_vm<MODE>(r, sy, sd, cxy, cz);
     }
     const HingeRec* __restrict__ hr = a.hinges + ph.hinge_off;

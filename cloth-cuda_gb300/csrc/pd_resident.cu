@@ -270,10 +270,16 @@ __global__ void __launch_bounds__(NT + 32, 512 / (NT + 32)) k_resident(PersistAr
     const int npad = ph.vm_npad;
 
     {
+        // records from the device format (groups of kCellGroup, piece-major),
+        // read in that order, into shared memory record after record
         const uint4* src = reinterpret_cast<const uint4*>(a.cells + ph.cell_off);
         uint4* dst = reinterpret_cast<uint4*>(rc);
-        const int n4 = ncell * (int)(sizeof(CellRec) / 16);
-        for (int q = tid; q < n4; q += NTT) dst[q] = __ldg(&src[q]);
+        const int n4 = (ncell + kCellGroup - 1) / kCellGroup * (9 * kCellGroup);
+        for (int q = tid; q < n4; q += NTT) {
+            const int grp = q / (9 * kCellGroup), r = q - grp * (9 * kCellGroup);
+            const int i = r / kCellGroup, cc = grp * kCellGroup + r % kCellGroup;
+            if (cc < ncell) dst[cc * 9 + i] = __ldg(&src[q]);
+        }
         const uint4* hsrc = reinterpret_cast<const uint4*>(a.hinges + ph.hinge_off);
         uint4* hdst = reinterpret_cast<uint4*>(rh);
         for (int q = tid; q < 2 * nhin; q += NTT) hdst[q] = __ldg(&hsrc[q]);

@@ -142,7 +142,7 @@ __device__ __forceinline__ void issue_patch(const IterArgs& a, const StreamArgs&
         bulk_g2s(stage + sa.o_d, Dk + h.vbegin, b_v, bar);
         bulk_g2s(stage + sa.o_dp, Dn + h.vbegin, b_v, bar);
     }
-    prefetch_l2(a.cells + h.cell_off, sizeof(CellRec) * (size_t)h.ncell);
+    prefetch_l2(a.cells + h.cell_off, sizeof(CellRec) * (size_t)((h.ncell + kCellGroup - 1) / kCellGroup * kCellGroup));
 }
 
 // Thread 0: asynchronous copy of a patch header (80 bytes, 16-byte aligned
@@ -200,7 +200,7 @@ __device__ __forceinline__ void issue_static(const IterArgs& a, const StreamArgs
         bulk_g2s(stage + sa.o_y, a.Y + h.vbegin, b_v, bar);
         bulk_g2s(stage + sa.o_dp, Dn + h.vbegin, b_v, bar);
     }
-    prefetch_l2(a.cells + h.cell_off, sizeof(CellRec) * (size_t)h.ncell);
+    prefetch_l2(a.cells + h.cell_off, sizeof(CellRec) * (size_t)((h.ncell + kCellGroup - 1) / kCellGroup * kCellGroup));
 }
 
 // Thread 0, first patch only: d^k of the owned vertices, completing on `bar`.
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_stream(IterArgs a, StreamArgs 
             for (int r = 0; r * NT < ncell; ++r) {
                 const int c = r * NT + ((r & 1) ? NT - 1 - tid : tid);
                 if (c < ncell) {
-                    const CellRec rec = cr[c];
+                    const CellRec rec = load_cell(cr, c);
                     cell_contrib_vm<MODE>(rec, const_cast<float4*>(sy), const_cast<float4*>(sd), cxy, cz);
                 }
             }

@@ -47,6 +47,14 @@ struct PatchHdr {            // 80 B
 // Absent parts carry zero weights and stiffness: a lone triangle has G1 = 0
 // and c3 = c0.  Outputs o0..o3 are the summed contributions to c0..c3 and
 // o4 / o5 those to x1 / x2.
+// On the device the records of a patch are stored in groups of kCellGroup:
+// 16-byte piece i of record c of a patch at piece index
+// cell_off * 9 + (c / 8) * 72 + i * 8 + c % 8, so that a warp's load of piece
+// i of 32 consecutive records reads four whole 128-byte lines (on the host,
+// L.cells holds them record after record).  Every patch's records start on a
+// multiple of kCellGroup; the layout pads the gaps with unused records.
+constexpr int kCellGroup = 8;
+
 struct CellRec {             // 144 B
     float4   G0, G1;         // Dm_inv of t0, t1, col-major (g00, g10, g01, g11)
     float4   W0, W1, W2;     // weights of c0..c3 in h0, h1, h2

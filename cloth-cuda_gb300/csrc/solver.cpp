@@ -62,7 +62,20 @@ int upload_all(pdg_solver* s)
     CK(s->halo.upload(L.halo, st));
     CK(s->csr_ptr.upload(L.csr_ptr, st));
     CK(s->patches.upload(L.patches, st));
-    CK(s->cells.upload(L.cells, st));
+    {
+        // cell records in the device format: groups of kCellGroup records,
+        // 16-byte piece i of every record of a group together (pdg_layout.h)
+        constexpr int P = (int)(sizeof(CellRec) / 16);
+        std::vector<CellRec> dev(L.cells.size());
+        const uint4* src = reinterpret_cast<const uint4*>(L.cells.data());
+        uint4* dst = reinterpret_cast<uint4*>(dev.data());
+        for (size_t g = 0; g < L.cells.size() / kCellGroup; ++g)
+            for (int j = 0; j < kCellGroup; ++j)
+                for (int i = 0; i < P; ++i)
+                    dst[(g * P + i) * kCellGroup + j] = src[(g * kCellGroup + j) * P + i];
+        CK(s->cells.upload(dev, st));
+        CK(cudaStreamSynchronize(st));   // `dev` is a host temporary
+    }
     CK(s->hinges.upload(L.hinges, st));
     CK(s->hvm.upload(L.hvm, st));
     CK(s->cinfo.upload(L.cinfo, st));
@@ -510,7 +523,8 @@ static int layout_check_impl(int n, const pdg_config* cfgs, const pdg_mesh* cons
             info->boundary_total += h.nbnd;
             info->phase_a_cells += h.ncell_a;
         }
-        info->cells = (long long)L.cells.size();
+        info->cells = 0;
+        for (const PatchHdr& h : L.patches) info->cells += h.ncell;
         info->lone_hinges = (long long)L.hinges.size();
         info->smem_resident = (long long)L.smem_resident;
         if (mistake && !plant_mistake(L, mistake))
