@@ -56,7 +56,10 @@ WORKLOADS = {
     "plain257": dict(kind="plain", n=257, side=2.0, ks=1e3, kb=1e-2, iters=32, tol=0.0),
     "large1025": dict(kind="plain", n=1025, side=4.0, ks=1e4, kb=1e-2, iters=200, tol=1e-6, wind=1.0, learned=True,
                       reach=3e-2),
-    "batch512": dict(kind="batch", count=512, iters=200, tol=1e-5, learned=True, reach=1e-2),
+    # streaming plan of the batch: 256-vertex patches on 256 threads, the
+    # measured best of the plans with power-of-two sizes on this workload
+    # (sweep 167.9 us against 174.0 us at 128/128)
+    "batch512": dict(kind="batch", count=512, iters=200, tol=1e-5, learned=True, reach=1e-2, plan=(256, 256)),
     # profiling case of the streaming sweep: 165 MB per sweep (> 129 MB L2)
     "stream769": dict(kind="plain", n=769, side=3.0, ks=1e4, kb=1e-2, iters=8, tol=0.0, wind=1.0),
 }
@@ -379,8 +382,8 @@ def run_batch(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     wl = WORKLOADS[args.workload]
     kern = args.kernel if args.kernel is not None else pdg.KERNEL_STREAM
-    pv = args.patch_verts or 128
-    bt = args.block_threads or 128
+    pv = args.patch_verts or wl.get("plan", (128, 128))[0]
+    bt = args.block_threads or wl.get("plan", (128, 128))[1]
     common = dict(kernel=kern, patch_verts=pv, block_threads=bt, compute_final_residual=1, smem_carveout=args.carveout)
     if wl["kind"] == "batch":
         count = args.cloths or wl["count"]
