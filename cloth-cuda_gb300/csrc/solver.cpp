@@ -291,13 +291,14 @@ int pdg::create_solver(int n, const pdg_config* cfgs, const pdg_mesh* const* mes
     const pdg_config& c0 = cfgs[0];
     s->mode = c0.mode;
     s->have_final = (c0.mode == PDG_MODE_CONSISTENT) && (c0.compute_final_residual || c0.tolerance > 0.f);
-    // defaults: the streaming kernel's measured best plan (128-vertex patches,
-    // 128 threads); the per-patch graph kernel's, 256 / 256
-    const bool stream_plan = c0.kernel == PDG_KERNEL_AUTO || c0.kernel == PDG_KERNEL_STREAM;
-    s->nt = c0.block_threads ? c0.block_threads : (stream_plan ? 128 : 256);
+    // defaults: 256-vertex patches on 256 threads, the measured best plan of
+    // the streaming kernel (512-cloth batch 167.9 against 174.0 us per sweep
+    // at 128 / 128, 1025x1025 57.3 against 62.6 us) and of the per-patch
+    // graph kernel
+    s->nt = c0.block_threads ? c0.block_threads : 256;
     if (s->nt != 128 && s->nt != 256 && s->nt != 512)
         return set_error(PDG_ERR_ARG, "block_threads must be 128, 256 or 512");
-    s->patch_verts = c0.patch_verts ? c0.patch_verts : (stream_plan ? 128 : 256);
+    s->patch_verts = c0.patch_verts ? c0.patch_verts : 256;
     if (c0.smem_carveout < 0 || c0.smem_carveout > 100) return set_error(PDG_ERR_ARG, "smem_carveout must be in [0, 100]");
     s->carveout = c0.smem_carveout;
     if (s->patch_verts < 16 || s->patch_verts > 4096) return set_error(PDG_ERR_ARG, "patch_verts must be in [16, 4096]");

@@ -506,12 +506,12 @@ def test_stream_sweeps_overlapping_their_predecessor_match_graph(pdg, oracle):
 
 def test_auto_plan_streams_what_the_resident_kernel_cannot_hold(pdg, oracle):
     # 513x513 cloth: more 448-vertex patches than SMs, so AUTO falls back to
-    # the streaming kernel at its default 128-vertex / 128-thread plan
+    # the streaming kernel at its default 256-vertex / 256-thread plan
     m, c, cfg, sc, a = scene(pdg, oracle, n=513, side=2.0, max_iterations=8, kernel=pdg.KERNEL_AUTO)
     s = pdg.Solver(cfg, m, c)
     info = s.launch_info()
     assert info["kernel"] == pdg.KERNEL_STREAM
-    assert (info["patch_verts"], info["block_threads"]) == (128, 128)
+    assert (info["patch_verts"], info["block_threads"]) == (256, 256)
     cfg.kernel = pdg.KERNEL_GRAPH
     g = pdg.Solver(cfg, m, c)
     s.step(1, stats=False); g.step(1, stats=False)
