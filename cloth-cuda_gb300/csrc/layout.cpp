@@ -768,9 +768,16 @@ std::string check_layout(const std::vector<ClothSetup>& cl, const HostLayout& L)
         for (int l = h.nbnd; l < h.nown; ++l)
             if (in_halo[h.vbegin + l]) return fail("patch %d: owned vertex %d is read by another patch but not among "
                                                    "the first %d", p, l, h.nbnd);
-        // 5. the records: local indices in range, and every owned vertex's
-        //    contributions j < deg written to slot j*npad + l exactly once,
-        //    by phase-A records (the prefix) if the vertex is a boundary one
+        // 5. the records: the patch's records start on a group boundary and
+        //    lie inside the record array (the device format groups them by
+        //    kCellGroup), local indices are in range, and every owned vertex's
+        //    contributions j < deg are written to slot j*npad + l exactly
+        //    once, by phase-A records (the prefix) if the vertex is a
+        //    boundary one
+        if (h.cell_off % kCellGroup != 0 || h.cell_off < 0 || h.ncell < 0 ||
+            (size_t)h.cell_off + (size_t)(h.ncell + kCellGroup - 1) / kCellGroup * kCellGroup > L.cells.size())
+            return fail("patch %d: records [%d, +%d) not group-aligned inside the record array", p, h.cell_off,
+                        h.ncell);
         const int npad = h.vm_npad;
         if (npad < h.nown) return fail("patch %d: slot stride %d below %d owned vertices", p, npad, h.nown);
         const int* ptr = L.csr_ptr.data() + h.csr_off;
